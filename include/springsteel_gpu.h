@@ -1,0 +1,185 @@
+/*
+ * springsteel_gpu.h — C ABI of the GB300 transform backend for Springsteel.jl
+ * RL / RLZ cylindrical grids.
+ *
+ * The library owns every device buffer of a grid: the physical array
+ * (np × nvars × nslots, column-major, exactly the reference's
+ * `grid.physical` layout) and the spectral array (nspec × nvars, the
+ * reference's `grid.spectral` layout).  Both stay resident in HBM between
+ * calls; host copies happen only through the explicit upload/download entry
+ * points.  No C++ exception, torch type or CUDA type crosses this boundary:
+ * streams are passed as `void*` (a cudaStream_t, NULL = the grid's own
+ * stream) and every entry point returns an `int32_t` status code.
+ *
+ * Reference boundary replaced (file:line within Springsteel.jl):
+ *   createGrid                  src/factory.jl:1104-1143 (RL :646-685, RLZ :688-740)
+ *   spectralTransform!(RL)      src/transforms_cylindrical.jl:153-222
+ *   gridTransform!(RL)          src/transforms_cylindrical.jl:254-428
+ *   spectralTransform!(RLZ)     src/transforms_cylindrical.jl:524-618
+ *   gridTransform!(RLZ)         src/transforms_cylindrical.jl:654-853
+ *   applyFilter!                src/filtering.jl:262-428
+ *   _set_wavenumber_ahat!       src/multipatch_registry.jl:45-62
+ *   solve / solve! (Krylov)     src/solver.jl:1002-1009, src/solver_problem.jl:207-222,474-529
+ * A handle is not thread-safe (same contract as Fourier1D, src/Fourier.jl:111-112);
+ * distinct handles may be used from distinct host threads.
+ */
+#ifndef SPRINGSTEEL_GPU_H
+#define SPRINGSTEEL_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SS_ABI_VERSION 1
+
+/* ---- status codes (no exceptions cross the ABI) ------------------------ */
+enum {
+    SS_OK = 0,
+    SS_BAD_ARG = 1,
+    SS_BAD_SHAPE = 2,
+    SS_NOT_SPD = 3,          /* mirrors PosDefException, src/banded_cholesky.jl:175-177 */
+    SS_UNSUPPORTED_BC = 4,   /* mirrors DomainError, src/Chebyshev.jl:1174 */
+    SS_CUDA_ERROR = 5,
+    SS_DEVICE_TIMEOUT = 6,
+    SS_NAN_DETECTED = 7,
+    SS_NOT_CONVERGED = 8,
+    SS_OUT_OF_MEMORY = 9,
+    SS_NO_DEVICE = 10
+};
+
+/* ---- geometry / precision --------------------------------------------- */
+enum { SS_GEOM_RL = 1, SS_GEOM_RLZ = 2 };
+enum {
+    SS_PREC_F64 = 0,         /* every stage in IEEE binary64 */
+    SS_PREC_F32_REFINED = 1  /* binary32 bulk; FP64 factor + one FP64 refinement in SA */
+};
+enum { SS_DTYPE_F64 = 0, SS_DTYPE_F32 = 1 };
+enum { SS_QUAD_GAUSS = 0, SS_QUAD_REGULAR = 1 };
+
+/* ---- boundary conditions ---------------------------------------------- */
+/* Cubic B-spline BC, the GammaBC kinds of src/CubicBSpline.jl:287-291.
+ * alpha/beta carry α1/β1 (rank 1) or α2/β2 (rank 2) of Ooyama (2002) Table 1,
+ * exactly as the reference's BC Dicts do (src/CubicBSpline.jl:41-122,
+ * converted from BoundaryConditions by src/factory.jl:343-375). */
+enum {
+    SS_SBC_R0 = 0,        /* NaturalBC                            */
+    SS_SBC_RANK1 = 1,     /* α1, β1: R1T0 (-4,-1), R1T1 (0,1), R1T2 (2,-1), Robin */
+    SS_SBC_RANK2 = 2,     /* α2, β2: R2T10 (1,-0.5), R2T20 (-1,0)  */
+    SS_SBC_PERIODIC = 3,  /* not supported by the GPU path (dense factor) */
+    SS_SBC_R3 = 4,        /* ZerosBC                              */
+    SS_SBC_R3X = 5        /* FixedBC: R3 fold plus background ahat */
+};
+typedef struct ss_spline_bc {
+    int32_t kind;
+    int32_t _pad;
+    double alpha;
+    double beta;
+} ss_spline_bc;
+
+/* Chebyshev BC kinds of src/Chebyshev.jl:949-963 (_bc_type). */
+enum { SS_CBC_R0 = 0, SS_CBC_R1T0 = 1, SS_CBC_R1T1 = 2 };
+
+/* ---- grid parameters: mirror of SpringsteelGridParameters ------------- */
+/* src/Springsteel.jl:425-465.  Per-variable dictionaries become arrays of
+ * nvars entries (variable v = index v-1 of the reference's vars Dict).    */
+typedef struct ss_grid_params {
+    int32_t geometry;        /* SS_GEOM_RL | SS_GEOM_RLZ                      */
+    int32_t precision;       /* SS_PREC_*                                     */
+    int32_t num_cells;
+    int32_t mubar;           /* default 3                                     */
+    int32_t quadrature;      /* SS_QUAD_GAUSS (mubar 1..5) | SS_QUAD_REGULAR  */
+    int32_t nvars;
+    int32_t kDim;            /* Chebyshev points (RLZ only)                   */
+    int32_t b_kDim;          /* 0 → min(kDim, floor((2kDim-1)/3)+1)          */
+    int32_t patchOffsetL;    /* (spectralIndexL-1)*mubar                      */
+    int32_t _pad0;
+    double iMin, iMax;
+    double kMin, kMax;
+    const double *l_q;                 /* nvars entries, NULL → 2.0             */
+    const ss_spline_bc *BCL;           /* nvars entries, NULL → R0              */
+    const ss_spline_bc *BCR;           /* nvars entries, NULL → R0              */
+    const int32_t *BCB;                /* nvars entries, NULL → SS_CBC_R0       */
+    const int32_t *BCT;                /* nvars entries, NULL → SS_CBC_R0       */
+    const int32_t *max_wavenumber;     /* nvars entries, NULL → -1 (ring kmax = ri).
+                                          RLZ rings are shared by all variables
+                                          (src/factory.jl:730-738): entry 0 is used. */
+} ss_grid_params;
+
+/* Derived dimensions (src/factory.jl:153-175, 290-298, 658-661, 700-706). */
+typedef struct ss_dims {
+    int64_t iDim;            /* num_cells*mubar                               */
+    int64_t b_iDim;          /* num_cells+3                                   */
+    int64_t jDim;            /* Σ_r (4+4 ri)                                  */
+    int64_t b_jDim;          /* Σ_r (1+2 ri)                                  */
+    int64_t kDim;            /* Chebyshev points (1 for RL)                   */
+    int64_t b_kDim;          /* Chebyshev modes (1 for RL)                    */
+    int64_t kDim_wn;         /* iDim+patchOffsetL: largest wavenumber         */
+    int64_t nvars;
+    int64_t nslots;          /* 5 (RL) or 7 (RLZ) derivative slots           */
+    int64_t n_physical;      /* rows of physical: jDim (RL), kDim*jDim (RLZ) */
+    int64_t n_spectral;      /* rows of spectral: b_kDim*b_iDim*(1+2 kDim_wn) */
+    int64_t n_blocks;        /* spectral blocks of b_iDim rows per variable   */
+} ss_dims;
+
+typedef struct ss_grid ss_grid;
+
+/* ---- library ----------------------------------------------------------- */
+int32_t ss_version(void);
+/* Message of the last failing call on this host thread (never NULL). */
+const char *ss_last_error_string(void);
+
+/* createGrid (src/factory.jl:1104-1143): builds the FP64 spline templates
+ * (P+Q fold and banded Cholesky factor, src/CubicBSpline.jl:733-783 and
+ * src/banded_cholesky.jl:99-197), ring/column tables, and allocates the
+ * device-resident physical and spectral arrays, zero-filled. */
+int32_t ss_grid_create(const ss_grid_params *params, ss_grid **out);
+int32_t ss_grid_destroy(ss_grid *grid);
+int32_t ss_grid_dims(const ss_grid *grid, ss_dims *out);
+/* The grid's own CUDA stream (cudaStream_t), for callers that time or order work. */
+int32_t ss_grid_stream(const ss_grid *grid, void **stream_out);
+/* Device pointers of grid.physical / grid.spectral (element type: F64 for
+ * SS_PREC_F64, F32 for SS_PREC_F32_REFINED). Owned by the grid. */
+int32_t ss_grid_device_physical(ss_grid *grid, void **dptr);
+int32_t ss_grid_device_spectral(ss_grid *grid, void **dptr);
+
+/* Host ↔ device copies.  `host` is borrowed for the call only; `dtype` is the
+ * host element type (converted on the device when it differs from the grid's).
+ * slot = 1..nslots copies one derivative slot (np × nvars); slot = 0 copies
+ * the whole physical array.  The copy is ordered on `stream`; the call
+ * returns after the host buffer may be reused (it synchronizes the stream). */
+int32_t ss_upload_physical(ss_grid *grid, const void *host, int32_t dtype,
+                           int32_t slot, void *stream);
+int32_t ss_download_physical(ss_grid *grid, void *host, int32_t dtype,
+                             int32_t slot, void *stream);
+int32_t ss_upload_spectral(ss_grid *grid, const void *host, int32_t dtype, void *stream);
+int32_t ss_download_spectral(ss_grid *grid, void *host, int32_t dtype, void *stream);
+
+/* spectralTransform!(grid): physical slot 1 → spectral (B-vectors), then the
+ * spectral filter epilogue (applyFilter!).  Asynchronous on `stream`. */
+int32_t ss_spectral_transform(ss_grid *grid, void *stream);
+/* gridTransform!(grid): spectral → all physical slots
+ * (RL: f, ∂r, ∂rr, ∂λ, ∂λλ; RLZ adds ∂z, ∂zz).  Asynchronous on `stream`. */
+int32_t ss_grid_transform(ss_grid *grid, void *stream);
+
+/* Spectral filter weights (applyFilter!, src/filtering.jl:262-428): the host
+ * evaluates the reference's _filter_weight per wavenumber (kDim_wn+1 values)
+ * and per Chebyshev mode (b_kDim values); NULL clears that filter. */
+int32_t ss_grid_set_filter(ss_grid *grid, int32_t var, const double *fourier_w,
+                           const double *chebyshev_w);
+
+/* Per-wavenumber R3X background coefficients (src/multipatch_registry.jl:45-62).
+ * `block` is the spectral block index (0 = k0, 2k-1 = k real, 2k = k imag,
+ * plus z_b*(1+2 kDim_wn) for RLZ); ahat has b_iDim entries.  A grid without
+ * any registered ahat uses zeros, as the reference does. */
+int32_t ss_grid_set_ahat(ss_grid *grid, int32_t var, int32_t block, const double *ahat);
+int32_t ss_grid_clear_ahat(ss_grid *grid);
+
+int32_t ss_grid_synchronize(ss_grid *grid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPRINGSTEEL_GPU_H */

@@ -1,0 +1,351 @@
+"""ctypes wrapper of the FP64 CPU oracle (test infrastructure only).
+
+The oracle restates Springsteel.jl's RL/RLZ transform path in C (see
+``ss_oracle.c`` for the file:line of each restated function).  Only the test
+suite, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use it.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+_PKG = os.path.join(ROOT, "springsteel.jl_gb300")
+if _PKG not in sys.path:
+    sys.path.insert(0, _PKG)
+
+from springsteel_gpu import abi  # noqa: E402
+
+sys.path.insert(0, HERE)
+import build as _oracle_build  # noqa: E402
+
+sys.path.remove(HERE)
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _oracle_build.build()
+        L = C.CDLL(path)
+        vp, i32, d = C.c_void_p, C.c_int32, C.c_double
+        sig = {
+            "or_last_error": ([], C.c_char_p),
+            "or_set_threads": ([C.c_int], None),
+            "or_grid_create": ([C.POINTER(abi.ss_grid_params), C.POINTER(vp)], i32),
+            "or_grid_destroy": ([vp], None),
+            "or_grid_dims": ([vp, C.POINTER(abi.ss_dims)], i32),
+            "or_spectral_transform": ([vp, vp, vp], i32),
+            "or_grid_transform": ([vp, vp, vp], i32),
+            "or_grid_set_ahat": ([vp, i32, i32, vp], i32),
+            "or_grid_set_filter": ([vp, i32, vp, vp], i32),
+            "or_grid_points": ([vp, vp], i32),
+            "or_grid_radial_points": ([vp, vp], i32),
+            "or_grid_ring_points": ([vp, i32, vp], i32),
+            "or_grid_column_points": ([vp, vp], i32),
+            "or_grid_factor": ([vp, i32, vp, C.POINTER(i32)], i32),
+            "or_spline_create": ([d, d, i32, i32, i32, d, C.POINTER(abi.ss_spline_bc),
+                                  C.POINTER(abi.ss_spline_bc), C.POINTER(vp)], i32),
+            "or_spline_destroy": ([vp], None),
+            "or_spline_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
+            "or_basis": ([vp, i32, d, i32], d),
+            "or_spline_mish": ([vp, vp], i32),
+            "or_spline_sb": ([vp, vp, vp], i32),
+            "or_spline_sa": ([vp, vp, vp, vp], i32),
+            "or_spline_si": ([vp, vp, i32, vp], i32),
+            "or_spline_si_points": ([vp, vp, vp, i32, i32, vp], i32),
+            "or_spline_gamma_dense": ([vp, vp], i32),
+            "or_spline_pq_dense": ([vp, vp], i32),
+            "or_spline_set_ahat_r3x": ([vp, d, d, d, i32, vp], i32),
+            "or_band_chol": ([vp, i32, vp], i32),
+            "or_band_solve": ([vp, i32, vp, vp], i32),
+            "or_r2hc": ([vp, i32, vp], i32),
+            "or_hc2r": ([vp, i32, vp], i32),
+            "or_fourier_fb": ([i32, i32, i32, d, vp, vp], i32),
+            "or_fourier_fa": ([i32, i32, i32, d, vp, vp], i32),
+            "or_fourier_fi": ([i32, i32, vp, i32, vp], i32),
+            "or_redft00": ([vp, i32, vp], i32),
+            "or_cheb_cb": ([i32, i32, vp, vp], i32),
+            "or_cheb_gamma": ([i32, i32, i32, vp, C.POINTER(i32)], i32),
+            "or_cheb_ca": ([i32, i32, i32, i32, vp, vp], i32),
+            "or_cheb_ci": ([i32, d, d, vp, i32, vp], i32),
+            "or_cheb_mish": ([i32, d, d, vp], i32),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def _check(st):
+    if st != 0:
+        raise OracleError(st, lib().or_last_error().decode())
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def set_threads(n):
+    lib().or_set_threads(int(n))
+
+
+class OracleGrid:
+    """FP64 CPU grid with the reference's physical/spectral layouts."""
+
+    def __init__(self, bundle):
+        self._bundle = bundle
+        h = C.c_void_p()
+        _check(lib().or_grid_create(bundle.ref, C.byref(h)))
+        self.h = h
+        d = abi.ss_dims()
+        _check(lib().or_grid_dims(h, C.byref(d)))
+        self.dims = d.as_dict()
+
+    def close(self):
+        if self.h:
+            lib().or_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def physical_shape(self):
+        d = self.dims
+        return (d["n_physical"], d["nvars"], d["nslots"])
+
+    @property
+    def spectral_shape(self):
+        d = self.dims
+        return (d["n_spectral"], d["nvars"])
+
+    def spectral_transform(self, physical):
+        """physical: array (n_physical, nvars[, nslots]) in column-major meaning
+        (numpy order='F'); only slot 1 is read.  Returns spectral (n_spectral, nvars)."""
+        ph = np.asfortranarray(physical, dtype=np.float64)
+        spec = np.zeros(self.spectral_shape, dtype=np.float64, order="F")
+        _check(lib().or_spectral_transform(self.h, _ptr(ph), _ptr(spec)))
+        return spec
+
+    def grid_transform(self, spectral):
+        sp = np.asfortranarray(spectral, dtype=np.float64)
+        ph = np.zeros(self.physical_shape, dtype=np.float64, order="F")
+        _check(lib().or_grid_transform(self.h, _ptr(sp), _ptr(ph)))
+        return ph
+
+    def set_ahat(self, var, block, ahat):
+        a = _f64(ahat)
+        _check(lib().or_grid_set_ahat(self.h, int(var), int(block), _ptr(a)))
+
+    def set_filter(self, var, fourier_w=None, chebyshev_w=None):
+        fw = _f64(fourier_w) if fourier_w is not None else None
+        cw = _f64(chebyshev_w) if chebyshev_w is not None else None
+        _check(lib().or_grid_set_filter(self.h, int(var), _ptr(fw) if fw is not None else None,
+                                        _ptr(cw) if cw is not None else None))
+
+    def gridpoints(self):
+        ncol = 3 if self.dims["b_kDim"] > 1 or self.dims["kDim"] > 1 else 2
+        out = np.zeros((self.dims["n_physical"], ncol), order="F")
+        _check(lib().or_grid_points(self.h, _ptr(out)))
+        return out
+
+    def radial_points(self):
+        out = np.zeros(self.dims["iDim"])
+        _check(lib().or_grid_radial_points(self.h, _ptr(out)))
+        return out
+
+    def ring_points(self, r):
+        out = np.zeros(4 + 4 * (r + self._bundle.params.patchOffsetL))
+        _check(lib().or_grid_ring_points(self.h, int(r), _ptr(out)))
+        return out
+
+    def column_points(self):
+        out = np.zeros(self.dims["kDim"])
+        _check(lib().or_grid_column_points(self.h, _ptr(out)))
+        return out
+
+    def factor(self, var=0):
+        n = C.c_int32()
+        out = np.zeros(4 * (self.dims["b_iDim"]))
+        _check(lib().or_grid_factor(self.h, int(var), _ptr(out), C.byref(n)))
+        return out[: 4 * n.value].reshape(n.value, 4)
+
+
+class OracleSpline:
+    """1-D cubic B-spline (Spline1D) for the basis KATs."""
+
+    def __init__(self, xmin, xmax, num_cells, mubar=3, quadrature=0, l_q=2.0,
+                 bcl=(0, 0.0, 0.0), bcr=(0, 0.0, 0.0)):
+        L, R = abi.ss_spline_bc(), abi.ss_spline_bc()
+        L.kind, L.alpha, L.beta = bcl
+        R.kind, R.alpha, R.beta = bcr
+        h = C.c_void_p()
+        _check(lib().or_spline_create(xmin, xmax, num_cells, mubar, quadrature, l_q,
+                                      C.byref(L), C.byref(R), C.byref(h)))
+        self.h = h
+        b, m, n = C.c_int32(), C.c_int32(), C.c_int32()
+        lib().or_spline_info(h, C.byref(b), C.byref(m), C.byref(n))
+        self.bDim, self.mishDim, self.Minterior = b.value, m.value, n.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_spline_destroy(self.h)
+            self.h = None
+
+    def basis(self, m, x, d=0):
+        return lib().or_basis(self.h, int(m), float(x), int(d))
+
+    def mish(self):
+        x = np.zeros(self.mishDim)
+        lib().or_spline_mish(self.h, _ptr(x))
+        return x
+
+    def sb(self, u):
+        u = _f64(u)
+        b = np.zeros(self.bDim)
+        _check(lib().or_spline_sb(self.h, _ptr(u), _ptr(b)))
+        return b
+
+    def sa(self, b, ahat=None):
+        b = _f64(b)
+        a = np.zeros(self.bDim)
+        ah = _f64(ahat) if ahat is not None else None
+        _check(lib().or_spline_sa(self.h, _ptr(b), _ptr(ah) if ah is not None else None, _ptr(a)))
+        return a
+
+    def si(self, a, d=0, points=None):
+        a = _f64(a)
+        if points is None:
+            u = np.zeros(self.mishDim)
+            _check(lib().or_spline_si(self.h, _ptr(a), int(d), _ptr(u)))
+        else:
+            p = _f64(points)
+            u = np.zeros(len(p))
+            _check(lib().or_spline_si_points(self.h, _ptr(a), _ptr(p), len(p), int(d), _ptr(u)))
+        return u
+
+    def gamma(self):
+        G = np.zeros((self.Minterior, self.bDim), order="F")
+        lib().or_spline_gamma_dense(self.h, _ptr(G))
+        return G
+
+    def pq(self):
+        P = np.zeros((self.bDim, self.bDim), order="F")
+        lib().or_spline_pq_dense(self.h, _ptr(P))
+        return P
+
+    def ahat_r3x(self, u0, u1, u2, side, ahat=None):
+        ah = np.zeros(self.bDim) if ahat is None else _f64(ahat).copy()
+        lib().or_spline_set_ahat_r3x(self.h, u0, u1, u2, 0 if side == "left" else 1, _ptr(ah))
+        return ah
+
+
+def band_chol(A):
+    A = np.asfortranarray(A, dtype=np.float64)
+    n = A.shape[0]
+    L4 = np.zeros(4 * n)
+    _check(lib().or_band_chol(_ptr(A), n, _ptr(L4)))
+    return L4
+
+
+def band_solve(L4, b):
+    b = _f64(b)
+    x = np.zeros_like(b)
+    _check(lib().or_band_solve(_ptr(_f64(L4)), len(b), _ptr(b), _ptr(x)))
+    return x
+
+
+def r2hc(x):
+    x = _f64(x)
+    out = np.zeros_like(x)
+    _check(lib().or_r2hc(_ptr(x), len(x), _ptr(out)))
+    return out
+
+
+def hc2r(x):
+    x = _f64(x)
+    out = np.zeros_like(x)
+    _check(lib().or_hc2r(_ptr(x), len(x), _ptr(out)))
+    return out
+
+
+def redft00(x):
+    x = _f64(x)
+    out = np.zeros_like(x)
+    _check(lib().or_redft00(_ptr(x), len(x), _ptr(out)))
+    return out
+
+
+def fourier_fb(u, kmax, bDim, ymin):
+    u = _f64(u)
+    b = np.zeros(bDim)
+    _check(lib().or_fourier_fb(len(u), kmax, bDim, ymin, _ptr(u), _ptr(b)))
+    return b
+
+
+def fourier_fa(b, yDim, kmax, ymin):
+    b = _f64(b)
+    a = np.zeros(yDim)
+    _check(lib().or_fourier_fa(yDim, kmax, len(b), ymin, _ptr(b), _ptr(a)))
+    return a
+
+
+def fourier_fi(a, kmax, d=0):
+    a = _f64(a)
+    u = np.zeros_like(a)
+    _check(lib().or_fourier_fi(len(a), kmax, _ptr(a), int(d), _ptr(u)))
+    return u
+
+
+def cheb_cb(u, bDim):
+    u = _f64(u)
+    b = np.zeros(bDim)
+    _check(lib().or_cheb_cb(len(u), bDim, _ptr(u), _ptr(b)))
+    return b
+
+
+def cheb_gamma(zDim, bcb, bct):
+    G = np.zeros(zDim * zDim)
+    ism = C.c_int32()
+    _check(lib().or_cheb_gamma(zDim, bcb, bct, _ptr(G), C.byref(ism)))
+    return G.reshape(zDim, zDim, order="F") if ism.value else G[:zDim].copy()
+
+
+def cheb_ca(b, zDim, bcb=0, bct=0):
+    b = _f64(b)
+    a = np.zeros(zDim)
+    _check(lib().or_cheb_ca(zDim, len(b), bcb, bct, _ptr(b), _ptr(a)))
+    return a
+
+
+def cheb_ci(a, zmin, zmax, d=0):
+    a = _f64(a)
+    u = np.zeros_like(a)
+    _check(lib().or_cheb_ci(len(a), zmin, zmax, _ptr(a), int(d), _ptr(u)))
+    return u
+
+
+def cheb_mish(zDim, zmin, zmax):
+    z = np.zeros(zDim)
+    _check(lib().or_cheb_mish(zDim, zmin, zmax, _ptr(z)))
+    return z
