@@ -1,0 +1,609 @@
+// ss_api.cu — the C ABI of libspringsteel_gpu (include/springsteel_gpu.h).
+//
+// An ss_grid is the device-resident counterpart of a SpringsteelGrid of RL or
+// RLZ geometry (src/types.jl:249-256): the physical and spectral arrays stay
+// in HBM; the FP64 tables built by ss_setup.cpp are uploaded once.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ss_internal.h"
+#include "ss_kernels.h"
+
+namespace ss {
+static thread_local std::string g_err;
+void set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+}  // namespace ss
+
+using namespace ss;
+
+struct RingBucket {
+    int offset;   // into the ring list
+    int count;
+    size_t smem_fwd_f64, smem_inv_f64;
+    int max_buf, max_kmax;
+};
+
+struct ss_grid {
+    ss_grid_params p{};
+    std::vector<double> l_q;
+    std::vector<ss_spline_bc> bcl, bcr;
+    std::vector<int32_t> bcb, bct, kmaxv;
+    ss_dims d{};
+    int prec = SS_PREC_F64;
+    size_t esz = 8;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nitems = 0, nslots_z = 0, pOL = 0, rlz = 0;
+    int64_t frows = 0;
+
+    void *phys = nullptr, *spec = nullptr, *C = nullptr, *F = nullptr, *G = nullptr, *H = nullptr;
+    void *stage = nullptr;
+    size_t stage_bytes = 0;
+
+    RingDesc *d_rings = nullptr;
+    int *d_ring_list = nullptr;
+    FftPlan *d_plans = nullptr;
+    double2 *d_pool = nullptr, *d_phase = nullptr;
+    int64_t *d_fofs = nullptr;
+    SplineDev *d_spl = nullptr;
+    ChebDev *d_cheb = nullptr;
+    double *d_ahat = nullptr, *d_fw = nullptr, *d_cw = nullptr;
+    int filtered = 0;
+    std::vector<RingBucket> buckets;
+    std::vector<void *> allocs;
+    std::vector<SplineHost> spl_host;
+};
+
+#define CUDA_TRY(expr)                                                                      \
+    do {                                                                                    \
+        cudaError_t _e = (expr);                                                            \
+        if (_e != cudaSuccess) {                                                            \
+            set_error("%s failed: %s", #expr, cudaGetErrorString(_e));                      \
+            return (_e == cudaErrorMemoryAllocation) ? SS_OUT_OF_MEMORY : SS_CUDA_ERROR;   \
+        }                                                                                   \
+    } while (0)
+
+static int32_t dev_alloc(ss_grid *g, void **p, size_t bytes, bool zero = true) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? SS_OUT_OF_MEMORY : SS_CUDA_ERROR;
+    }
+    g->allocs.push_back(*p);
+    if (zero) CUDA_TRY(cudaMemsetAsync(*p, 0, bytes, g->stream));
+    return SS_OK;
+}
+
+template <typename V>
+static int32_t upload_vec(ss_grid *g, V **dst, const std::vector<V> &src) {
+    int32_t st = dev_alloc(g, (void **)dst, src.size() * sizeof(V), false);
+    if (st) return st;
+    if (!src.empty()) CUDA_TRY(cudaMemcpy(*dst, src.data(), src.size() * sizeof(V), cudaMemcpyHostToDevice));
+    return SS_OK;
+}
+
+static void free_grid(ss_grid *g) {
+    if (!g) return;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    for (void *p : g->allocs) cudaFree(p);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+static int32_t build_grid(ss_grid *g) {
+    const ss_grid_params &p = g->p;
+    const int nv = p.nvars;
+    const int iDim = p.num_cells * p.mubar;
+    g->rlz = p.geometry == SS_GEOM_RLZ;
+    g->pOL = p.patchOffsetL;
+    g->prec = p.precision;
+    g->esz = p.precision == SS_PREC_F64 ? 8 : 4;
+    int kz = 1, bk = 1;
+    if (g->rlz) {
+        kz = p.kDim;
+        if (kz < 2) { set_error("RLZ needs kDim >= 2"); return SS_BAD_SHAPE; }
+        bk = p.b_kDim > 0 ? p.b_kDim : (int)std::min<double>(kz, std::floor((2.0 * kz - 1) / 3.0) + 1);
+        if (bk < 1 || bk > kz) { set_error("b_kDim out of range"); return SS_BAD_SHAPE; }
+    }
+    const int K = iDim + g->pOL;
+    ss_dims &d = g->d;
+    d.iDim = iDim;
+    d.b_iDim = p.num_cells + 3;
+    d.kDim = kz;
+    d.b_kDim = bk;
+    d.kDim_wn = K;
+    d.nvars = nv;
+    d.nslots = g->rlz ? 7 : 5;
+    int64_t jDim = 0, bj = 0;
+    for (int r = 1; r <= iDim; r++) { jDim += 4 + 4 * (r + g->pOL); bj += 1 + 2 * (r + g->pOL); }
+    d.jDim = jDim;
+    d.b_jDim = bj;
+    d.n_physical = jDim * kz;
+    d.n_blocks = (int64_t)bk * (1 + 2 * (int64_t)K);
+    d.n_spectral = d.n_blocks * d.b_iDim;
+    g->nitems = nv * bk;
+    g->nslots_z = 1 + 2 * K;
+    g->frows = bj;
+
+    // ---- spline templates (one per variable; src/factory.jl:670-680)
+    g->spl_host.resize(nv);
+    std::vector<SplineDev> sdev(nv);
+    for (int v = 0; v < nv; v++) {
+        int32_t st = build_spline(p.iMin, p.iMax, p.num_cells, p.mubar, p.quadrature, g->l_q[v], g->bcl[v], g->bcr[v],
+                                  g->spl_host[v]);
+        if (st) return st;
+        const SplineHost &sh = g->spl_host[v];
+        SplineDev &sd = sdev[v];
+        std::memset(&sd, 0, sizeof sd);
+        sd.bDim = sh.bDim; sd.Min = sh.Min; sd.rankL = sh.rankL; sd.rankR = sh.rankR;
+        sd.lk = sh.lk; sd.rk = sh.rk; sd.r3x = sh.r3x;
+        sd.aL = sh.aL; sd.bL = sh.bL; sd.aR = sh.aR; sd.bR = sh.bR;
+        std::vector<double> dinv(sh.Min);
+        for (int i = 0; i < sh.Min; i++) dinv[i] = 1.0 / sh.L4[size_t(i) * 4];
+        if ((st = upload_vec(g, &sd.L4, sh.L4))) return st;
+        if ((st = upload_vec(g, &sd.dinv, dinv))) return st;
+        if ((st = upload_vec(g, &sd.PQb, sh.PQb))) return st;
+        if ((st = upload_vec(g, &sd.sbw, sh.sbw))) return st;
+        if ((st = upload_vec(g, &sd.siw, sh.siw))) return st;
+        if ((st = upload_vec(g, &sd.si_m0, sh.si_m0))) return st;
+    }
+    int32_t st = upload_vec(g, &g->d_spl, sdev);
+    if (st) return st;
+
+    // ---- rings (src/factory.jl:608-624) and FFT plans
+    TwiddlePool pool;
+    PlanSet plans;
+    std::vector<double> phase;
+    const int nring_sets = g->rlz ? 1 : nv;
+    std::vector<RingDesc> rings(size_t(nring_sets) * iDim);
+    std::vector<int64_t> fofs(iDim);
+    for (int set = 0; set < nring_sets; set++) {
+        int64_t jo = 0, fo = 0;
+        for (int r = 1; r <= iDim; r++) {
+            RingDesc &rd = rings[size_t(set) * iDim + (r - 1)];
+            const int ri = r + g->pOL;
+            rd.L = 4 + 4 * ri;
+            rd.ri = ri;
+            int kmax = ri;
+            const int var_kmax = g->kmaxv[g->rlz ? 0 : set];
+            if (var_kmax >= 0) kmax = std::min(var_kmax, ri);
+            rd.kmax = kmax;
+            rd.plan = plans.plan_for(rd.L / 2, pool);
+            rd.utw = plans.unpack_for(rd.L, pool);
+            // PhaseFilter(fp): cos(k*ymin), sin(k*ymin) with ymin = 0.5*(2π/L)*(ri-1)
+            const double dl = 2 * 3.14159265358979323846 / rd.L;
+            const double ymin = 0.5 * dl * (ri - 1);
+            rd.phase = (int64_t)phase.size() / 2;
+            for (int k = 1; k <= kmax; k++) {
+                phase.push_back(std::cos(k * ymin));
+                phase.push_back(std::sin(k * ymin));
+            }
+            rd.jofs = jo;
+            rd.fofs = fo;
+            fofs[r - 1] = fo;
+            jo += rd.L;
+            fo += 1 + 2 * ri;
+        }
+    }
+    if (phase.empty()) phase.assign(2, 0.0);
+    if ((st = upload_vec(g, &g->d_rings, rings))) return st;
+    if ((st = upload_vec(g, &g->d_fofs, fofs))) return st;
+    if ((st = upload_vec(g, &g->d_plans, plans.plans))) return st;
+    {
+        std::vector<double2> pv(pool.v.size() / 2);
+        for (size_t i = 0; i < pv.size(); i++) pv[i] = make_double2(pool.v[2 * i], pool.v[2 * i + 1]);
+        if (pv.empty()) pv.push_back(make_double2(0, 0));
+        if ((st = upload_vec(g, &g->d_pool, pv))) return st;
+        std::vector<double2> ph(phase.size() / 2);
+        for (size_t i = 0; i < ph.size(); i++) ph[i] = make_double2(phase[2 * i], phase[2 * i + 1]);
+        if ((st = upload_vec(g, &g->d_phase, ph))) return st;
+    }
+    // buckets of rings by shared-memory need (largest first)
+    {
+        std::vector<int> order(iDim);
+        for (int r = 0; r < iDim; r++) order[r] = r;
+        auto bufof = [&](int r) { return fft_buffer_len(plans.plans[rings[r].plan]); };
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return bufof(a) > bufof(b); });
+        size_t maxsm = 0;
+        int dev = g->device;
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        int i = 0;
+        while (i < iDim) {
+            RingBucket bkt{};
+            bkt.offset = i;
+            int top = bufof(order[i]);
+            int j = i;
+            while (j < iDim && bufof(order[j]) * 2 > top) j++;
+            bkt.count = j - i;
+            bkt.max_buf = top;
+            int km = 0;
+            for (int q = i; q < j; q++) km = std::max(km, rings[order[q]].kmax);
+            bkt.max_kmax = km;
+            bkt.smem_fwd_f64 = size_t(2) * top * 16;
+            bkt.smem_inv_f64 = (size_t(2) * top + km + 1) * 16;
+            maxsm = std::max(maxsm, bkt.smem_inv_f64 * (g->esz == 8 ? 1 : 2) / 2);
+            g->buckets.push_back(bkt);
+            i = j;
+        }
+        size_t need = 0;
+        for (auto &bkt : g->buckets) need = std::max(need, (g->esz == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2);
+        if (optin > 0 && need > (size_t)optin) {
+            set_error("ring of length %d needs %zu bytes of shared memory (> %d per block)", rings[order[0]].L, need, optin);
+            return SS_BAD_SHAPE;
+        }
+        (void)maxsm;
+        if ((st = upload_vec(g, &g->d_ring_list, order))) return st;
+    }
+
+    // ---- Chebyshev columns (src/factory.jl:722-728)
+    if (g->rlz) {
+        std::vector<ChebDev> cdev(nv);
+        for (int v = 0; v < nv; v++) {
+            ChebHost ch;
+            st = build_cheb(kz, bk, g->bcb[v], g->bct[v], p.kMin, p.kMax, ch);
+            if (st) return st;
+            ChebDev &cd = cdev[v];
+            std::memset(&cd, 0, sizeof cd);
+            cd.N = ch.N; cd.bk = ch.bk; cd.nrank = ch.nrank; cd.half = ch.half; cd.dscale = ch.dscale;
+            if ((st = upload_vec(g, &cd.fwd, ch.fwd))) return st;
+            if ((st = upload_vec(g, &cd.inv_e, ch.inv_e))) return st;
+            if ((st = upload_vec(g, &cd.inv_o, ch.inv_o))) return st;
+            std::vector<double> gu = ch.gu, gv = ch.gv;
+            if (gu.empty()) gu.push_back(0.0);
+            if (gv.empty()) gv.push_back(0.0);
+            if ((st = upload_vec(g, &cd.gu, gu))) return st;
+            if ((st = upload_vec(g, &cd.gv, gv))) return st;
+        }
+        if ((st = upload_vec(g, &g->d_cheb, cdev))) return st;
+    }
+
+    // ---- device arrays
+    const size_t es = g->esz;
+    if ((st = dev_alloc(g, &g->phys, size_t(d.n_physical) * nv * d.nslots * es))) return st;
+    if ((st = dev_alloc(g, &g->spec, size_t(d.n_spectral) * nv * es))) return st;
+    if ((st = dev_alloc(g, &g->F, size_t(g->nitems) * g->frows * es))) return st;
+    if ((st = dev_alloc(g, &g->G, size_t(3) * g->nitems * g->frows * es))) return st;
+    if (g->rlz) {
+        if ((st = dev_alloc(g, &g->C, size_t(nv) * bk * jDim * es))) return st;
+        if ((st = dev_alloc(g, &g->H, size_t(5) * nv * bk * jDim * es))) return st;
+    }
+    {
+        std::vector<double> ones_f(size_t(nv) * (K + 1), 1.0), ones_c(size_t(nv) * bk, 1.0);
+        if ((st = upload_vec(g, &g->d_fw, ones_f))) return st;
+        if ((st = upload_vec(g, &g->d_cw, ones_c))) return st;
+    }
+    fft_init_constants();
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    return SS_OK;
+}
+
+// ---------------------------------------------------------------- launches
+template <typename T>
+static int32_t run_forward(ss_grid *g, cudaStream_t st) {
+    const ss_dims &d = g->d;
+    const int nv = (int)d.nvars, bk = (int)d.b_kDim;
+    if (g->rlz) {
+        ChebLaunch P{};
+        P.in = g->phys; P.out = g->C; P.cheb = g->d_cheb; P.rings = g->d_rings;
+        P.jDim = d.jDim; P.np = d.n_physical; P.iDim = (int)d.iDim; P.bk = bk; P.nvars = nv;
+        const int N = (int)d.kDim, half = (N + 1) / 2;
+        size_t smem = (size_t(64) * N + size_t(bk) * half) * sizeof(T);
+        CUDA_TRY(launch_cheb_forward<T>(P, smem, st));
+    }
+    RingLaunch L{};
+    L.rings = g->d_rings;
+    L.ring_var_stride = g->rlz ? 0 : d.iDim;
+    L.plans = g->d_plans; L.pool = g->d_pool; L.phase = g->d_phase;
+    L.in = g->rlz ? g->C : g->phys;
+    L.out = g->F;
+    L.in_item_stride = d.n_physical;
+    L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
+    L.nitems = g->nitems; L.nvars = nv; L.bk = bk; L.rlz = g->rlz;
+    for (const RingBucket &bkt : g->buckets) {
+        L.ring_list = g->d_ring_list + bkt.offset;
+        size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
+        CUDA_TRY(launch_ring_forward<T>(L, bkt.count, g->nitems, smem, st));
+    }
+    SbLaunch S{};
+    S.F = g->F; S.spec = g->spec; S.spl = g->d_spl; S.fofs = g->d_fofs;
+    S.fw = g->filtered ? g->d_fw : nullptr;
+    S.cw = g->filtered ? g->d_cw : nullptr;
+    S.frows = g->frows; S.nspec = d.n_spectral;
+    S.iDim = (int)d.iDim; S.b = (int)d.b_iDim; S.mubar = g->p.mubar; S.pOL = g->pOL; S.K = (int)d.kDim_wn;
+    S.nslots_z = g->nslots_z; S.bk = bk; S.filtered = g->filtered;
+    CUDA_TRY(launch_sb_project<T>(S, g->nitems, st));
+    return SS_OK;
+}
+
+template <typename T>
+static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
+    const ss_dims &d = g->d;
+    const int nv = (int)d.nvars, bk = (int)d.b_kDim;
+    SaLaunch A{};
+    A.spec = g->spec; A.G = g->G; A.spl = g->d_spl; A.fofs = g->d_fofs; A.ahat = g->d_ahat;
+    A.frows = g->frows; A.nspec = d.n_spectral; A.nblocks = d.n_blocks;
+    A.iDim = (int)d.iDim; A.b = (int)d.b_iDim; A.ld = (A.b % 2) ? A.b : A.b + 1;
+    A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = bk; A.nitems = g->nitems;
+    int nmax = 0;
+    for (auto &sh : g->spl_host) nmax = std::max(nmax, sh.Min);
+    size_t smem = (size_t(32) * A.ld + size_t(5) * nmax) * sizeof(double);
+    CUDA_TRY(launch_sa_si<T>(A, g->nitems, smem, st));
+
+    RingLaunch L{};
+    L.rings = g->d_rings;
+    L.ring_var_stride = g->rlz ? 0 : d.iDim;
+    L.plans = g->d_plans; L.pool = g->d_pool; L.phase = g->d_phase;
+    L.in = g->G;
+    L.out = g->rlz ? g->H : g->phys;
+    L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
+    L.nitems = g->nitems; L.nvars = nv; L.bk = bk; L.rlz = g->rlz;
+    for (const RingBucket &bkt : g->buckets) {
+        L.ring_list = g->d_ring_list + bkt.offset;
+        size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
+        CUDA_TRY(launch_ring_inverse<T>(L, bkt.count, g->nitems, sm, st));
+    }
+    if (g->rlz) {
+        ChebLaunch P{};
+        P.in = g->H; P.out = g->phys; P.cheb = g->d_cheb; P.rings = g->d_rings;
+        P.jDim = d.jDim; P.np = d.n_physical; P.iDim = (int)d.iDim; P.bk = bk; P.nvars = nv;
+        const int N = (int)d.kDim, half = (N + 1) / 2, ne = (N + 1) / 2, no = std::max(N / 2, 1);
+        size_t sm = (size_t(128) * N + size_t(half) * ne + size_t(half) * no + size_t(64) * bk) * sizeof(T);
+        CUDA_TRY(launch_cheb_inverse<T>(P, sm, st));
+    }
+    return SS_OK;
+}
+
+// ---------------------------------------------------------------- helpers
+__global__ void convert_kernel_f64_to_f32(const double *in, float *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+__global__ void convert_kernel_f32_to_f64(const float *in, double *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+static cudaStream_t pick(ss_grid *g, void *s) { return s ? (cudaStream_t)s : g->stream; }
+
+static int32_t ensure_stage(ss_grid *g, size_t bytes) {
+    if (g->stage_bytes >= bytes) return SS_OK;
+    if (g->stage) {
+        cudaStreamSynchronize(g->stream);
+        cudaFree(g->stage);
+        g->allocs.erase(std::remove(g->allocs.begin(), g->allocs.end(), g->stage), g->allocs.end());
+        g->stage = nullptr;
+        g->stage_bytes = 0;
+    }
+    int32_t st = dev_alloc(g, &g->stage, bytes, false);
+    if (st) return st;
+    g->stage_bytes = bytes;
+    return SS_OK;
+}
+
+static int32_t copy_in(ss_grid *g, void *dst, const void *host, int32_t dtype, size_t n, cudaStream_t s) {
+    const size_t hes = dtype == SS_DTYPE_F64 ? 8 : 4;
+    if (hes == g->esz) {
+        CUDA_TRY(cudaMemcpyAsync(dst, host, n * hes, cudaMemcpyHostToDevice, s));
+    } else {
+        int32_t st = ensure_stage(g, n * hes);
+        if (st) return st;
+        CUDA_TRY(cudaMemcpyAsync(g->stage, host, n * hes, cudaMemcpyHostToDevice, s));
+        if (hes == 8) convert_kernel_f64_to_f32<<<1216, 256, 0, s>>>((const double *)g->stage, (float *)dst, n);
+        else convert_kernel_f32_to_f64<<<1216, 256, 0, s>>>((const float *)g->stage, (double *)dst, n);
+        CUDA_TRY(cudaGetLastError());
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return SS_OK;
+}
+
+static int32_t copy_out(ss_grid *g, void *host, const void *src, int32_t dtype, size_t n, cudaStream_t s) {
+    const size_t hes = dtype == SS_DTYPE_F64 ? 8 : 4;
+    if (hes == g->esz) {
+        CUDA_TRY(cudaMemcpyAsync(host, src, n * hes, cudaMemcpyDeviceToHost, s));
+    } else {
+        int32_t st = ensure_stage(g, n * hes);
+        if (st) return st;
+        if (hes == 8) convert_kernel_f32_to_f64<<<1216, 256, 0, s>>>((const float *)src, (double *)g->stage, n);
+        else convert_kernel_f64_to_f32<<<1216, 256, 0, s>>>((const double *)src, (float *)g->stage, n);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(host, g->stage, n * hes, cudaMemcpyDeviceToHost, s));
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return SS_OK;
+}
+
+#define CHECK_GRID(g)                                         \
+    do {                                                      \
+        if (!(g)) { set_error("null grid"); return SS_BAD_ARG; } \
+        cudaSetDevice((g)->device);                           \
+    } while (0)
+
+// ================================================================ C ABI
+extern "C" {
+
+int32_t ss_version(void) { return SS_ABI_VERSION; }
+
+const char *ss_last_error_string(void) { return g_err.c_str(); }
+
+int32_t ss_grid_create(const ss_grid_params *params, ss_grid **out) {
+    if (!out) { set_error("null output pointer"); return SS_BAD_ARG; }
+    *out = nullptr;
+    if (!params) { set_error("null params"); return SS_BAD_ARG; }
+    const ss_grid_params &p = *params;
+    if (p.geometry != SS_GEOM_RL && p.geometry != SS_GEOM_RLZ) { set_error("geometry must be RL or RLZ"); return SS_BAD_ARG; }
+    if (p.precision != SS_PREC_F64 && p.precision != SS_PREC_F32_REFINED) { set_error("unknown precision"); return SS_BAD_ARG; }
+    if (p.nvars < 1 || p.num_cells < 1 || p.mubar < 1 || p.patchOffsetL < 0) { set_error("bad sizes"); return SS_BAD_SHAPE; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device visible");
+        return SS_NO_DEVICE;
+    }
+    ss_grid *g = new ss_grid();
+    g->p = p;
+    const int nv = p.nvars;
+    g->l_q.assign(nv, 2.0);
+    g->bcl.assign(nv, ss_spline_bc{SS_SBC_R0, 0, 0.0, 0.0});
+    g->bcr.assign(nv, ss_spline_bc{SS_SBC_R0, 0, 0.0, 0.0});
+    g->bcb.assign(nv, SS_CBC_R0);
+    g->bct.assign(nv, SS_CBC_R0);
+    g->kmaxv.assign(nv, -1);
+    for (int v = 0; v < nv; v++) {
+        if (p.l_q) g->l_q[v] = p.l_q[v];
+        if (p.BCL) g->bcl[v] = p.BCL[v];
+        if (p.BCR) g->bcr[v] = p.BCR[v];
+        if (p.BCB) g->bcb[v] = p.BCB[v];
+        if (p.BCT) g->bct[v] = p.BCT[v];
+        if (p.max_wavenumber) g->kmaxv[v] = p.max_wavenumber[v];
+    }
+    g->p.l_q = nullptr; g->p.BCL = g->p.BCR = nullptr; g->p.BCB = g->p.BCT = nullptr; g->p.max_wavenumber = nullptr;
+    cudaGetDevice(&g->device);
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        delete g;
+        return SS_CUDA_ERROR;
+    }
+    int32_t st = build_grid(g);
+    if (st) { free_grid(g); return st; }
+    *out = g;
+    return SS_OK;
+}
+
+int32_t ss_grid_destroy(ss_grid *g) {
+    if (!g) return SS_OK;
+    cudaSetDevice(g->device);
+    free_grid(g);
+    return SS_OK;
+}
+
+int32_t ss_grid_dims(const ss_grid *g, ss_dims *out) {
+    if (!g || !out) { set_error("null argument"); return SS_BAD_ARG; }
+    *out = g->d;
+    return SS_OK;
+}
+
+int32_t ss_grid_stream(const ss_grid *g, void **s) {
+    if (!g || !s) { set_error("null argument"); return SS_BAD_ARG; }
+    *s = (void *)g->stream;
+    return SS_OK;
+}
+
+int32_t ss_grid_device_physical(ss_grid *g, void **p) {
+    if (!g || !p) { set_error("null argument"); return SS_BAD_ARG; }
+    *p = g->phys;
+    return SS_OK;
+}
+int32_t ss_grid_device_spectral(ss_grid *g, void **p) {
+    if (!g || !p) { set_error("null argument"); return SS_BAD_ARG; }
+    *p = g->spec;
+    return SS_OK;
+}
+
+int32_t ss_upload_physical(ss_grid *g, const void *host, int32_t dtype, int32_t slot, void *stream) {
+    CHECK_GRID(g);
+    if (!host || (dtype != SS_DTYPE_F64 && dtype != SS_DTYPE_F32)) { set_error("bad host buffer or dtype"); return SS_BAD_ARG; }
+    if (slot < 0 || slot > g->d.nslots) { set_error("slot out of range"); return SS_BAD_ARG; }
+    const size_t per = size_t(g->d.n_physical) * g->d.nvars;
+    char *dst = (char *)g->phys + (slot ? size_t(slot - 1) * per * g->esz : 0);
+    return copy_in(g, dst, host, dtype, slot ? per : per * g->d.nslots, pick(g, stream));
+}
+
+int32_t ss_download_physical(ss_grid *g, void *host, int32_t dtype, int32_t slot, void *stream) {
+    CHECK_GRID(g);
+    if (!host || (dtype != SS_DTYPE_F64 && dtype != SS_DTYPE_F32)) { set_error("bad host buffer or dtype"); return SS_BAD_ARG; }
+    if (slot < 0 || slot > g->d.nslots) { set_error("slot out of range"); return SS_BAD_ARG; }
+    const size_t per = size_t(g->d.n_physical) * g->d.nvars;
+    const char *src = (const char *)g->phys + (slot ? size_t(slot - 1) * per * g->esz : 0);
+    return copy_out(g, host, src, dtype, slot ? per : per * g->d.nslots, pick(g, stream));
+}
+
+int32_t ss_upload_spectral(ss_grid *g, const void *host, int32_t dtype, void *stream) {
+    CHECK_GRID(g);
+    if (!host || (dtype != SS_DTYPE_F64 && dtype != SS_DTYPE_F32)) { set_error("bad host buffer or dtype"); return SS_BAD_ARG; }
+    return copy_in(g, g->spec, host, dtype, size_t(g->d.n_spectral) * g->d.nvars, pick(g, stream));
+}
+
+int32_t ss_download_spectral(ss_grid *g, void *host, int32_t dtype, void *stream) {
+    CHECK_GRID(g);
+    if (!host || (dtype != SS_DTYPE_F64 && dtype != SS_DTYPE_F32)) { set_error("bad host buffer or dtype"); return SS_BAD_ARG; }
+    return copy_out(g, host, g->spec, dtype, size_t(g->d.n_spectral) * g->d.nvars, pick(g, stream));
+}
+
+int32_t ss_spectral_transform(ss_grid *g, void *stream) {
+    CHECK_GRID(g);
+    return g->esz == 8 ? run_forward<double>(g, pick(g, stream)) : run_forward<float>(g, pick(g, stream));
+}
+
+int32_t ss_grid_transform(ss_grid *g, void *stream) {
+    CHECK_GRID(g);
+    return g->esz == 8 ? run_inverse<double>(g, pick(g, stream)) : run_inverse<float>(g, pick(g, stream));
+}
+
+int32_t ss_grid_set_filter(ss_grid *g, int32_t var, const double *fw, const double *cw) {
+    CHECK_GRID(g);
+    if (var < 0 || var >= g->d.nvars) { set_error("var out of range"); return SS_BAD_ARG; }
+    const int K = (int)g->d.kDim_wn, bk = (int)g->d.b_kDim;
+    std::vector<double> f(K + 1, 1.0), c(bk, 1.0);
+    if (fw) std::copy(fw, fw + K + 1, f.begin());
+    if (cw) std::copy(cw, cw + bk, c.begin());
+    CUDA_TRY(cudaMemcpyAsync(g->d_fw + size_t(var) * (K + 1), f.data(), f.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(g->d_cw + size_t(var) * bk, c.data(), c.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    if (fw || cw) g->filtered = 1;
+    return SS_OK;
+}
+
+int32_t ss_grid_set_ahat(ss_grid *g, int32_t var, int32_t block, const double *ahat) {
+    CHECK_GRID(g);
+    if (var < 0 || var >= g->d.nvars || block < 0 || block >= g->d.n_blocks || !ahat) {
+        set_error("ahat index out of range");
+        return SS_BAD_ARG;
+    }
+    const size_t b = g->d.b_iDim;
+    if (!g->d_ahat) {
+        int32_t st = dev_alloc(g, (void **)&g->d_ahat, size_t(g->d.nvars) * g->d.n_blocks * b * 8);
+        if (st) return st;
+    }
+    CUDA_TRY(cudaMemcpyAsync(g->d_ahat + (size_t(var) * g->d.n_blocks + block) * b, ahat, b * 8, cudaMemcpyHostToDevice,
+                             g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    return SS_OK;
+}
+
+int32_t ss_grid_clear_ahat(ss_grid *g) {
+    CHECK_GRID(g);
+    if (g->d_ahat) {
+        CUDA_TRY(cudaStreamSynchronize(g->stream));
+        cudaFree(g->d_ahat);
+        g->allocs.erase(std::remove(g->allocs.begin(), g->allocs.end(), (void *)g->d_ahat), g->allocs.end());
+        g->d_ahat = nullptr;
+    }
+    return SS_OK;
+}
+
+int32_t ss_grid_synchronize(ss_grid *g) {
+    CHECK_GRID(g);
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    CUDA_TRY(cudaGetLastError());
+    return SS_OK;
+}
+
+}  // extern "C"

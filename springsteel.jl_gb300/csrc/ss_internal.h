@@ -1,0 +1,124 @@
+// ss_internal.h — internal structures of the GB300 transform backend.
+//
+// Host-side setup (FP64) lives in ss_setup.cpp; device kernels in
+// ss_kernels.cu; the C ABI in ss_api.cu.  All device tables are built once at
+// ss_grid_create (the analogue of createGrid's template caches,
+// src/CubicBSpline.jl:931-977, src/Fourier.jl:189-204) and stay resident.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "springsteel_gpu.h"
+
+#ifdef __CUDACC__
+#define SS_HD __host__ __device__
+#else
+#define SS_HD
+#endif
+
+namespace ss {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char *fmt, ...);
+struct Status {
+    int32_t code = SS_OK;
+};
+
+// ----------------------------------------------------------- FFT plans
+// Complex DFT of length N evaluated by mixed-radix Stockham passes in
+// shared memory, or (N with a prime factor > 13) by Bluestein's chirp-z
+// convolution of smooth length M >= 2N-1.
+constexpr int kMaxRadices = 24;
+struct FftPlan {
+    int N;
+    int nrad;
+    int rad[kMaxRadices];
+    int64_t tw;      // pool offset of W_N^t, t < N
+    int blu;
+    int M;
+    int mnrad;
+    int mrad[kMaxRadices];
+    int64_t mtw;     // pool offset of W_M^t, t < M
+    int64_t chirp;   // pool offset of exp(-πi k²/N), k < N
+    int64_t filt;    // pool offset of FFT_M(conj chirp filter)/M
+};
+
+// One Fourier ring (src/factory.jl:608-624): L = 4+4ri points, kmax, bDim = 2ri+1.
+struct RingDesc {
+    int L;
+    int ri;
+    int kmax;
+    int plan;          // index of the length-L/2 complex plan
+    int64_t utw;       // pool offset of W_L^t, t < L/2 (real-packing twiddles)
+    int64_t phase;     // offset of cos(k ymin), sin(k ymin) (k = 1..kmax) in the phase pool
+    int64_t jofs;      // Σ_{r'<r} L_r'   (ring start in jDim numbering)
+    int64_t fofs;      // Σ_{r'<r} (1+2ri') (packed coefficient row start)
+};
+
+// Per-variable spline template on the device (FP64 factor, B-spline weights).
+struct SplineDev {
+    int bDim, Min, rankL, rankR, lk, rk, r3x, _pad;
+    double aL, bL, aR, bR;
+    double *L4;      // Min*4: L[j+d][j] at j*4+d   (FP64 banded Cholesky factor)
+    double *dinv;    // Min: 1/L[j][j]
+    double *PQb;     // bDim*7 full P+Q band (R3X only)
+    double *sbw;     // bDim*(4 mubar) SB weights (row mi, tap)
+    double *siw;     // 3*mishDim*4 SI weights (derivative, point, tap)
+    int *si_m0;      // mishDim: first coefficient index of the 4-tap window
+};
+
+// Per-variable Chebyshev column tables (src/Chebyshev.jl).
+struct ChebDev {
+    int N, bk, nrank, half;
+    double dscale;   // -0.5*(zmax - zmin)
+    double *fwd;     // bk × ceil(N/2): folded forward DCT-I rows (scale, filter folded)
+    double *inv_e;   // half_out × ne: inverse DCT-I, even-k columns
+    double *inv_o;   // half_out × no: inverse DCT-I, odd-k columns
+    double *gu;      // nrank × bk   (Γ = Σ u vᵀ restricted to the first bk rows)
+    double *gv;      // nrank × N
+};
+
+enum { BC_R0 = 0, BC_A1 = 1, BC_A2 = 2, BC_PER = 3, BC_R3 = 4 };
+
+// ---------------------------------------------------------- host setup
+struct SplineHost {
+    double xmin, xmax, DX, DXrecip, l_q;
+    int nc, mubar, bDim, mishDim;
+    std::vector<double> qp, qw, mish;
+    int Mdim, Min, rankL, rankR, lk, rk, r3x;
+    double aL, bL, aR, bR;
+    std::vector<double> PQb, L4, sbw, siw;
+    std::vector<int> si_m0;
+};
+int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, double l_q,
+                     const ss_spline_bc &bcl, const ss_spline_bc &bcr, SplineHost &out);
+
+struct ChebHost {
+    int N, bk, nrank, half;
+    double dscale;
+    std::vector<double> fwd, inv_e, inv_o, gu, gv, mish;
+};
+int32_t build_cheb(int N, int bk, int bcb, int bct, double zmin, double zmax, ChebHost &out);
+
+// Pool of complex twiddles (interleaved re, im) in FP64.
+struct TwiddlePool {
+    std::vector<double> v;  // 2 doubles per complex entry
+    int64_t push_table(int n, int sign, int len);   // exp(sign 2πi t/n), t < len
+    int64_t push(const std::vector<double> &cplx_interleaved);
+    int64_t size() const { return (int64_t)v.size() / 2; }
+};
+struct PlanSet {
+    std::vector<FftPlan> plans;
+    std::vector<int> plan_of_N;     // index by N (−1 if absent)
+    std::vector<int64_t> utw_of_L;  // by L
+    std::vector<int64_t> mtw_of_M;  // by M
+    int max_smem_cplx = 0;          // largest complex buffer (N or M)
+    int plan_for(int N, TwiddlePool &pool);
+    int64_t unpack_for(int L, TwiddlePool &pool);
+};
+// complex entries of one ping-pong buffer of a plan
+SS_HD inline int fft_buffer_len(const FftPlan &p) { return p.blu ? p.M : p.N; }
+
+}  // namespace ss

@@ -1,0 +1,469 @@
+// ss_setup.cpp — one-time FP64 host setup of a grid's device tables.
+//
+// This is the createGrid side of the library (src/factory.jl:646-740): the
+// spline template (quadrature, Γ fold, P+Q and its banded Cholesky factor,
+// src/CubicBSpline.jl:172-200, 321-424, 733-783; src/banded_cholesky.jl:99-197),
+// the SB/SI weights (the entries of the reference's _sb_matrix,
+// src/CubicBSpline.jl:1000-1030, and of SItransform's 4-tap window,
+// :1554-1567), the Chebyshev tables (src/Chebyshev.jl:329-378, 991-1177) and
+// the FFT plans/twiddles.  Nothing here runs per transform.
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "ss_internal.h"
+
+namespace ss {
+
+static const double kPi = 3.14159265358979323846264338327950288;
+
+// -------------------------------------------------------------- B-spline
+static int quad_rule(int mb, int quad, std::vector<double> &qp, std::vector<double> &qw) {
+    qp.assign(mb, 0.0);
+    qw.assign(mb, 0.0);
+    if (mb < 1) { set_error("mubar must be >= 1, got %d", mb); return SS_BAD_ARG; }
+    if (quad == SS_QUAD_GAUSS) {
+        double nd[5] = {0}, w[5] = {0};
+        switch (mb) {
+        case 1: nd[0] = 0.0; w[0] = 2.0; break;
+        case 2: nd[0] = -1.0 / std::sqrt(3.0); nd[1] = 1.0 / std::sqrt(3.0); w[0] = w[1] = 1.0; break;
+        case 3:
+            nd[0] = -std::sqrt(3.0 / 5.0); nd[1] = 0.0; nd[2] = std::sqrt(3.0 / 5.0);
+            w[0] = 5.0 / 9.0; w[1] = 8.0 / 9.0; w[2] = 5.0 / 9.0;
+            break;
+        case 4: {
+            double a = std::sqrt(3.0 / 7.0 + 2.0 / 7.0 * std::sqrt(6.0 / 5.0));
+            double b = std::sqrt(3.0 / 7.0 - 2.0 / 7.0 * std::sqrt(6.0 / 5.0));
+            nd[0] = -a; nd[1] = -b; nd[2] = b; nd[3] = a;
+            w[0] = w[3] = (18.0 - std::sqrt(30.0)) / 36.0;
+            w[1] = w[2] = (18.0 + std::sqrt(30.0)) / 36.0;
+            break;
+        }
+        case 5: {
+            double a = std::sqrt(5.0 + 2.0 * std::sqrt(10.0 / 7.0)) / 3.0;
+            double b = std::sqrt(5.0 - 2.0 * std::sqrt(10.0 / 7.0)) / 3.0;
+            nd[0] = -a; nd[1] = -b; nd[2] = 0.0; nd[3] = b; nd[4] = a;
+            w[0] = w[4] = (322.0 - 13.0 * std::sqrt(70.0)) / 900.0;
+            w[1] = w[3] = (322.0 + 13.0 * std::sqrt(70.0)) / 900.0;
+            w[2] = 128.0 / 225.0;
+            break;
+        }
+        default: set_error("Gauss-Legendre quadrature supports mubar 1-5, got %d", mb); return SS_BAD_ARG;
+        }
+        for (int k = 0; k < mb; k++) { qp[k] = (nd[k] + 1.0) / 2.0; qw[k] = w[k] / 2.0; }
+        return SS_OK;
+    }
+    if (quad == SS_QUAD_REGULAR) {
+        for (int k = 1; k <= mb; k++) { qp[k - 1] = double(2 * k - 1) / double(2 * mb); qw[k - 1] = 1.0 / mb; }
+        return SS_OK;
+    }
+    set_error("unknown quadrature %d", quad);
+    return SS_BAD_ARG;
+}
+
+// φ_m^(d)(x), Ooyama (2002) cubic B-spline (same piecewise form as basis(),
+// src/CubicBSpline.jl:585-628)
+static double bspline(const SplineHost &s, int m, double x, int d) {
+    double b = 0.0;
+    double xm = s.xmin + (m * s.DX);
+    double delta = (x - xm) * s.DXrecip;
+    double z = std::fabs(delta);
+    if (z < 2.0) {
+        if (d == 0) {
+            z = 2.0 - z; b = (z * z * z) * (1.0 / 6.0); z -= 1.0;
+            if (z > 0) b -= (z * z * z) * (4.0 / 6.0);
+        } else if (d == 1) {
+            z = 2.0 - z; b = (z * z) * (1.0 / 6.0); z -= 1.0;
+            if (z > 0) b -= (z * z) * (4.0 / 6.0);
+            b *= ((delta > 0) ? -1.0 : 1.0) * 3.0 * s.DXrecip;
+        } else if (d == 2) {
+            z = 2.0 - z; b = z; z -= 1.0;
+            if (z > 0) b -= z * 4;
+            b *= s.DXrecip * s.DXrecip;
+        } else {
+            if (z > 1.0) b = 1.0;
+            else if (z < 1.0) b = -3.0;
+            b *= ((delta > 0) ? -1.0 : 1.0) * s.DXrecip * s.DXrecip * s.DXrecip;
+        }
+    }
+    return b;
+}
+
+// Γ entry (1-based), the structured BC fold of src/CubicBSpline.jl:336-376
+static double gamma_at(const SplineHost &g, int i, int j) {
+    double val = (j == i + g.rankL) ? 1.0 : 0.0;
+    if (g.lk == BC_A1) {
+        if (j == 1) { if (i == 1) val += g.aL; if (i == 2) val += g.bL; }
+    } else if (g.lk == BC_A2) {
+        if (j == 1 && i == 1) val += g.aL;
+        else if (j == 2 && i == 1) val += g.bL;
+    }
+    if (g.rk == BC_A1) {
+        if (j == g.Mdim) { if (i == g.Min) val += g.aR; if (i == g.Min - 1) val += g.bR; }
+    } else if (g.rk == BC_A2) {
+        if (j == g.Mdim && i == g.Min) val += g.aR;
+        else if (j == g.Mdim - 1 && i == g.Min) val += g.bR;
+    }
+    return val;
+}
+
+static int side_bc(const ss_spline_bc &bc, int right, int &rank, int &kind, double &a, double &b, int &r3x) {
+    switch (bc.kind) {
+    case SS_SBC_R0: rank = 0; kind = BC_R0; a = b = 0.0; return SS_OK;
+    case SS_SBC_RANK1: rank = 1; kind = BC_A1; a = bc.alpha; b = bc.beta; return SS_OK;
+    case SS_SBC_RANK2: rank = 2; kind = BC_A2; a = bc.alpha; b = bc.beta; return SS_OK;
+    case SS_SBC_R3: rank = 3; kind = BC_R3; a = b = 0.0; return SS_OK;
+    case SS_SBC_R3X: rank = 3; kind = BC_R3; a = b = 0.0; r3x = 1; return SS_OK;
+    case SS_SBC_PERIODIC:
+        set_error("PERIODIC spline BC (%s) needs a dense factor; not supported by the GPU path",
+                  right ? "BCR" : "BCL");
+        return SS_UNSUPPORTED_BC;
+    default: set_error("unrecognised spline BC kind %d", bc.kind); return SS_UNSUPPORTED_BC;
+    }
+}
+
+int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, double l_q,
+                     const ss_spline_bc &bcl, const ss_spline_bc &bcr, SplineHost &s) {
+    if (nc < 1) { set_error("num_cells must be >= 1"); return SS_BAD_SHAPE; }
+    if (!(xmax > xmin)) { set_error("iMax must exceed iMin"); return SS_BAD_ARG; }
+    s.xmin = xmin; s.xmax = xmax; s.nc = nc; s.mubar = mubar; s.l_q = l_q;
+    s.DX = (xmax - xmin) / nc;
+    s.DXrecip = 1.0 / s.DX;
+    s.bDim = nc + 3;
+    s.mishDim = nc * mubar;
+    int st = quad_rule(mubar, quad, s.qp, s.qw);
+    if (st) return st;
+    s.r3x = 0;
+    st = side_bc(bcl, 0, s.rankL, s.lk, s.aL, s.bL, s.r3x);
+    if (st) return st;
+    st = side_bc(bcr, 1, s.rankR, s.rk, s.aR, s.bR, s.r3x);
+    if (st) return st;
+    s.Mdim = s.bDim;
+    s.Min = s.Mdim - s.rankL - s.rankR;
+    if (s.Min < 2) { set_error("too few interior coefficients (%d) for the banded solve", s.Min); return SS_BAD_SHAPE; }
+    s.mish.resize(s.mishDim);
+    for (int mc = 0; mc < nc; mc++)
+        for (int mu = 0; mu < mubar; mu++) s.mish[mu + mubar * mc] = xmin + mc * s.DX + s.qp[mu] * s.DX;
+
+    // P and Q on the ±3 band (calcPQfactor, src/CubicBSpline.jl:733-783)
+    const int Md = s.Mdim;
+    const double eps_q = std::pow((l_q * s.DX) / (2 * kPi), 6);
+    std::vector<double> P(Md * 7, 0.0), Q(Md * 7, 0.0);
+    for (int mi1 = 1; mi1 <= Md; mi1++)
+        for (int mi2 = std::max(1, mi1 - 3); mi2 <= std::min(Md, mi1 + 3); mi2++) {
+            int m1 = mi1 - 2, m2 = mi2 - 2;
+            for (int mc = 0; mc < nc; mc++) {
+                if (mc < m1 - 2 || mc > m1 + 1 || mc < m2 - 2 || mc > m2 + 1) continue;
+                for (int mu = 0; mu < mubar; mu++) {
+                    double x = xmin + mc * s.DX + s.qp[mu] * s.DX;
+                    double pm1 = bspline(s, m1, x, 0), qm1 = bspline(s, m1, x, 3);
+                    double pm2 = bspline(s, m2, x, 0), qm2 = bspline(s, m2, x, 3);
+                    P[(mi1 - 1) * 7 + (mi2 - mi1 + 3)] += s.DX * s.qw[mu] * pm1 * pm2;
+                    Q[(mi1 - 1) * 7 + (mi2 - mi1 + 3)] += s.DX * s.qw[mu] * eps_q * qm1 * qm2;
+                }
+            }
+        }
+    s.PQb.assign(Md * 7, 0.0);
+    for (int i = 0; i < Md * 7; i++) s.PQb[i] = P[i] + Q[i];
+
+    // open form Γ P Γᵀ + Γ Q Γᵀ on the band, then the banded LLᵀ factor
+    const int n = s.Min;
+    std::vector<double> A(size_t(n) * 4, 0.0);  // A[j*4+d] = Aopen[j+d][j]
+    for (int j = 1; j <= n; j++)
+        for (int i = j; i <= std::min(n, j + 6); i++) {
+            double aP = 0.0, aQ = 0.0;
+            for (int a = std::max(1, i - 3); a <= std::min(Md, i + 3 + s.rankL); a++) {
+                double ga = gamma_at(s, i, a);
+                if (ga == 0.0) continue;
+                for (int b = std::max(1, a - 3); b <= std::min(Md, a + 3); b++) {
+                    double gb = gamma_at(s, j, b);
+                    if (gb == 0.0) continue;
+                    aP += ga * P[(a - 1) * 7 + (b - a + 3)] * gb;
+                    aQ += ga * Q[(a - 1) * 7 + (b - a + 3)] * gb;
+                }
+            }
+            double v = aP + aQ;
+            if (i - j > 3) {
+                if (v != 0.0) { set_error("open-form P+Q exceeds half-bandwidth 3"); return SS_BAD_ARG; }
+            } else {
+                A[size_t(j - 1) * 4 + (i - j)] = v;
+            }
+        }
+    // _band_factor3! (src/banded_cholesky.jl:166-197)
+    for (int j = 0; j < n; j++) {
+        double d = A[j * 4];
+        for (int k = std::max(0, j - 3); k < j; k++) { double l = A[k * 4 + (j - k)]; d -= l * l; }
+        if (d <= 0.0) { set_error("P+Q not positive definite (PosDefException at %d)", j + 1); return SS_NOT_SPD; }
+        double ljj = std::sqrt(d);
+        A[j * 4] = ljj;
+        double inv = 1.0 / ljj;
+        for (int i = j + 1; i <= std::min(n - 1, j + 3); i++) {
+            double t = A[j * 4 + (i - j)];
+            for (int k = std::max(0, i - 3); k < j; k++) t -= A[k * 4 + (i - k)] * A[k * 4 + (j - k)];
+            A[j * 4 + (i - j)] = t * inv;
+        }
+    }
+    s.L4 = A;
+
+    // SB weights: row mi (0-based), tap t = c*mubar + mu over cells mc = mi-3+c
+    const int taps = 4 * mubar;
+    s.sbw.assign(size_t(Md) * taps, 0.0);
+    for (int mi = 0; mi < Md; mi++) {
+        int m = mi - 1;
+        for (int c = 0; c < 4; c++) {
+            int mc = m - 2 + c;
+            if (mc < 0 || mc > nc - 1) continue;
+            for (int mu = 0; mu < mubar; mu++) {
+                double x = xmin + mc * s.DX + s.qp[mu] * s.DX;
+                s.sbw[size_t(mi) * taps + c * mubar + mu] = s.DX * s.qw[mu] * bspline(s, m, x, 0);
+            }
+        }
+    }
+    // SI weights at the mish points (SItransform(sp, a, points, u, d))
+    s.siw.assign(size_t(3) * s.mishDim * 4, 0.0);
+    s.si_m0.assign(s.mishDim, 0);
+    for (int i = 0; i < s.mishDim; i++) {
+        double x = s.mish[i];
+        long xm = (long)std::ceil((x - xmin - (2.0 * s.DX)) * s.DXrecip);
+        int m0 = int(xm) + 1;  // coefficient index of m = xm
+        int base = std::min(std::max(m0, 0), Md - 4);
+        s.si_m0[i] = base;
+        for (int q = 0; q < 4; q++) {
+            long m = xm + q;
+            if (m < -1 || m > nc + 1) continue;
+            int idx = int(m + 1) - base;
+            if (idx < 0 || idx > 3) { set_error("SI window out of range"); return SS_BAD_ARG; }
+            for (int d = 0; d < 3; d++) s.siw[(size_t(d) * s.mishDim + i) * 4 + idx] = bspline(s, int(m), x, d);
+        }
+    }
+    return SS_OK;
+}
+
+// -------------------------------------------------------------- Chebyshev
+static double cospi_frac(long num, long den) {  // cos(π num/den) with exact reduction
+    long per = 2 * den;
+    num %= per;
+    if (num < 0) num += per;
+    bool flip = num > den;  // cos(π(2d - n)/d) = cos(πn/d)
+    long nn = flip ? per - num : num;
+    return std::cos(kPi * (double)nn / (double)den);
+}
+
+int32_t build_cheb(int N, int bk, int bcb, int bct, double zmin, double zmax, ChebHost &c) {
+    if (N < 2) { set_error("kDim must be >= 2"); return SS_BAD_SHAPE; }
+    if (bk < 1 || bk > N) { set_error("b_kDim out of range"); return SS_BAD_SHAPE; }
+    c.N = N; c.bk = bk;
+    c.half = (N + 1) / 2;
+    c.dscale = -0.5 * (zmax - zmin);
+    c.mish.resize(N);
+    {
+        double scale = -0.5 * (zmax - zmin), offset = 0.5 * (zmin + zmax);
+        for (int n = 1; n <= N; n++) c.mish[n - 1] = std::cos((n - 1) * kPi / (N - 1)) * scale + offset;
+    }
+    // forward: b[k] = filt_k * (1/(2(N-1))) * REDFT00(x)[k], folded over j ↔ N-1-j
+    const double scale = 1.0 / (2 * (N - 1));
+    c.fwd.assign(size_t(bk) * c.half, 0.0);
+    for (int k = 0; k < bk; k++) {
+        double filt = (bk < N) ? 1.0 : std::exp(-36.0 * std::pow(double(k + 1) / N, 36));
+        for (int j = 0; j < c.half; j++) {
+            int jj = N - 1 - j;
+            double w = (j == 0) ? 1.0 : 2.0;  // endpoint weight 1, interior 2
+            double cs = cospi_frac((long)j * k, N - 1);
+            if (jj == j) w = 2.0;              // middle point of odd N: counted once
+            c.fwd[size_t(k) * c.half + j] = filt * scale * w * cs;
+        }
+    }
+    // inverse REDFT00 folded over outputs j ↔ N-1-j; split into even / odd k
+    const int ne = (N + 1) / 2, no = N / 2;
+    c.inv_e.assign(size_t(c.half) * ne, 0.0);
+    c.inv_o.assign(size_t(c.half) * (no > 0 ? no : 1), 0.0);
+    for (int j = 0; j < c.half; j++) {
+        for (int k = 0; k < N; k++) {
+            double w = (k == 0 || k == N - 1) ? 1.0 : 2.0;
+            double v = w * cospi_frac((long)j * k, N - 1);
+            if (k % 2 == 0) c.inv_e[size_t(j) * ne + k / 2] = v;
+            else c.inv_o[size_t(j) * no + k / 2] = v;
+        }
+    }
+    // Γ (calcGammaBC, src/Chebyshev.jl:991-1177) as Σ_p u_p v_pᵀ, rank ≤ 2
+    std::vector<double> cv(N, 1.0);
+    cv[0] = 2.0; cv[N - 1] = 2.0;
+    auto sgn = [](long e) { return (e % 2 == 0) ? 1.0 : -1.0; };
+    std::vector<std::vector<double>> U, V;
+    // R1T0 bottom vector gl (rank 1, v = ones)
+    auto add_gl = [&]() {
+        std::vector<double> u(N), v(N, 1.0);
+        for (int i = 0; i < N; i++) u[i] = ((i == 0 || i == N - 1) ? 1.0 : 2.0) * (-0.5 / (N - 1));
+        U.push_back(u); V.push_back(v);
+    };
+    // R1T0 top: D[i,j] = -(-1)^i (-1)^j/(N-1), rows 0 and N-1 halved
+    auto add_top_dirichlet = [&]() {
+        std::vector<double> u(N), v(N);
+        for (int i = 0; i < N; i++) u[i] = -1.0 * sgn(i) / (N - 1) * ((i == 0 || i == N - 1) ? 0.5 : 1.0);
+        for (int j = 0; j < N; j++) v[j] = sgn(j);
+        U.push_back(u); V.push_back(v);
+    };
+    // R1T1 bottom: B[i,j] = n²/(sf c_j (N-1))
+    auto add_bot_neumann = [&]() {
+        double sf = 0.0;
+        for (int i = 0; i < N; i++) sf += -(double(i) * i) / (cv[i] * (N - 1));
+        std::vector<double> u(N), v(N);
+        for (int i = 0; i < N; i++) u[i] = double(i) * i / sf;
+        for (int j = 0; j < N; j++) v[j] = 1.0 / (cv[j] * (N - 1));
+        U.push_back(u); V.push_back(v);
+    };
+    // R1T1 top: T[i,j] = (-1)^(j+1) (-1)^(n+1) n²/(sf c_j (N-1))  (1-based j)
+    auto add_top_neumann = [&]() {
+        double sf = 0.0;
+        for (int i = 0; i < N; i++) sf += -(double(i) * i) * sgn(i) * sgn(i + 1) / (cv[i] * (N - 1));
+        std::vector<double> u(N), v(N);
+        for (int i = 0; i < N; i++) u[i] = sgn(i + 1) * double(i) * i / sf;
+        for (int j = 0; j < N; j++) v[j] = sgn(j + 2) / (cv[j] * (N - 1));
+        U.push_back(u); V.push_back(v);
+    };
+    if (bcb == SS_CBC_R0 && bct == SS_CBC_R0) {
+    } else if (bcb == SS_CBC_R1T0 && bct == SS_CBC_R0) { add_gl();
+    } else if (bcb == SS_CBC_R1T1 && bct == SS_CBC_R0) { add_bot_neumann();
+    } else if (bcb == SS_CBC_R0 && bct == SS_CBC_R1T0) { add_top_dirichlet();
+    } else if (bcb == SS_CBC_R0 && bct == SS_CBC_R1T1) { add_top_neumann();
+    } else if (bcb == SS_CBC_R1T0 && bct == SS_CBC_R1T0) { add_top_dirichlet(); add_gl();
+    } else if (bcb == SS_CBC_R1T1 && bct == SS_CBC_R1T1) { add_bot_neumann(); add_top_neumann();
+    } else if (bcb == SS_CBC_R1T0 && bct == SS_CBC_R1T1) { add_gl(); add_top_neumann();
+    } else if (bcb == SS_CBC_R1T1 && bct == SS_CBC_R1T0) { add_bot_neumann(); add_top_dirichlet();
+    } else {
+        set_error("Chebyshev boundary condition combination not implemented (BCB=%d, BCT=%d)", bcb, bct);
+        return SS_UNSUPPORTED_BC;
+    }
+    c.nrank = (int)U.size();
+    c.gu.assign(size_t(c.nrank) * bk, 0.0);
+    c.gv.assign(size_t(c.nrank) * N, 0.0);
+    for (int p = 0; p < c.nrank; p++) {
+        for (int i = 0; i < bk; i++) c.gu[size_t(p) * bk + i] = U[p][i];
+        for (int j = 0; j < N; j++) c.gv[size_t(p) * N + j] = V[p][j];
+    }
+    return SS_OK;
+}
+
+// -------------------------------------------------------------- FFT plans
+static std::complex<double> unit_root(long t, long n, int sign);
+int64_t TwiddlePool::push_table(int n, int sign, int len) {
+    int64_t off = size();
+    for (int t = 0; t < len; t++) {
+        std::complex<double> w = unit_root(t, n, sign);
+        v.push_back(w.real());
+        v.push_back(w.imag());
+    }
+    return off;
+}
+int64_t TwiddlePool::push(const std::vector<double> &ci) {
+    int64_t off = size();
+    v.insert(v.end(), ci.begin(), ci.end());
+    return off;
+}
+
+static bool factor_radices(int n, int *rad, int &nrad, bool smooth_only) {
+    nrad = 0;
+    while (n % 4 == 0 && n > 1) { rad[nrad++] = 4; n /= 4; }
+    const int primes[] = {2, 3, 5, 7, 11, 13};
+    for (int f : primes) {
+        if (smooth_only && f > 7) break;
+        while (n % f == 0) { rad[nrad++] = f; n /= f; }
+    }
+    if (nrad > kMaxRadices) return false;
+    return n == 1;
+}
+
+// exp(sign 2πi t/n) for 0 <= t < n, reduced by conjugate symmetry to t <= n/2
+static std::complex<double> unit_root(long t, long n, int sign) {
+    t %= n;
+    if (t < 0) t += n;
+    bool flip = 2 * t > n;
+    long tt = flip ? n - t : t;
+    double a = 2.0 * kPi * (double)tt / (double)n;
+    double c = std::cos(a), sn = std::sin(a);
+    if (flip) sn = -sn;
+    return std::complex<double>(c, sign * sn);
+}
+
+// host Stockham (double) used only to precompute Bluestein filters; tw[t] = W_N^t
+static void host_stockham(std::vector<std::complex<double>> &x, const int *rad, int nrad,
+                          const std::vector<std::complex<double>> &tw) {
+    const int N = (int)x.size();
+    std::vector<std::complex<double>> y(N);
+    int Ns = 1;
+    for (int s = 0; s < nrad; s++) {
+        int R = rad[s];
+        for (int j = 0; j < N / R; j++) {
+            int k = j % Ns;
+            std::complex<double> v[16], o[16];
+            for (int r = 0; r < R; r++) {
+                v[r] = x[j + r * (N / R)];
+                if (r > 0 && k > 0) v[r] *= tw[(size_t)k * r * (N / (Ns * R))];
+            }
+            for (int q = 0; q < R; q++) {
+                std::complex<double> acc = 0;
+                for (int r = 0; r < R; r++) acc += v[r] * tw[(size_t)((r * q) % R) * (N / R)];
+                o[q] = acc;
+            }
+            int idxD = (j / Ns) * Ns * R + k;
+            for (int r = 0; r < R; r++) y[idxD + r * Ns] = o[r];
+        }
+        x.swap(y);
+        Ns *= R;
+    }
+}
+
+
+int PlanSet::plan_for(int N, TwiddlePool &pool) {
+    if ((int)plan_of_N.size() <= N) plan_of_N.resize(N + 1, -1);
+    if (plan_of_N[N] >= 0) return plan_of_N[N];
+    FftPlan p;
+    std::memset(&p, 0, sizeof p);
+    p.N = N;
+    if (factor_radices(N, p.rad, p.nrad, false)) {
+        p.blu = 0;
+        p.tw = pool.push_table(N, -1, N);
+    } else {
+        p.blu = 1;
+        int M = 2 * N - 1;
+        for (;; M++)
+            if (factor_radices(M, p.mrad, p.mnrad, true)) break;
+        p.M = M;
+        p.nrad = 0;
+        if ((int)mtw_of_M.size() <= M) mtw_of_M.resize(M + 1, -1);
+        if (mtw_of_M[M] < 0) mtw_of_M[M] = pool.push_table(M, -1, M);
+        p.mtw = mtw_of_M[M];
+        std::vector<double> ch(2 * N);
+        std::vector<std::complex<double>> c(N);
+        for (long k = 0; k < N; k++) {
+            long t = (k * k) % (2L * N);  // exp(-πi t/N) = W_{2N}^t
+            c[k] = unit_root(t, 2L * N, -1);
+            ch[2 * k] = c[k].real();
+            ch[2 * k + 1] = c[k].imag();
+        }
+        p.chirp = pool.push(ch);
+        std::vector<std::complex<double>> f(M, 0.0);
+        f[0] = std::conj(c[0]);
+        for (int k = 1; k < N; k++) { f[k] = std::conj(c[k]); f[M - k] = std::conj(c[k]); }
+        std::vector<std::complex<double>> twm(M);
+        for (int t = 0; t < M; t++) twm[t] = unit_root(t, M, -1);
+        host_stockham(f, p.mrad, p.mnrad, twm);
+        std::vector<double> fi(2 * M);
+        for (int k = 0; k < M; k++) { fi[2 * k] = f[k].real() / M; fi[2 * k + 1] = f[k].imag() / M; }
+        p.filt = pool.push(fi);
+    }
+    plans.push_back(p);
+    plan_of_N[N] = (int)plans.size() - 1;
+    max_smem_cplx = std::max(max_smem_cplx, fft_buffer_len(p));
+    return plan_of_N[N];
+}
+
+int64_t PlanSet::unpack_for(int L, TwiddlePool &pool) {
+    if ((int)utw_of_L.size() <= L) utw_of_L.resize(L + 1, -1);
+    if (utw_of_L[L] < 0) utw_of_L[L] = pool.push_table(L, -1, L / 2);
+    return utw_of_L[L];
+}
+
+}  // namespace ss

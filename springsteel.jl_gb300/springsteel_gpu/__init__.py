@@ -1,0 +1,506 @@
+"""Host-side mirror of Springsteel.jl's RL/RLZ grid API over the GB300 C ABI.
+
+The reference's Julia entry points map one to one:
+
+=====================================  ==========================================
+Springsteel.jl                         here
+=====================================  ==========================================
+``SpringsteelGridParameters(...)``     :class:`SpringsteelGridParameters`
+``createGrid(gp)``                     :func:`createGrid` → :class:`SpringsteelGrid`
+``spectralTransform!(grid)``           :func:`spectralTransform_b` (alias ``spectralTransform``)
+``gridTransform!(grid)``               :func:`gridTransform_b` (alias ``gridTransform``)
+``getGridpoints(grid)``                :func:`getGridpoints`
+``NaturalBC()``, ``DirichletBC()``…    same names (src/Springsteel.jl:68-137)
+``SpectralFilter``/``GaussianFilter``  same names (src/filtering.jl:31-127)
+=====================================  ==========================================
+
+``grid.physical`` and ``grid.spectral`` live in device memory; reading the
+attributes downloads a host copy (``numpy`` arrays in the reference's
+column-major shape), assigning them uploads.  The compute path is the CUDA
+library only: if it cannot be loaded, calls raise instead of falling back.
+"""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import abi
+
+_PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+_lib = None
+
+
+class SpringsteelError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def load_library(build_if_missing=True):
+    """Load libspringsteel_gpu.so (building it with nvcc when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from . import build as _build
+
+    path = _build.LIB
+    if build_if_missing and (not os.path.exists(path) or _build._stale()):
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("libspringsteel_gpu.so is missing; run springsteel_gpu.build.build()")
+    _lib = abi.bind(C.CDLL(path))
+    return _lib
+
+
+def _check(st):
+    if st != abi.SS_OK:
+        raise SpringsteelError(st, load_library().ss_last_error_string().decode())
+
+
+# ----------------------------------------------------------------- BCs
+class BoundaryConditions:
+    """src/Springsteel.jl:45-63: constraint slots u, du, d2u, robin; periodic."""
+
+    def __init__(self, u=None, du=None, d2u=None, robin=None, periodic=False):
+        if robin is not None and any(x is not None for x in (u, du, d2u)):
+            raise ValueError("Robin BC is mutually exclusive with u/du/d2u constraint slots")
+        if periodic and any(x is not None for x in (u, du, d2u, robin)):
+            raise ValueError("PeriodicBC must have all other slots as nothing")
+        self.u, self.du, self.d2u, self.robin, self.periodic = u, du, d2u, robin, periodic
+
+    def __repr__(self):
+        return "BoundaryConditions(u=%r, du=%r, d2u=%r, robin=%r, periodic=%r)" % (
+            self.u, self.du, self.d2u, self.robin, self.periodic)
+
+
+def NaturalBC():
+    return BoundaryConditions()
+
+
+def DirichletBC(v=0.0):
+    return BoundaryConditions(u=float(v))
+
+
+def NeumannBC(v=0.0):
+    return BoundaryConditions(du=float(v))
+
+
+def SecondDerivativeBC(v=0.0):
+    return BoundaryConditions(d2u=float(v))
+
+
+def RobinBC(alpha, beta, gamma=0.0):
+    return BoundaryConditions(robin=(float(alpha), float(beta), float(gamma)))
+
+
+def PeriodicBC():
+    return BoundaryConditions(periodic=True)
+
+
+def CauchyBC(u, du):
+    return BoundaryConditions(u=float(u), du=float(du))
+
+
+def ExponentialBC(lam):
+    return RobinBC(1.0, -float(lam), 0.0)
+
+
+def SymmetricBC():
+    return NeumannBC(0.0)
+
+
+def AntisymmetricBC():
+    return BoundaryConditions(u=0.0, d2u=0.0)
+
+
+def ZerosBC():
+    return BoundaryConditions(u=0.0, du=0.0, d2u=0.0)
+
+
+def FixedBC(u=None, du=0.0, d2u=0.0):
+    if u is None:
+        return BoundaryConditions(u=math.nan, du=math.nan, d2u=math.nan)
+    return BoundaryConditions(u=float(u), du=float(du), d2u=float(d2u))
+
+
+def bc_rank(bc):
+    """src/Springsteel.jl:147-151."""
+    if bc.periodic:
+        return 0
+    if bc.robin is not None:
+        return 1
+    return sum(x is not None for x in (bc.u, bc.du, bc.d2u))
+
+
+def is_inhomogeneous(bc):
+    if bc.robin is not None:
+        return bc.robin[2] != 0.0
+    return any(x is not None and x != 0.0 for x in (bc.u, bc.du, bc.d2u))
+
+
+# legacy CubicBSpline BC dicts (src/CubicBSpline.jl:41-122) as (kind, α, β)
+R0 = (abi.SS_SBC_R0, 0.0, 0.0)
+R1T0 = (abi.SS_SBC_RANK1, -4.0, -1.0)
+R1T1 = (abi.SS_SBC_RANK1, 0.0, 1.0)
+R1T2 = (abi.SS_SBC_RANK1, 2.0, -1.0)
+R2T10 = (abi.SS_SBC_RANK2, 1.0, -0.5)
+R2T20 = (abi.SS_SBC_RANK2, -1.0, 0.0)
+R3 = (abi.SS_SBC_R3, 0.0, 0.0)
+R3X = (abi.SS_SBC_R3X, 0.0, 0.0)
+PERIODIC = (abi.SS_SBC_PERIODIC, 0.0, 0.0)
+# legacy Chebyshev BC dicts (src/Chebyshev.jl) as kinds
+CHEB_R0 = abi.SS_CBC_R0
+CHEB_R1T0 = abi.SS_CBC_R1T0
+CHEB_R1T1 = abi.SS_CBC_R1T1
+
+
+def _bc_to_spline(bc):
+    """_bc_to_spline_dict, src/factory.jl:343-375."""
+    if isinstance(bc, tuple):
+        return bc
+    if bc.periodic:
+        return PERIODIC
+    r = bc_rank(bc)
+    if r == 0:
+        return R0
+    if r == 1:
+        if bc.u is not None:
+            return R1T0
+        if bc.du is not None:
+            return R1T1
+        if bc.d2u is not None:
+            return R1T2
+        a, b, _ = bc.robin
+        lam = -b / a
+        return (abi.SS_SBC_RANK1, -4.0 / (3 * lam + 1), (3 * lam - 1) / (3 * lam + 1))
+    if r == 2:
+        if bc.u is not None and bc.du is not None:
+            return R2T10
+        if bc.u is not None and bc.d2u is not None:
+            return R2T20
+        raise ValueError("Unsupported rank-2 BC combination for CubicBSpline: du + d2u without u is not defined")
+    return R3X if is_inhomogeneous(bc) or any(x is not None and math.isnan(x) for x in (bc.u, bc.du, bc.d2u)) else R3
+
+
+def _bc_to_chebyshev(bc):
+    """_bc_to_chebyshev_dict + _bc_type, src/factory.jl:378-396, src/Chebyshev.jl:949-963."""
+    if isinstance(bc, int):
+        return bc
+    if bc.periodic:
+        raise ValueError("PeriodicBC is not supported for Chebyshev basis")
+    if bc.robin is not None:
+        raise ValueError("RobinBC is not supported for Chebyshev basis")
+    r = bc_rank(bc)
+    if r == 0:
+        return abi.SS_CBC_R0
+    if r == 1:
+        if bc.u is not None:
+            return abi.SS_CBC_R1T0
+        if bc.du is not None:
+            return abi.SS_CBC_R1T1
+        raise ValueError("Chebyshev BC R1T2 is not supported by calcGammaBC")
+    raise ValueError("Rank-%d BCs are not yet implemented for Chebyshev basis" % r)
+
+
+# ----------------------------------------------------------------- filters
+class SpectralFilter:
+    """src/filtering.jl:58-64."""
+
+    def __init__(self, low_pass=-1, high_pass=0, notch=(), window="boxcar", taper_width=0):
+        self.low_pass, self.high_pass = int(low_pass), int(high_pass)
+        self.notch = [int(n) for n in notch]
+        self.window, self.taper_width = window, int(taper_width)
+
+
+class GaussianFilter:
+    """src/filtering.jl:87-90."""
+
+    def __init__(self, sigma, order=1):
+        self.sigma, self.order = float(sigma), int(order)
+
+
+def _window_weight(window, t):
+    """src/filtering.jl:110-127."""
+    t = min(max(t, 0.0), 1.0)
+    if window == "boxcar":
+        return 1.0 if t < 1.0 else 0.0
+    if window == "hann":
+        return 0.5 * (1.0 + math.cos(math.pi * t))
+    if window == "lanczos":
+        # t ≈ 0 with isapprox's default atol = 0 holds only for t == 0
+        return 1.0 if t == 0.0 else math.sin(math.pi * t) / (math.pi * t)
+    if window == "exponential":
+        return math.exp(-t * t * 4.0)
+    raise ValueError("Unknown window function: %s" % window)
+
+
+def filter_weight(f, k):
+    """_filter_weight, src/filtering.jl:145-194."""
+    if isinstance(f, GaussianFilter):
+        return math.exp(-(float(k) / f.sigma) ** (2 * f.order))
+    if k in f.notch:
+        return 0.0
+    d = f.taper_width
+    if f.high_pass > 0 and k < f.high_pass:
+        if d > 0:
+            dist = f.high_pass - k
+            return 0.0 if dist > d else _window_weight(f.window, dist / d)
+        return 0.0
+    if f.low_pass >= 0 and k > f.low_pass:
+        if d > 0:
+            dist = k - f.low_pass
+            return 0.0 if dist > d else _window_weight(f.window, dist / d)
+        return 0.0
+    return 1.0
+
+
+def _snap(w):
+    # the reference skips blocks with w ≈ 1 (isapprox, rtol = √eps) and zeroes w ≈ 0
+    if abs(w - 1.0) <= 1.4901161193847656e-08 * max(abs(w), 1.0):
+        return 1.0
+    return w
+
+
+# ----------------------------------------------------------------- params
+def _per_var(d, key, default):
+    if not isinstance(d, dict):
+        return d
+    if key in d:
+        return d[key]
+    return d.get("default", default)
+
+
+class SpringsteelGridParameters:
+    """src/Springsteel.jl:425-465 (RL / RLZ fields), plus ``precision``."""
+
+    def __init__(self, geometry="RL", iMin=0.0, iMax=0.0, num_cells=0, mubar=3, quadrature="gauss",
+                 l_q=None, BCL=None, BCR=None, kMin=0.0, kMax=0.0, kDim=0, b_kDim=None, BCB=None, BCT=None,
+                 vars=None, max_wavenumber=None, fourier_filter=None, chebyshev_filter=None,
+                 spectralIndexL=1, patchOffsetL=None, precision="f64"):
+        geom = {"RL": "RL", "Spline1D_Fourier": "RL", "RLZ": "RLZ"}.get(geometry, geometry)
+        if geom not in ("RL", "RLZ"):
+            raise ValueError("only RL and RLZ geometries run on the GPU path (got %r)" % geometry)
+        self.geometry = geom
+        self.iMin, self.iMax, self.num_cells, self.mubar = float(iMin), float(iMax), int(num_cells), int(mubar)
+        self.quadrature = quadrature
+        self.iDim = self.num_cells * self.mubar
+        self.b_iDim = self.num_cells + 3
+        self.l_q = l_q if l_q is not None else {"default": 2.0}
+        self.BCL = BCL if BCL is not None else {"default": R0}
+        self.BCR = BCR if BCR is not None else {"default": R0}
+        self.kMin, self.kMax, self.kDim = float(kMin), float(kMax), int(kDim)
+        self.b_kDim = (min(self.kDim, (2 * self.kDim - 1) // 3 + 1) if b_kDim is None else int(b_kDim))
+        self.BCB = BCB if BCB is not None else {"default": CHEB_R0}
+        self.BCT = BCT if BCT is not None else {"default": CHEB_R0}
+        self.vars = vars if vars is not None else {"u": 1}
+        self.max_wavenumber = max_wavenumber if max_wavenumber is not None else {"default": -1}
+        self.fourier_filter = fourier_filter or {}
+        self.chebyshev_filter = chebyshev_filter or {}
+        self.spectralIndexL = int(spectralIndexL)
+        self.patchOffsetL = (self.spectralIndexL - 1) * self.mubar if patchOffsetL is None else int(patchOffsetL)
+        self.precision = precision
+
+    def var_names(self):
+        names = [None] * len(self.vars)
+        for k, v in self.vars.items():
+            names[v - 1] = k
+        return names
+
+    def to_abi(self):
+        names = self.var_names()
+        nv = len(names)
+        quad = {"gauss": abi.SS_QUAD_GAUSS, "regular": abi.SS_QUAD_REGULAR}[self.quadrature]
+        prec = {"f64": abi.SS_PREC_F64, "f32": abi.SS_PREC_F32_REFINED,
+                "f32_refined": abi.SS_PREC_F32_REFINED}[self.precision]
+        geom = abi.SS_GEOM_RL if self.geometry == "RL" else abi.SS_GEOM_RLZ
+        kw = dict(
+            mubar=self.mubar, quadrature=quad, precision=prec, patchOffsetL=self.patchOffsetL,
+            l_q=[float(_per_var(self.l_q, n, 2.0)) for n in names],
+            BCL=[_bc_to_spline(_per_var(self.BCL, n, R0)) for n in names],
+            BCR=[_bc_to_spline(_per_var(self.BCR, n, R0)) for n in names],
+            max_wavenumber=[int(_per_var(self.max_wavenumber, n, -1)) for n in names],
+        )
+        if self.geometry == "RLZ":
+            kw.update(kDim=self.kDim, b_kDim=self.b_kDim, kMin=self.kMin, kMax=self.kMax,
+                      BCB=[_bc_to_chebyshev(_per_var(self.BCB, n, CHEB_R0)) for n in names],
+                      BCT=[_bc_to_chebyshev(_per_var(self.BCT, n, CHEB_R0)) for n in names])
+        return abi.make_params(geom, self.num_cells, self.iMin, self.iMax, nv, **kw)
+
+
+# ----------------------------------------------------------------- grid
+_DTYPES = {np.dtype(np.float64): abi.SS_DTYPE_F64, np.dtype(np.float32): abi.SS_DTYPE_F32}
+
+
+class SpringsteelGrid:
+    """Device-resident RL/RLZ grid (the GPU counterpart of SpringsteelGrid, src/types.jl:249-256)."""
+
+    def __init__(self, gp):
+        self.params = gp
+        self._bundle = gp.to_abi()
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.ss_grid_create(self._bundle.ref, C.byref(h)))
+        self._h = h
+        d = abi.ss_dims()
+        _check(lib.ss_grid_dims(h, C.byref(d)))
+        self.dims = d.as_dict()
+        self.dtype = np.float64 if gp.precision == "f64" else np.float32
+        self._apply_filters()
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().ss_grid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def physical_shape(self):
+        d = self.dims
+        return (d["n_physical"], d["nvars"], d["nslots"])
+
+    @property
+    def spectral_shape(self):
+        return (self.dims["n_spectral"], self.dims["nvars"])
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(load_library().ss_grid_stream(self._h, C.byref(s)))
+        return s.value
+
+    # -- host copies
+    def get_physical(self, slot=0, dtype=np.float64):
+        n, nv, ns = self.physical_shape
+        out = np.empty((n, nv, ns) if slot == 0 else (n, nv), dtype=dtype, order="F")
+        _check(load_library().ss_download_physical(self._h, out.ctypes.data_as(C.c_void_p),
+                                                   _DTYPES[np.dtype(dtype)], int(slot), None))
+        return out
+
+    def set_physical(self, arr, slot=1):
+        n, nv, ns = self.physical_shape
+        a = np.asfortranarray(arr)
+        if a.dtype not in _DTYPES:
+            a = a.astype(np.float64, order="F")
+        want = (n, nv, ns) if slot == 0 else (n, nv)
+        if a.ndim == 3 and slot != 0:
+            a = np.asfortranarray(a[:, :, slot - 1])
+        if a.shape != want and a.size == int(np.prod(want)):
+            a = np.asfortranarray(a.reshape(want, order="F"))
+        if a.shape != want:
+            raise ValueError("physical shape %s, expected %s" % (a.shape, want))
+        _check(load_library().ss_upload_physical(self._h, a.ctypes.data_as(C.c_void_p), _DTYPES[a.dtype],
+                                                 int(slot), None))
+
+    def get_spectral(self, dtype=np.float64):
+        out = np.empty(self.spectral_shape, dtype=dtype, order="F")
+        _check(load_library().ss_download_spectral(self._h, out.ctypes.data_as(C.c_void_p),
+                                                   _DTYPES[np.dtype(dtype)], None))
+        return out
+
+    def set_spectral(self, arr):
+        a = np.asfortranarray(arr)
+        if a.dtype not in _DTYPES:
+            a = a.astype(np.float64, order="F")
+        if a.shape != self.spectral_shape:
+            raise ValueError("spectral shape %s, expected %s" % (a.shape, self.spectral_shape))
+        _check(load_library().ss_upload_spectral(self._h, a.ctypes.data_as(C.c_void_p), _DTYPES[a.dtype], None))
+
+    physical = property(lambda self: self.get_physical(), lambda self, a: self.set_physical(a, 0))
+    spectral = property(lambda self: self.get_spectral(), lambda self, a: self.set_spectral(a))
+
+    # -- registry hooks
+    def set_wavenumber_ahat(self, var, block, ahat):
+        """_set_wavenumber_ahat! (src/multipatch_registry.jl:45-62); `block` is the spectral block index."""
+        a = np.ascontiguousarray(ahat, dtype=np.float64)
+        if a.size != self.dims["b_iDim"]:
+            raise ValueError("ahat needs b_iDim entries")
+        _check(load_library().ss_grid_set_ahat(self._h, int(var), int(block), a.ctypes.data_as(C.c_void_p)))
+
+    def clear_wavenumber_ahat(self):
+        _check(load_library().ss_grid_clear_ahat(self._h))
+
+    def _apply_filters(self):
+        gp = self.params
+        if not gp.fourier_filter and not gp.chebyshev_filter:
+            return
+        K, bk = self.dims["kDim_wn"], self.dims["b_kDim"]
+        for v, name in enumerate(gp.var_names()):
+            ff = _per_var(gp.fourier_filter, name, None)
+            cf_ = _per_var(gp.chebyshev_filter, name, None) if gp.geometry == "RLZ" else None
+            fw = cw = None
+            if ff is not None:
+                fw = np.array([_snap(filter_weight(ff, k)) for k in range(K + 1)])
+            if cf_ is not None:
+                cw = np.array([_snap(filter_weight(cf_, z)) for z in range(bk)])
+            if fw is None and cw is None:
+                continue
+            _check(load_library().ss_grid_set_filter(
+                self._h, v, fw.ctypes.data_as(C.c_void_p) if fw is not None else None,
+                cw.ctypes.data_as(C.c_void_p) if cw is not None else None))
+
+    def synchronize(self):
+        _check(load_library().ss_grid_synchronize(self._h))
+
+
+def createGrid(gp):
+    """createGrid (src/factory.jl:1104-1143) for RL / RLZ geometries."""
+    return SpringsteelGrid(gp)
+
+
+def spectralTransform_b(grid, stream=None):
+    """spectralTransform!(grid): physical slot 1 → spectral, then applyFilter! (asynchronous)."""
+    _check(load_library().ss_spectral_transform(grid.handle, stream))
+    return grid
+
+
+def gridTransform_b(grid, stream=None):
+    """gridTransform!(grid): spectral → every physical derivative slot (asynchronous)."""
+    _check(load_library().ss_grid_transform(grid.handle, stream))
+    return grid
+
+
+spectralTransform = spectralTransform_b
+gridTransform = gridTransform_b
+
+
+def getGridpoints(grid):
+    """getGridpoints (src/transforms_cylindrical.jl:75-90, 454-476)."""
+    gp = grid.params
+    d = grid.dims
+    nc, mb = gp.num_cells, gp.mubar
+    DX = (gp.iMax - gp.iMin) / nc
+    if gp.quadrature == "gauss":
+        nodes = np.polynomial.legendre.leggauss(mb)[0] if mb != 3 else np.array([-math.sqrt(0.6), 0.0, math.sqrt(0.6)])
+        q = (nodes + 1.0) / 2.0
+    else:
+        q = (2 * np.arange(1, mb + 1) - 1) / (2 * mb)
+    rmish = np.array([gp.iMin + mc * DX + q[mu] * DX for mc in range(nc) for mu in range(mb)])
+    pts = []
+    kz = d["kDim"]
+    if gp.geometry == "RLZ":
+        N = gp.kDim
+        scale, offset = -0.5 * (gp.kMax - gp.kMin), 0.5 * (gp.kMin + gp.kMax)
+        zm = np.cos(np.arange(N) * math.pi / (N - 1)) * scale + offset
+    for r in range(1, d["iDim"] + 1):
+        ri = r + gp.patchOffsetL
+        L = 4 + 4 * ri
+        ymin = 0.5 * (2 * math.pi / L) * (ri - 1)
+        lam = ymin + 2 * math.pi * np.arange(L) / L
+        if gp.geometry == "RL":
+            pts.append(np.column_stack([np.full(L, rmish[r - 1]), lam]))
+        else:
+            rr = np.full(L * kz, rmish[r - 1])
+            ll = np.repeat(lam, kz)
+            zz = np.tile(zm, L)
+            pts.append(np.column_stack([rr, ll, zz]))
+    return np.asfortranarray(np.vstack(pts))

@@ -1,0 +1,82 @@
+"""Seeded synthetic fields of the benchmark shapes (no public dataset is involved).
+
+All generators use numpy's PCG64 (``numpy.random.default_rng(seed)``), which is
+bit-reproducible across platforms.
+"""
+import numpy as np
+
+from . import SpringsteelGridParameters, DirichletBC, NaturalBC
+
+
+def gaussian_ring_field(points, seed=1, noise=1e-3):
+    """u = exp(-(r/20)²)(1 + 0.1 cos 2λ) + N(0, noise) at the gridpoints (RL shape)."""
+    r, lam = points[:, 0], points[:, 1]
+    rng = np.random.default_rng(seed)
+    return np.exp(-((r / 20.0) ** 2)) * (1.0 + 0.1 * np.cos(2.0 * lam)) + rng.normal(0.0, noise, r.shape)
+
+
+def blob_sum(points, seed, nblobs=8, rmax=None, zmin=0.0, zmax=1.0, wmin=5.0, wmax=30.0, vert=100.0,
+             noise=0.0):
+    """Σ A exp(-[(x-xc)²+(y-yc)²]/w² - (z-zc)²/(vert·w)²), x = r cos λ, y = r sin λ.
+
+    Centres are uniform in the disc of radius rmax (and in [zmin, zmax]),
+    widths w ~ U[wmin, wmax], amplitudes A ~ N(0, 1).  ``points`` has columns
+    (r, λ[, z]); a 2-column input drops the z factor."""
+    rng = np.random.default_rng(seed)
+    r, lam = points[:, 0], points[:, 1]
+    x, y = r * np.cos(lam), r * np.sin(lam)
+    if rmax is None:
+        rmax = float(r.max())
+    has_z = points.shape[1] > 2
+    z = points[:, 2] if has_z else None
+    out = np.zeros(r.shape)
+    for _ in range(nblobs):
+        rc = rmax * np.sqrt(rng.uniform())
+        tc = rng.uniform(0.0, 2 * np.pi)
+        xc, yc = rc * np.cos(tc), rc * np.sin(tc)
+        zc = rng.uniform(zmin, zmax)
+        w = rng.uniform(wmin, wmax)
+        A = rng.normal()
+        e = ((x - xc) ** 2 + (y - yc) ** 2) / (w * w)
+        if has_z:
+            e = e + ((z - zc) / (vert * w)) ** 2
+        out += A * np.exp(-e)
+    if noise:
+        out += rng.normal(0.0, noise, out.shape)
+    return out
+
+
+# ---------------------------------------------------------------- benchmark shapes
+def config1_params(precision="f64"):
+    """RL, radius 0-100, 100 cells × 3 Gauss points, rings of 4+4r, one variable.
+    NaturalBC at both ends (the reference has no RL axis-regularity BC)."""
+    return SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=100.0, num_cells=100,
+                                     BCL={"default": NaturalBC()}, BCR={"default": NaturalBC()},
+                                     vars={"u": 1}, precision=precision)
+
+
+def config2_params(precision="f64", num_cells=200, kDim=32, nvars=5):
+    """RLZ, 200 cells on r ∈ [0, 200] (DX = 1), 32 Chebyshev levels on z ∈ [0, 20000],
+    5 variables, Dirichlet in z (Chebyshev R1T0 both ends)."""
+    vars_ = {"v%d" % i: i for i in range(1, nvars + 1)}
+    return SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=float(num_cells), num_cells=num_cells,
+                                     kMin=0.0, kMax=20000.0, kDim=kDim, vars=vars_,
+                                     BCB={"default": DirichletBC()}, BCT={"default": DirichletBC()},
+                                     precision=precision)
+
+
+def config4_params(precision="f32", num_cells=400, kDim=64, nvars=8):
+    """RLZ, 400 cells (r ∈ [0, 400]), 64 Chebyshev levels on z ∈ [0, 20000], 8 variables."""
+    vars_ = {"v%d" % i: i for i in range(1, nvars + 1)}
+    return SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=float(num_cells), num_cells=num_cells,
+                                     kMin=0.0, kMax=20000.0, kDim=kDim, vars=vars_,
+                                     BCB={"default": DirichletBC()}, BCT={"default": DirichletBC()},
+                                     precision=precision)
+
+
+def rlz_blob_fields(points, nvars, base_seed=2, zmax=20000.0, noise=0.0):
+    """(n_physical, nvars) Fortran-ordered array of per-variable blob sums."""
+    out = np.empty((points.shape[0], nvars), order="F")
+    for v in range(nvars):
+        out[:, v] = blob_sum(points, seed=base_seed * 1000 + v, zmax=zmax, noise=noise)
+    return out

@@ -1,0 +1,184 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle.
+
+Relative error of a (variable, slot) block = max|gpu - oracle| / max|oracle|.
+FP64 path tolerance: 1e-12 (the reference's own FP64 round-off budget,
+spec bound).  FP32+refinement path: stated per slot below.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import springsteel_gpu as S
+from springsteel_gpu import fields
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+
+def _rel(a, b):
+    den = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / den) if den > 0 else float(np.max(np.abs(a)))
+
+
+def _run_both(gp, phys_slot1, ahats=None):
+    g = S.createGrid(gp)
+    o = O.OracleGrid(gp.to_abi())
+    if ahats:
+        for (v, blk, a) in ahats:
+            g.set_wavenumber_ahat(v, blk, a)
+            o.set_ahat(v, blk, a)
+    if gp.fourier_filter or gp.chebyshev_filter:
+        K, bk = o.dims["kDim_wn"], o.dims["b_kDim"]
+        for v, name in enumerate(gp.var_names()):
+            ff = S._per_var(gp.fourier_filter, name, None)
+            cf = S._per_var(gp.chebyshev_filter, name, None)
+            fw = np.array([S._snap(S.filter_weight(ff, k)) for k in range(K + 1)]) if ff else None
+            cw = np.array([S._snap(S.filter_weight(cf, z)) for z in range(bk)]) if cf else None
+            o.set_filter(v, fw, cw)
+    ph = np.zeros(o.physical_shape, order="F")
+    ph[:, :, 0] = phys_slot1
+    g.set_physical(ph[:, :, 0], slot=1)
+    S.spectralTransform_b(g)
+    spec_g = g.get_spectral()
+    spec_o = o.spectral_transform(ph)
+    S.gridTransform_b(g)
+    phys_g = g.get_physical()
+    phys_o = o.grid_transform(spec_o)
+    return g, o, spec_g, spec_o, phys_g, phys_o
+
+
+def _assert_parity(spec_g, spec_o, phys_g, phys_o, tol=TOL64, slot_tol=None):
+    nv = spec_o.shape[1]
+    for v in range(nv):
+        e = _rel(spec_g[:, v], spec_o[:, v])
+        assert e <= tol, ("spectral", v, e)
+        for s in range(phys_o.shape[2]):
+            t = (slot_tol or {}).get(s + 1, tol)
+            e = _rel(phys_g[:, v, s], phys_o[:, v, s])
+            assert e <= t, ("physical slot", s + 1, "var", v, e)
+
+
+def test_rl_config1_parity():
+    gp = fields.config1_params()
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.gaussian_ring_field(pts, seed=1)
+    _, _, sg, so, pg, po = _run_both(gp, u[:, None])
+    _assert_parity(sg, so, pg, po)
+
+
+def test_rl_gridpoints_match_oracle():
+    gp = fields.config1_params()
+    g = S.createGrid(gp)
+    o = O.OracleGrid(gp.to_abi())
+    assert np.max(np.abs(S.getGridpoints(g) - o.gridpoints())) < 1e-13
+
+
+def test_rl_multivar_bcs_offset_kmax():
+    gp = S.SpringsteelGridParameters(
+        geometry="RL", iMin=5.0, iMax=65.0, num_cells=20, vars={"a": 1, "b": 2, "c": 3, "d": 4},
+        BCL={"a": S.DirichletBC(), "b": S.NeumannBC(), "c": S.CauchyBC(0.0, 0.0), "d": S.ZerosBC()},
+        BCR={"a": S.NaturalBC(), "b": S.SecondDerivativeBC(), "c": S.AntisymmetricBC(), "d": S.RobinBC(1.0, -2.0)},
+        l_q={"default": 2.0, "c": 0.5}, max_wavenumber={"default": -1, "b": 7, "d": 0},
+        spectralIndexL=2)
+    g0 = S.createGrid(gp)
+    pts = S.getGridpoints(g0)
+    u = np.column_stack([fields.blob_sum(pts, seed=s, nblobs=5, wmin=3, wmax=10) for s in range(4)])
+    _, _, sg, so, pg, po = _run_both(gp, u)
+    _assert_parity(sg, so, pg, po)
+
+
+def test_rl_r3x_ahat():
+    gp = S.SpringsteelGridParameters(geometry="RL", iMin=10.0, iMax=40.0, num_cells=15,
+                                     BCL={"default": S.FixedBC()}, BCR={"default": S.NaturalBC()})
+    g0 = S.createGrid(gp)
+    pts = S.getGridpoints(g0)
+    u = (fields.blob_sum(pts, seed=7, nblobs=4, wmin=2, wmax=8) + 0.5)[:, None]
+    b = g0.dims["b_iDim"]
+    rng = np.random.default_rng(3)
+    ahats = []
+    for blk in (0, 1, 2, 5, 6):
+        a = np.zeros(b)
+        a[:3] = rng.normal(size=3)
+        ahats.append((0, blk, a))
+    _, _, sg, so, pg, po = _run_both(gp, u, ahats)
+    _assert_parity(sg, so, pg, po)
+
+
+def test_rl_filters():
+    gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=30.0, num_cells=10,
+                                     fourier_filter={"default": S.SpectralFilter(low_pass=6, notch=[2], window="hann",
+                                                                                 taper_width=3)})
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.blob_sum(pts, seed=11, nblobs=6, wmin=2, wmax=6)[:, None]
+    _, _, sg, so, pg, po = _run_both(gp, u)
+    _assert_parity(sg, so, pg, po)
+
+
+@pytest.mark.parametrize("bcb,bct", [(S.DirichletBC(), S.DirichletBC()), (S.NaturalBC(), S.NaturalBC()),
+                                     (S.NeumannBC(), S.DirichletBC()), (S.NeumannBC(), S.NeumannBC()),
+                                     (S.DirichletBC(), S.NaturalBC())])
+def test_rlz_parity_bcs(bcb, bct):
+    gp = S.SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=40.0, num_cells=20, kMin=0.0,
+                                     kMax=20000.0, kDim=16, vars={"u": 1, "w": 2},
+                                     BCB={"default": bcb}, BCT={"default": bct})
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.rlz_blob_fields(pts, 2, zmax=20000.0)
+    _, _, sg, so, pg, po = _run_both(gp, u)
+    _assert_parity(sg, so, pg, po)
+
+
+def test_rlz_config2_shape_reduced():
+    # the configuration-2 layout (kz = 32, 5 variables, Dirichlet in z) at 40 cells
+    gp = fields.config2_params(num_cells=40)
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.rlz_blob_fields(pts, 5, zmax=20000.0)
+    _, _, sg, so, pg, po = _run_both(gp, u)
+    _assert_parity(sg, so, pg, po)
+
+
+def test_rlz_patch_offset_and_filters():
+    gp = S.SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=40.0, num_cells=4, spectralIndexL=2,
+                                     kMin=0.0, kMax=10.0, kDim=8,
+                                     fourier_filter={"default": S.GaussianFilter(sigma=6.0, order=2)},
+                                     chebyshev_filter={"default": S.SpectralFilter(low_pass=3)})
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = (pts[:, 0] * pts[:, 2] + np.cos(3 * pts[:, 1]) * pts[:, 0] / 40.0)[:, None]
+    _, _, sg, so, pg, po = _run_both(gp, u)
+    _assert_parity(sg, so, pg, po)
+
+
+def test_rl_linear_field_exact():
+    # f = 3r + 7 is reproduced exactly by the cubic B-spline fit (test/multipatch.jl:1258-1283 pattern)
+    gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=120.0, num_cells=60)
+    g = S.createGrid(gp)
+    pts = S.getGridpoints(g)
+    g.set_physical((3 * pts[:, 0] + 7)[:, None], slot=1)
+    S.spectralTransform_b(g)
+    S.gridTransform_b(g)
+    ph = g.get_physical()
+    assert np.max(np.abs(ph[:, 0, 0] - (3 * pts[:, 0] + 7))) < 1e-8
+    assert np.max(np.abs(ph[:, 0, 1] - 3.0)) < 1e-8
+    assert np.max(np.abs(ph[:, 0, 2])) < 1e-8
+
+
+def test_fp32_refined_error_vs_fp64_oracle():
+    gp = S.SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=40.0, num_cells=20, kMin=0.0,
+                                     kMax=20000.0, kDim=16, vars={"u": 1},
+                                     BCB={"default": S.DirichletBC()}, BCT={"default": S.DirichletBC()},
+                                     precision="f32")
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.rlz_blob_fields(pts, 1, zmax=20000.0)
+    _, o, sg, so, pg, po = _run_both(gp, u)
+    for s in range(po.shape[2]):
+        e = _rel(pg[:, 0, s], po[:, 0, s])
+        assert e < 1e-4, (s + 1, e)
+
+
+def test_bad_shapes_rejected():
+    with pytest.raises(S.SpringsteelError):
+        S.createGrid(S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=1.0, num_cells=0))
+    with pytest.raises(S.SpringsteelError) as e:
+        S.createGrid(S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=1.0, num_cells=4,
+                                                 BCL={"default": S.PeriodicBC()}, BCR={"default": S.PeriodicBC()}))
+    assert e.value.status == S.abi.SS_UNSUPPORTED_BC
