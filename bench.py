@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 RL/RLZ transform path (one JSON line on rank 0).
+
+Metric: RLZ transforms/s — one transform = one round trip, spectralTransform!
+followed by gridTransform!, over every variable of the grid, all 7 derivative
+slots.  Default workload: the 5-variable RLZ grid of 200 radial cells, rings
+of 4+4r points, 32 Chebyshev levels on z ∈ [0, 20000], FP64 (the reference's
+precision).  ``--workload rlz400-f32`` runs the 8-variable 400-cell / 64-level
+FP32+refinement grid instead.
+
+  value     round trips/s with inputs resident in HBM (CUDA events on the
+            library's stream, max over ranks)
+  e2e       round trips/s through the C ABI with pinned host buffers: upload of
+            physical slot 1, both transforms, download of all 7 slots, per step
+  roofline  the dominant stage, timed live with CUDA events inside the timed
+            region (the library's stage instrumentation)
+  cpu_baseline  the FP64 oracle (C port of the reference path) on the host
+            cores, on one variable of the same grid, scaled to the workload
+
+``--impl reference`` times the reference's CPU path instead: Julia is not
+available on either machine, so that arm runs the C port of the reference
+algorithm (the oracle) with every host thread.  Multi-GPU: independent
+replicas of the grid (no collective on the data path), weak scaling.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "springsteel.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "rlz200-f64": dict(num_cells=200, kDim=32, nvars=5, precision="f64"),
+    "rlz400-f32": dict(num_cells=400, kDim=64, nvars=8, precision="f32"),
+    # small case for profiling captures (same kernels, a few hundred MB)
+    "rlz100-f64": dict(num_cells=100, kDim=32, nvars=2, precision="f64"),
+    "rlz200-f32": dict(num_cells=200, kDim=64, nvars=2, precision="f32"),
+}
+
+
+def _params(wl):
+    from springsteel_gpu import fields
+
+    w = WORKLOADS[wl]
+    if w["precision"] == "f64":
+        return fields.config2_params(precision="f64", num_cells=w["num_cells"], kDim=w["kDim"], nvars=w["nvars"])
+    return fields.config4_params(precision="f32", num_cells=w["num_cells"], kDim=w["kDim"], nvars=w["nvars"])
+
+
+def _config(wl, dims):
+    w = WORKLOADS[wl]
+    return {
+        "workload": "RLZ %d cells x %d Chebyshev levels, %d vars, %s" % (
+            w["num_cells"], w["kDim"], w["nvars"], "FP64" if w["precision"] == "f64" else "FP32+FP64 refinement"),
+        "geometry": "RLZ", "num_cells": w["num_cells"], "iDim": dims["iDim"], "kDim": w["kDim"],
+        "b_kDim": dims["b_kDim"], "nvars": w["nvars"], "jDim": dims["jDim"],
+        "physical_points_per_var": dims["n_physical"], "spectral_per_var": dims["n_spectral"],
+        "fields": "seeded Gaussian-blob sums (8 blobs, widths 5-30, z in [0, 20000])",
+        "l2": "inputs larger than L2 (physical slot 1 > 129 MB)",
+    }
+
+
+def _bytes_per_roundtrip(dims, w):
+    """Algorithmic HBM bytes of one round trip: read slot 1, write every slot,
+    write + read spectral (per variable)."""
+    return w * dims["nvars"] * (dims["n_physical"] * (1 + dims["nslots"]) + 2 * dims["n_spectral"])
+
+
+def _stage_bytes(dims, w):
+    """Compulsory bytes of each stage for one round trip (all variables)."""
+    nv, bk, jD, fr = dims["nvars"], dims["b_kDim"], dims["jDim"], dims["b_jDim"]
+    npx, ns = dims["n_physical"], dims["n_spectral"]
+    rlz = dims["kDim"] > 1
+    out = {
+        "cheb_forward": w * nv * (npx + bk * jD) if rlz else 0,
+        "ring_forward": w * nv * ((bk * jD if rlz else npx) + bk * fr),
+        "sb_project": w * nv * (bk * fr + ns),
+        "sa_si": w * nv * (ns + 3 * bk * fr),
+        "ring_inverse": w * nv * (3 * bk * fr + (5 * bk * jD if rlz else 5 * npx)),
+        "cheb_inverse": w * nv * (5 * bk * jD + 7 * npx) if rlz else 0,
+    }
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _oracle_sample(wl, threads, seconds_hint=None):
+    """One round trip of ONE variable of the workload grid on the host (FP64 oracle)."""
+    import oracle as O
+    from springsteel_gpu import fields
+
+    w = dict(WORKLOADS[wl])
+    gp = _params(wl)
+    gp1 = fields.config2_params(num_cells=w["num_cells"], kDim=w["kDim"], nvars=1)
+    o = O.OracleGrid(gp1.to_abi())
+    O.set_threads(threads)
+    pts = o.gridpoints()
+    ph = np.zeros(o.physical_shape, order="F")
+    ph[:, 0, 0] = fields.blob_sum(pts, seed=2000, zmax=20000.0)
+    t0 = time.perf_counter()
+    sp = o.spectral_transform(ph)
+    o.grid_transform(sp)
+    dt = time.perf_counter() - t0
+    del gp
+    return dt, w["nvars"]
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    wl = args.workload
+    for _ in range(args.warmup):
+        _oracle_sample(wl, threads)
+    times = []
+    for _ in range(args.steps):
+        dt, nv = _oracle_sample(wl, threads)
+        times.append(dt * nv)  # one full round trip = nv variables
+    per = sum(times) / len(times)
+    val = 1.0 / per
+    from springsteel_gpu import fields  # noqa: F401
+
+    line = {
+        "impl": "reference", "metric": "RLZ transforms/s", "value": val, "unit": "round trips/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[wl], "sample": "1 variable round trip per step, scaled by nvars"},
+        "cpu_baseline": {"value": val, "unit": "round trips/s", "cores": threads, "kind": "port",
+                         "sample": "one of %d variables per step (FP64 C port of the reference path, OpenMP "
+                                   "over rings/columns), time x nvars" % WORKLOADS[wl]["nvars"]},
+        "e2e": {"value": val, "unit": "round trips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Julia/FFTW are not installed; the reference arm runs the oracle's C restatement",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import springsteel_gpu as S
+    from springsteel_gpu import abi, fields
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    lib = S.load_library()
+    wl = args.workload
+    gp = _params(wl)
+    grid = S.createGrid(gp)
+    dims = grid.dims
+    w = 8 if gp.precision == "f64" else 4
+    pts = S.getGridpoints(grid)
+    u = fields.rlz_blob_fields(pts, dims["nvars"], base_seed=2 + rank, zmax=20000.0)
+    host_dtype = np.float64 if w == 8 else np.float32
+    # pinned host buffers for the end-to-end leg
+    h_in = torch.from_numpy(np.ascontiguousarray(u.T.astype(host_dtype))).pin_memory()
+    n_out = dims["n_physical"] * dims["nvars"] * dims["nslots"]
+    h_out = torch.empty(n_out, dtype=torch.float64 if w == 8 else torch.float32).pin_memory()
+    dt_code = abi.SS_DTYPE_F64 if w == 8 else abi.SS_DTYPE_F32
+    h2d = h_in.numel() * h_in.element_size()
+    d2h = h_out.numel() * h_out.element_size()
+
+    def chk(st):
+        S._check(st)
+
+    chk(lib.ss_upload_physical(grid.handle, C.c_void_p(h_in.data_ptr()), dt_code, 1, None))
+    sptr = grid.stream()
+    stream = torch.cuda.ExternalStream(sptr)
+
+    def step():
+        chk(lib.ss_spectral_transform(grid.handle, None))
+        chk(lib.ss_grid_transform(grid.handle, None))
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    grid.synchronize()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        grid.synchronize()
+
+    # ---- device-resident timed region (with live stage events)
+    chk(lib.ss_grid_profile(grid.handle, 1))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        ev1.synchronize()
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    stage_ms = (C.c_double * 6)()
+    launches = (C.c_int64 * 6)()
+    chk(lib.ss_grid_profile_read(grid.handle, stage_ms, launches))
+    chk(lib.ss_grid_profile(grid.handle, 0))
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * args.steps / (ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        chk(lib.ss_upload_physical(grid.handle, C.c_void_p(h_in.data_ptr()), dt_code, 1, None))
+        step()
+        chk(lib.ss_download_physical(grid.handle, C.c_void_p(h_out.data_ptr()), dt_code, 0, None))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = ws * e2e_steps / e2e_s
+
+    # ---- roofline of the dominant stage
+    sb = _stage_bytes(dims, w)
+    names = abi.STAGES
+    per_step_ms = {names[i]: stage_ms[i] / args.steps for i in range(6)}
+    dom = max(per_step_ms, key=per_step_ms.get)
+    peak, peak_kind = _peaks()
+    achieved = sb[dom] / (per_step_ms[dom] * 1e-3) / 1e9
+    path_gbs = _bytes_per_roundtrip(dims, w) / (ms_step * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "algorithmic_bytes_per_launch": sb[dom],
+            "stage_ms_per_step": per_step_ms,
+            "path_achieved_gbs": path_gbs, "path_frac": path_gbs / peak}
+    gpu_launches = int(sum(launches[i] for i in range(6)))
+
+    line = {
+        "metric": "RLZ transforms/s", "value": value, "unit": "round trips/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if w == 8 else "f32",
+        "data": "synthetic", "config": dict(_config(wl, dims), parallelism="replicas" if ws > 1 else "single"),
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_val, "unit": "round trips/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps},
+        "gpu_launches": gpu_launches,
+        "roofline": roof,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        dt, nv = _oracle_sample(wl, threads)
+        line["cpu_baseline"] = {
+            "value": 1.0 / (dt * nv), "unit": "round trips/s", "cores": threads, "kind": "port",
+            "sample": "one of %d variables of the same grid, forward+inverse, FP64 C port (oracle), "
+                      "%.2f s, scaled x%d" % (nv, dt, nv)}
+    grid.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="rlz200-f64", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

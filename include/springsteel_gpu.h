@@ -179,6 +179,24 @@ int32_t ss_grid_clear_ahat(ss_grid *grid);
 
 int32_t ss_grid_synchronize(ss_grid *grid);
 
+/* ---- stage timing (the library's own instrumentation; no reference
+ * counterpart: the reference times whole calls with BenchmarkTools,
+ * bench/bench_grids.jl:20-38).  With profiling on, CUDA events bracket every
+ * stage on the stream it runs on; reading synchronizes and returns the
+ * accumulated milliseconds and the kernel launches of each stage since the
+ * last ss_grid_profile(grid, 1). */
+enum {
+    SS_STAGE_CHEB_FWD = 0,   /* CBtransform! columns            */
+    SS_STAGE_RING_FWD = 1,   /* FBtransform! rings              */
+    SS_STAGE_SB = 2,         /* SBtransform! per spectral slot  */
+    SS_STAGE_SA_SI = 3,      /* SAtransform! + SI/SIx/SIxx      */
+    SS_STAGE_RING_INV = 4,   /* FAtransform! + FI/FIx/FIxx      */
+    SS_STAGE_CHEB_INV = 5,   /* CAtransform! + CI/CIx/CIxx      */
+    SS_NSTAGES = 6
+};
+int32_t ss_grid_profile(ss_grid *grid, int32_t enable);
+int32_t ss_grid_profile_read(ss_grid *grid, double *ms, int64_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,43 @@ struct ss_grid {
     std::vector<RingBucket> buckets;
     std::vector<void *> allocs;
     std::vector<SplineHost> spl_host;
+    // stage instrumentation
+    int profiling = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    struct Mark { int stage; cudaEvent_t a, b; };
+    std::vector<Mark> marks;
+    int64_t launches[SS_NSTAGES] = {0, 0, 0, 0, 0, 0};
+    double stage_ms[SS_NSTAGES] = {0, 0, 0, 0, 0, 0};
+};
+
+static cudaEvent_t next_event(ss_grid *g) {
+    if (g->ev_used == g->ev_pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        g->ev_pool.push_back(e);
+    }
+    return g->ev_pool[g->ev_used++];
+}
+// brackets one stage with events when profiling is on
+struct StageScope {
+    ss_grid *g;
+    int stage;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    StageScope(ss_grid *g_, int s_, cudaStream_t st_) : g(g_), stage(s_), st(st_) {
+        if (g->profiling) {
+            a = next_event(g);
+            cudaEventRecord(a, st);
+        }
+    }
+    ~StageScope() {
+        if (g->profiling) {
+            cudaEvent_t b = next_event(g);
+            cudaEventRecord(b, st);
+            g->marks.push_back({stage, a, b});
+        }
+    }
 };
 
 #define CUDA_TRY(expr)                                                                      \
@@ -102,6 +139,7 @@ static int32_t upload_vec(ss_grid *g, V **dst, const std::vector<V> &src) {
 static void free_grid(ss_grid *g) {
     if (!g) return;
     if (g->stream) cudaStreamSynchronize(g->stream);
+    for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
     for (void *p : g->allocs) cudaFree(p);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
@@ -306,7 +344,9 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
         P.jDim = d.jDim; P.np = d.n_physical; P.iDim = (int)d.iDim; P.bk = bk; P.nvars = nv;
         const int N = (int)d.kDim, half = (N + 1) / 2;
         size_t smem = (size_t(64) * N + size_t(bk) * half) * sizeof(T);
+        StageScope sc(g, SS_STAGE_CHEB_FWD, st);
         CUDA_TRY(launch_cheb_forward<T>(P, smem, st));
+        g->launches[SS_STAGE_CHEB_FWD]++;
     }
     RingLaunch L{};
     L.rings = g->d_rings;
@@ -317,10 +357,14 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
     L.in_item_stride = d.n_physical;
     L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
     L.nitems = g->nitems; L.nvars = nv; L.bk = bk; L.rlz = g->rlz;
-    for (const RingBucket &bkt : g->buckets) {
-        L.ring_list = g->d_ring_list + bkt.offset;
-        size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
-        CUDA_TRY(launch_ring_forward<T>(L, bkt.count, g->nitems, smem, st));
+    {
+        StageScope sc(g, SS_STAGE_RING_FWD, st);
+        for (const RingBucket &bkt : g->buckets) {
+            L.ring_list = g->d_ring_list + bkt.offset;
+            size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
+            CUDA_TRY(launch_ring_forward<T>(L, bkt.count, g->nitems, smem, st));
+            g->launches[SS_STAGE_RING_FWD]++;
+        }
     }
     SbLaunch S{};
     S.F = g->F; S.spec = g->spec; S.spl = g->d_spl; S.fofs = g->d_fofs;
@@ -329,7 +373,11 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
     S.frows = g->frows; S.nspec = d.n_spectral;
     S.iDim = (int)d.iDim; S.b = (int)d.b_iDim; S.mubar = g->p.mubar; S.pOL = g->pOL; S.K = (int)d.kDim_wn;
     S.nslots_z = g->nslots_z; S.bk = bk; S.filtered = g->filtered;
-    CUDA_TRY(launch_sb_project<T>(S, g->nitems, st));
+    {
+        StageScope sc(g, SS_STAGE_SB, st);
+        CUDA_TRY(launch_sb_project<T>(S, g->nitems, st));
+        g->launches[SS_STAGE_SB]++;
+    }
     return SS_OK;
 }
 
@@ -345,7 +393,11 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
     int nmax = 0;
     for (auto &sh : g->spl_host) nmax = std::max(nmax, sh.Min);
     size_t smem = (size_t(32) * A.ld + size_t(5) * nmax) * sizeof(double);
-    CUDA_TRY(launch_sa_si<T>(A, g->nitems, smem, st));
+    {
+        StageScope sc(g, SS_STAGE_SA_SI, st);
+        CUDA_TRY(launch_sa_si<T>(A, g->nitems, smem, st));
+        g->launches[SS_STAGE_SA_SI]++;
+    }
 
     RingLaunch L{};
     L.rings = g->d_rings;
@@ -355,10 +407,14 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
     L.out = g->rlz ? g->H : g->phys;
     L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
     L.nitems = g->nitems; L.nvars = nv; L.bk = bk; L.rlz = g->rlz;
-    for (const RingBucket &bkt : g->buckets) {
-        L.ring_list = g->d_ring_list + bkt.offset;
-        size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
-        CUDA_TRY(launch_ring_inverse<T>(L, bkt.count, g->nitems, sm, st));
+    {
+        StageScope sc(g, SS_STAGE_RING_INV, st);
+        for (const RingBucket &bkt : g->buckets) {
+            L.ring_list = g->d_ring_list + bkt.offset;
+            size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
+            CUDA_TRY(launch_ring_inverse<T>(L, bkt.count, g->nitems, sm, st));
+            g->launches[SS_STAGE_RING_INV]++;
+        }
     }
     if (g->rlz) {
         ChebLaunch P{};
@@ -366,7 +422,9 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
         P.jDim = d.jDim; P.np = d.n_physical; P.iDim = (int)d.iDim; P.bk = bk; P.nvars = nv;
         const int N = (int)d.kDim, half = (N + 1) / 2, ne = (N + 1) / 2, no = std::max(N / 2, 1);
         size_t sm = (size_t(128) * N + size_t(half) * ne + size_t(half) * no + size_t(64) * bk) * sizeof(T);
+        StageScope sc(g, SS_STAGE_CHEB_INV, st);
         CUDA_TRY(launch_cheb_inverse<T>(P, sm, st));
+        g->launches[SS_STAGE_CHEB_INV]++;
     }
     return SS_OK;
 }
@@ -595,6 +653,33 @@ int32_t ss_grid_clear_ahat(ss_grid *g) {
         cudaFree(g->d_ahat);
         g->allocs.erase(std::remove(g->allocs.begin(), g->allocs.end(), (void *)g->d_ahat), g->allocs.end());
         g->d_ahat = nullptr;
+    }
+    return SS_OK;
+}
+
+int32_t ss_grid_profile(ss_grid *g, int32_t enable) {
+    CHECK_GRID(g);
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    g->profiling = enable ? 1 : 0;
+    g->marks.clear();
+    g->ev_used = 0;
+    for (int i = 0; i < SS_NSTAGES; i++) { g->launches[i] = 0; g->stage_ms[i] = 0.0; }
+    return SS_OK;
+}
+
+int32_t ss_grid_profile_read(ss_grid *g, double *ms, int64_t *launches) {
+    CHECK_GRID(g);
+    for (auto &m : g->marks) {
+        CUDA_TRY(cudaEventSynchronize(m.b));
+        float t = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&t, m.a, m.b));
+        g->stage_ms[m.stage] += t;
+    }
+    g->marks.clear();
+    g->ev_used = 0;
+    for (int i = 0; i < SS_NSTAGES; i++) {
+        if (ms) ms[i] = g->stage_ms[i];
+        if (launches) launches[i] = g->launches[i];
     }
     return SS_OK;
 }

@@ -148,8 +148,10 @@ EXPORTED = [
     "ss_grid_stream", "ss_grid_device_physical", "ss_grid_device_spectral",
     "ss_upload_physical", "ss_download_physical", "ss_upload_spectral", "ss_download_spectral",
     "ss_spectral_transform", "ss_grid_transform", "ss_grid_set_filter", "ss_grid_set_ahat",
-    "ss_grid_clear_ahat", "ss_grid_synchronize",
+    "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
 ]
+
+STAGES = ["cheb_forward", "ring_forward", "sb_project", "sa_si", "ring_inverse", "cheb_inverse"]
 
 
 def bind(lib):
@@ -175,6 +177,8 @@ def bind(lib):
         "ss_grid_set_ahat": ([vp, i32, i32, vp], i32),
         "ss_grid_clear_ahat": ([vp], i32),
         "ss_grid_synchronize": ([vp], i32),
+        "ss_grid_profile": ([vp, i32], i32),
+        "ss_grid_profile_read": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
