@@ -194,6 +194,21 @@ enum {
     SS_STAGE_CHEB_INV = 5,   /* CAtransform! + CI/CIx/CIxx      */
     SS_NSTAGES = 6
 };
+/* ---- forward RL transform that allocates nothing ------------------------
+ * No counterpart in the reference.  spectralTransform! of an RL grid in FP64
+ * for callers that cannot call cudaMalloc where they transform (inside an
+ * open stream capture, under a host framework's own device-memory pool, in a
+ * loop that must not enter the allocator).  Input (physical slot 1,
+ * n_physical × nvars) and output (spectral, n_spectral × nvars) are the
+ * caller's device arrays; the ring-coefficient scratch is a fixed 8 MiB static
+ * device array (1,048,576 FP64 values, reserved on every GPU that loads the
+ * library until exit), so grids needing more (nvars × Σ(1+2ri) > 1,048,576)
+ * get SS_BAD_SHAPE.  The first call on a device resolves the array's device
+ * address; make that call before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race.  Asynchronous on `stream`. */
+int32_t ss_spectral_transform_noalloc(const ss_grid *grid, const double *d_physical_slot1,
+                                      double *d_spectral, void *stream);
+
 int32_t ss_grid_profile(ss_grid *grid, int32_t enable);
 int32_t ss_grid_profile_read(ss_grid *grid, double *ms, int64_t *launches);
 

@@ -692,3 +692,84 @@ int32_t ss_grid_synchronize(ss_grid *g) {
 }
 
 }  // extern "C"
+
+// ====================================================================
+// Forward RL transform without any allocation
+// --------------------------------------------------------------------
+// Some callers cannot call cudaMalloc at the point where they transform:
+// code recorded into a CUDA stream capture (allocation is not allowed while a
+// capture is open), host frameworks whose device memory is owned by their own
+// pool allocator (e.g. a Julia CUDA.jl array pool or a serving process with
+// a fixed memory budget), and real-time loops that must not touch the driver
+// allocator.  They pass their own device input and output arrays; the ring
+// coefficient scratch that ring_forward writes and sb_project reads lives in
+// the fixed array below instead of the grid's scratch buffer.
+//
+// Limit: kStaticScratchDoubles = 1,048,576 FP64 values (8 MiB), i.e.
+// nvars × Σ_r (1 + 2 ri) ≤ 1,048,576 (config 1 needs 90,600).  Every GPU that
+// loads the library keeps this 8 MiB reserved until the process exits.
+// Every call shares the array and it keeps the last call's contents; the
+// kernels write every entry they later read within one call, so nothing has
+// to start at zero.  Calls whose work overlaps on the GPU (different streams
+// without ordering, or several host threads) race on the array.
+// ====================================================================
+static constexpr size_t kStaticScratchDoubles = size_t(1) << 20;
+static __device__ __align__(256) double g_static_ring_scratch[kStaticScratchDoubles];
+
+// device address of g_static_ring_scratch, looked up once per device
+static constexpr int kMaxDevices = 64;
+static double *g_static_scratch_ptr[kMaxDevices] = {nullptr};
+
+extern "C" int32_t ss_spectral_transform_noalloc(const ss_grid *g, const double *d_physical_slot1,
+                                                 double *d_spectral, void *stream) {
+    if (!g || !d_physical_slot1 || !d_spectral) { set_error("null argument"); return SS_BAD_ARG; }
+    if (g->rlz || g->esz != 8) {
+        set_error("ss_spectral_transform_noalloc supports RL grids with SS_PREC_F64 only");
+        return SS_BAD_ARG;
+    }
+    const size_t need = size_t(g->nitems) * size_t(g->frows);
+    if (need > kStaticScratchDoubles) {
+        set_error("ss_spectral_transform_noalloc: grid needs %zu scratch values (nvars x sum(1+2ri)), "
+                  "the static scratch holds %zu", need, kStaticScratchDoubles);
+        return SS_BAD_SHAPE;
+    }
+    if (g->device < 0 || g->device >= kMaxDevices) { set_error("device index out of range"); return SS_BAD_ARG; }
+    CUDA_TRY(cudaSetDevice(g->device));
+    // first call on this device: resolve the array's device address (host code
+    // only sees a host-side stand-in for the symbol).  Do this first call
+    // before any stream capture.
+    if (!g_static_scratch_ptr[g->device]) {
+        double *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_static_ring_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error("cudaGetSymbolAddress(g_static_ring_scratch) failed: %s", cudaGetErrorString(e));
+            return SS_CUDA_ERROR;
+        }
+        g_static_scratch_ptr[g->device] = p;
+    }
+    double *scratch = g_static_scratch_ptr[g->device];
+    cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+    const ss_dims &d = g->d;
+    RingLaunch L{};
+    L.rings = g->d_rings;
+    L.ring_var_stride = d.iDim;
+    L.plans = g->d_plans; L.pool = g->d_pool; L.phase = g->d_phase;
+    L.in = d_physical_slot1;
+    L.out = scratch;
+    L.in_item_stride = d.n_physical;
+    L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
+    L.nitems = g->nitems; L.nvars = (int)d.nvars; L.bk = 1; L.rlz = 0;
+    for (const RingBucket &bkt : g->buckets) {
+        L.ring_list = g->d_ring_list + bkt.offset;
+        CUDA_TRY(launch_ring_forward<double>(L, bkt.count, g->nitems, bkt.smem_fwd_f64, st));
+    }
+    SbLaunch S{};
+    S.F = scratch; S.spec = d_spectral; S.spl = g->d_spl; S.fofs = g->d_fofs;
+    S.fw = g->filtered ? g->d_fw : nullptr;
+    S.cw = g->filtered ? g->d_cw : nullptr;
+    S.frows = g->frows; S.nspec = d.n_spectral;
+    S.iDim = (int)d.iDim; S.b = (int)d.b_iDim; S.mubar = g->p.mubar; S.pOL = g->pOL; S.K = (int)d.kDim_wn;
+    S.nslots_z = g->nslots_z; S.bk = 1; S.filtered = g->filtered;
+    CUDA_TRY(launch_sb_project<double>(S, g->nitems, st));
+    return SS_OK;
+}

@@ -149,6 +149,7 @@ EXPORTED = [
     "ss_upload_physical", "ss_download_physical", "ss_upload_spectral", "ss_download_spectral",
     "ss_spectral_transform", "ss_grid_transform", "ss_grid_set_filter", "ss_grid_set_ahat",
     "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
+    "ss_spectral_transform_noalloc",
 ]
 
 STAGES = ["cheb_forward", "ring_forward", "sb_project", "sa_si", "ring_inverse", "cheb_inverse"]
@@ -179,6 +180,7 @@ def bind(lib):
         "ss_grid_synchronize": ([vp], i32),
         "ss_grid_profile": ([vp, i32], i32),
         "ss_grid_profile_read": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)], i32),
+        "ss_spectral_transform_noalloc": ([vp, vp, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
