@@ -41,6 +41,7 @@ import numpy as np  # noqa: E402
 
 WORKLOADS = {
     "rlz200-f64": dict(num_cells=200, kDim=32, nvars=5, precision="f64"),
+    "rlz200-f64fast": dict(num_cells=200, kDim=32, nvars=5, precision="f64_fast"),
     "rlz400-f32": dict(num_cells=400, kDim=64, nvars=8, precision="f32"),
     # small case for profiling captures (same kernels, a few hundred MB)
     "rlz100-f64": dict(num_cells=100, kDim=32, nvars=2, precision="f64"),
@@ -52,8 +53,9 @@ def _params(wl):
     from springsteel_gpu import fields
 
     w = WORKLOADS[wl]
-    if w["precision"] == "f64":
-        return fields.config2_params(precision="f64", num_cells=w["num_cells"], kDim=w["kDim"], nvars=w["nvars"])
+    if w["precision"] != "f32":
+        return fields.config2_params(precision=w["precision"], num_cells=w["num_cells"], kDim=w["kDim"],
+                                     nvars=w["nvars"])
     return fields.config4_params(precision="f32", num_cells=w["num_cells"], kDim=w["kDim"], nvars=w["nvars"])
 
 
@@ -61,7 +63,10 @@ def _config(wl, dims):
     w = WORKLOADS[wl]
     return {
         "workload": "RLZ %d cells x %d Chebyshev levels, %d vars, %s" % (
-            w["num_cells"], w["kDim"], w["nvars"], "FP64" if w["precision"] == "f64" else "FP32+FP64 refinement"),
+            w["num_cells"], w["kDim"], w["nvars"],
+            {"f64_fast": "FP64 data, double-float FFT/DCT on FP32 pipes", "f64": "FP64 throughout",
+             "f32": "FP32+FP64 refinement"}[w["precision"]]),
+        "precision": w["precision"],
         "geometry": "RLZ", "num_cells": w["num_cells"], "iDim": dims["iDim"], "kDim": w["kDim"],
         "b_kDim": dims["b_kDim"], "nvars": w["nvars"], "jDim": dims["jDim"],
         "physical_points_per_var": dims["n_physical"], "spectral_per_var": dims["n_spectral"],
@@ -233,7 +238,7 @@ def run_ours(args):
     gp = _params(wl)
     grid = S.createGrid(gp)
     dims = grid.dims
-    w = 8 if gp.precision == "f64" else 4
+    w = 4 if gp.precision == "f32" else 8
     pts = S.getGridpoints(grid)
     u = fields.rlz_blob_fields(pts, dims["nvars"], base_seed=2 + rank, zmax=20000.0)
     host_dtype = np.float64 if w == 8 else np.float32

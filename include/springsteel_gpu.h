@@ -53,8 +53,11 @@ enum {
 /* ---- geometry / precision --------------------------------------------- */
 enum { SS_GEOM_RL = 1, SS_GEOM_RLZ = 2 };
 enum {
-    SS_PREC_F64 = 0,         /* every stage in IEEE binary64 */
-    SS_PREC_F32_REFINED = 1  /* binary32 bulk; FP64 factor + one FP64 refinement in SA */
+    SS_PREC_F64 = 0,         /* every stage in IEEE binary64 (parity with the reference's Float64) */
+    SS_PREC_F32_REFINED = 1, /* binary32 bulk; FP64 factor + one FP64-accurate refinement in SA */
+    SS_PREC_F64_FAST = 2     /* binary64 data, FFT/DCT bulk in double-float (two binary32, 48-bit
+                                significand) on the FP32 pipes: ~2^-48 rounding, so derivative
+                                slots carry ~1e-11 relative error instead of ~1e-14 */
 };
 enum { SS_DTYPE_F64 = 0, SS_DTYPE_F32 = 1 };
 enum { SS_QUAD_GAUSS = 0, SS_QUAD_REGULAR = 1 };
@@ -194,6 +197,43 @@ enum {
     SS_STAGE_CHEB_INV = 5,   /* CAtransform! + CI/CIx/CIxx      */
     SS_NSTAGES = 6
 };
+/* ---- many grids: batches under a CUDA graph ----------------------------
+ * No single reference counterpart: the reference transforms grids one call
+ * at a time (multipatch layers "can be transformed in parallel",
+ * src/multipatch.jl:659-661, but run serially :771-784).  A batch enqueues
+ * every grid's stages on forked streams; with use_graph the sequence is
+ * captured once into a CUDA graph and replayed.  flags & 1 autotunes the
+ * ring-kernel CTA size of each grid at creation (timed on the grid's data). */
+typedef struct ss_batch ss_batch;
+int32_t ss_batch_create(ss_grid *const *grids, int32_t n, int32_t flags, ss_batch **out);
+int32_t ss_batch_destroy(ss_batch *batch);
+/* what: 1 spectralTransform!, 2 gridTransform!, 3 both */
+int32_t ss_batch_run(ss_batch *batch, int32_t what, int32_t use_graph, void *stream);
+int32_t ss_batch_synchronize(ss_batch *batch);
+int32_t ss_batch_ring_threads(const ss_batch *batch, int32_t index, int32_t *fwd, int32_t *inv);
+
+/* ---- RL multi-patch chain ---------------------------------------------
+ * PatchChain(grids) (src/multipatch.jl:825-848) and multiGridTransform!
+ * (src/multipatch.jl:769-786) with the per-wavenumber R3X coupling of
+ * update_interface! (_rl_kernel!, src/multipatch.jl:417-478).  Grids are
+ * given in spatial order; at each interface the coarser patch is primary
+ * (NaturalBC side), the finer secondary (FixedBC side); DX ratio 1:1 or 2:1. */
+typedef struct ss_chain ss_chain;
+int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **out);
+int32_t ss_chain_destroy(ss_chain *chain);
+int32_t ss_multi_grid_transform(ss_chain *chain, void *stream);
+
+/* ---- radial tiles ------------------------------------------------------
+ * sumSpectralTile! (set = 0) / the write of setSpectralTile! (set = 1),
+ * src/tiling.jl:1040-1330: add (or write) a tile's spectral blocks into the
+ * patch at the tile's spectralIndexL; the 3 overlapping coefficients of
+ * adjacent tiles form the halo sum.  ss_tile_copy_physical moves the tile's
+ * rings of a physical slot (0 = all) between patch and tile (direction 0:
+ * patch → tile, 1: tile → patch). */
+int32_t ss_tile_sum_spectral(ss_grid *patch, const ss_grid *tile, int32_t set, void *stream);
+int32_t ss_tile_copy_physical(ss_grid *patch, ss_grid *tile, int32_t slot, int32_t direction, void *stream);
+int32_t ss_grid_zero_spectral(ss_grid *grid, void *stream);
+
 /* ---- forward RL transform that allocates nothing ------------------------
  * No counterpart in the reference.  spectralTransform! of an RL grid in FP64
  * for callers that cannot call cudaMalloc where they transform (inside an

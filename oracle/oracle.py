@@ -349,3 +349,34 @@ def cheb_mish(zDim, zmin, zmax):
     z = np.zeros(zDim)
     _check(lib().or_cheb_mish(zDim, zmin, zmax, _ptr(z)))
     return z
+
+
+class OracleChain:
+    """PatchChain + multiGridTransform! on the oracle (src/multipatch.jl)."""
+
+    def __init__(self, grids):
+        L = lib()
+        L.or_chain_create.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]
+        L.or_chain_create.restype = C.c_int32
+        L.or_chain_destroy.argtypes = [C.c_void_p]
+        L.or_chain_destroy.restype = None
+        L.or_multi_grid_transform.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.or_multi_grid_transform.restype = C.c_int32
+        self.grids = list(grids)
+        arr = (C.c_void_p * len(self.grids))(*[g.h.value for g in self.grids])
+        h = C.c_void_p()
+        _check(L.or_chain_create(arr, len(self.grids), C.byref(h)))
+        self.h = h
+
+    def multi_grid_transform(self, spectrals):
+        sp = [np.asfortranarray(s, dtype=np.float64) for s in spectrals]
+        ph = [np.zeros(g.physical_shape, order="F") for g in self.grids]
+        sarr = (C.c_void_p * len(sp))(*[s.ctypes.data for s in sp])
+        parr = (C.c_void_p * len(ph))(*[p.ctypes.data for p in ph])
+        _check(lib().or_multi_grid_transform(self.h, sarr, parr))
+        return ph
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_chain_destroy(self.h)
+            self.h = None

@@ -1392,3 +1392,136 @@ int32_t or_grid_transform(or_grid *g, const double *spec, double *phys) {
     }
     return SS_OK;
 }
+
+/* ======================================================================
+ * RL multi-patch chain (src/multipatch.jl)
+ * ====================================================================== */
+
+typedef struct {
+    int primary, secondary;     /* patch indices */
+    int pside, sside;           /* 0 = left, 1 = right */
+    double C[9];                /* 3×3 coupling matrix, row-major */
+    int node[3];                /* 0-based indices into the primary's a */
+} or_iface;
+
+struct or_chain {
+    int n;
+    or_grid **g;
+    int nif;
+    or_iface *ifs;
+    int nlayers;
+    int *layer_of;              /* patch → topological layer */
+    double **state;             /* per patch: nvars × 3 × b (spline objects k0, real, imag .ahat) */
+};
+typedef struct or_chain or_chain;
+
+/* _build_coupling_matrix, src/multipatch.jl:42-53 (COUPLING_MATRIX_1X / _2X :21-33) */
+static int coupling_matrix(double pDX, double sDX, double *C) {
+    double ratio = pDX / sDX, tol = 1e-12 * (pDX > sDX ? pDX : sDX);
+    static const double M1[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    static const double M2[9] = {0.5, 0.5, 0.0, 0.125, 0.75, 0.125, 0.0, 0.5, 0.5};
+    if (fabs(ratio - 1.0) < tol) { memcpy(C, M1, sizeof M1); return SS_OK; }
+    if (fabs(ratio - 2.0) < tol) { memcpy(C, M2, sizeof M2); return SS_OK; }
+    set_err("Only 1:1 and 2:1 coarse-to-fine ratios are supported, got %g:1", ratio);
+    return SS_BAD_ARG;
+}
+
+/* PatchChain (src/multipatch.jl:825-848) + _topological_sort (:666-724) */
+int32_t or_chain_create(or_grid **grids, int32_t n, or_chain **out) {
+    *out = NULL;
+    if (n < 2) { set_err("PatchChain requires at least 2 grids, got %d", n); return SS_BAD_ARG; }
+    for (int k = 0; k < n; k++)
+        if (grids[k]->geom != SS_GEOM_RL || grids[k]->nvars != grids[0]->nvars) {
+            set_err("the chain supports RL patches with equal variable counts");
+            return SS_BAD_ARG;
+        }
+    or_chain *c = (or_chain *)calloc(1, sizeof *c);
+    c->n = n;
+    c->g = (or_grid **)malloc(sizeof(or_grid *) * (size_t)n);
+    memcpy(c->g, grids, sizeof(or_grid *) * (size_t)n);
+    c->nif = n - 1;
+    c->ifs = (or_iface *)calloc((size_t)(n - 1), sizeof(or_iface));
+    for (int k = 0; k < n - 1; k++) {
+        const or_spline *L = grids[k]->spl[0], *R = grids[k + 1]->spl[0];
+        or_iface *f = &c->ifs[k];
+        if (L->DX >= R->DX) { f->primary = k; f->secondary = k + 1; f->pside = 1; f->sside = 0; }
+        else { f->primary = k + 1; f->secondary = k; f->pside = 0; f->sside = 1; }
+        const or_spline *P = grids[f->primary]->spl[0], *S = grids[f->secondary]->spl[0];
+        int st = coupling_matrix(P->DX, S->DX, f->C);
+        if (st) { free(c->ifs); free(c->g); free(c); return st; }
+        for (int v = 0; v < grids[0]->nvars; v++)
+            if (!grids[f->secondary]->spl[v]->r3x || grids[f->primary]->spl[v]->r3x) {
+                set_err("chain interface %d: secondary needs R3X and primary must not be R3X", k);
+                free(c->ifs); free(c->g); free(c);
+                return SS_UNSUPPORTED_BC;
+            }
+        /* hollow nest node indices (src/multipatch.jl:290-316) */
+        int b = P->bDim;
+        if (f->pside == 1) { f->node[0] = b - 3; f->node[1] = b - 2; f->node[2] = b - 1; }
+        else { f->node[0] = 0; f->node[1] = 1; f->node[2] = 2; }
+    }
+    c->layer_of = (int *)calloc((size_t)n, sizeof(int));
+    /* Kahn layers: a secondary sits one layer after its latest primary */
+    int changed = 1, guard = 0;
+    while (changed && guard++ < n + 2) {
+        changed = 0;
+        for (int i = 0; i < c->nif; i++) {
+            int need = c->layer_of[c->ifs[i].primary] + 1;
+            if (c->layer_of[c->ifs[i].secondary] < need) { c->layer_of[c->ifs[i].secondary] = need; changed = 1; }
+        }
+    }
+    c->nlayers = 0;
+    for (int i = 0; i < n; i++) if (c->layer_of[i] + 1 > c->nlayers) c->nlayers = c->layer_of[i] + 1;
+    c->state = (double **)calloc((size_t)n, sizeof(double *));
+    for (int i = 0; i < n; i++)
+        c->state[i] = (double *)calloc((size_t)grids[i]->nvars * 3 * grids[i]->b, sizeof(double));
+    *out = c;
+    return SS_OK;
+}
+
+void or_chain_destroy(or_chain *c) {
+    if (!c) return;
+    for (int i = 0; i < c->n; i++) free(c->state[i]);
+    free(c->state); free(c->layer_of); free(c->ifs); free(c->g); free(c);
+}
+
+/* _rl_kernel! (src/multipatch.jl:417-478): SA of each primary wavenumber slot,
+ * 3 interface coefficients × coupling matrix, written into the secondary
+ * spline object's ahat (k0 / real / imag objects are shared by all
+ * wavenumbers) and the whole ahat vector copied into the per-wavenumber
+ * registry (src/multipatch_registry.jl:45-62). */
+static void chain_update_interface(or_chain *c, const or_iface *f, const double *spec_p) {
+    or_grid *P = c->g[f->primary], *S = c->g[f->secondary];
+    int bp = P->b, bs = S->b;
+    int Kp = P->K, Ks = S->K, Kc = Kp < Ks ? Kp : Ks;
+    double *a = (double *)malloc(sizeof(double) * (size_t)bp);
+    double *t = (double *)malloc(sizeof(double) * 3 * (size_t)bp);
+    for (int v = 0; v < S->nvars; v++) {
+        const double *sp = spec_p + (size_t)P->nspec * v;
+        for (int q = 0; q <= 2 * Kc; q++) {
+            /* q: 0 = k0, odd = real k=(q+1)/2, even = imag */
+            int obj = (q == 0) ? 0 : ((q & 1) ? 1 : 2);
+            spline_sa(P->spl[v], sp + (size_t)q * bp, NULL, a, t, t + bp, t + 2 * bp);
+            double ex[3] = {a[f->node[0]], a[f->node[1]], a[f->node[2]]};
+            double *st = c->state[f->secondary] + ((size_t)v * 3 + obj) * bs;
+            double *dst = (f->sside == 0) ? st : st + bs - 3;
+            for (int r = 0; r < 3; r++) dst[r] = f->C[r * 3] * ex[0] + f->C[r * 3 + 1] * ex[1] + f->C[r * 3 + 2] * ex[2];
+            or_grid_set_ahat(S, v, q, st);
+        }
+    }
+    free(a); free(t);
+}
+
+/* multiGridTransform! (src/multipatch.jl:769-786) */
+int32_t or_multi_grid_transform(or_chain *c, const double **spectral, double **physical) {
+    for (int L = 0; L < c->nlayers; L++) {
+        for (int i = 0; i < c->n; i++)
+            if (c->layer_of[i] == L) {
+                int st = or_grid_transform(c->g[i], spectral[i], physical[i]);
+                if (st) return st;
+            }
+        for (int k = 0; k < c->nif; k++)
+            if (c->layer_of[c->ifs[k].primary] == L) chain_update_interface(c, &c->ifs[k], spectral[c->ifs[k].primary]);
+    }
+    return SS_OK;
+}

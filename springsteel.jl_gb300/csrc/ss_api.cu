@@ -13,8 +13,10 @@
 #include <string>
 #include <vector>
 
+#include "ss_grid.h"
 #include "ss_internal.h"
 #include "ss_kernels.h"
+#include "ss_df64.cuh"
 
 namespace ss {
 static thread_local std::string g_err;
@@ -29,81 +31,6 @@ void set_error(const char *fmt, ...) {
 }  // namespace ss
 
 using namespace ss;
-
-struct RingBucket {
-    int offset;   // into the ring list
-    int count;
-    size_t smem_fwd_f64, smem_inv_f64;
-    int max_buf, max_kmax;
-};
-
-struct ss_grid {
-    ss_grid_params p{};
-    std::vector<double> l_q;
-    std::vector<ss_spline_bc> bcl, bcr;
-    std::vector<int32_t> bcb, bct, kmaxv;
-    ss_dims d{};
-    int prec = SS_PREC_F64;
-    size_t esz = 8;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int nitems = 0, nslots_z = 0, pOL = 0, rlz = 0;
-    int64_t frows = 0;
-
-    void *phys = nullptr, *spec = nullptr, *C = nullptr, *F = nullptr, *G = nullptr, *H = nullptr;
-    void *stage = nullptr;
-    size_t stage_bytes = 0;
-
-    RingDesc *d_rings = nullptr;
-    int *d_ring_list = nullptr;
-    FftPlan *d_plans = nullptr;
-    double2 *d_pool = nullptr, *d_phase = nullptr;
-    int64_t *d_fofs = nullptr;
-    SplineDev *d_spl = nullptr;
-    ChebDev *d_cheb = nullptr;
-    double *d_ahat = nullptr, *d_fw = nullptr, *d_cw = nullptr;
-    int filtered = 0;
-    std::vector<RingBucket> buckets;
-    std::vector<void *> allocs;
-    std::vector<SplineHost> spl_host;
-    // stage instrumentation
-    int profiling = 0;
-    std::vector<cudaEvent_t> ev_pool;
-    size_t ev_used = 0;
-    struct Mark { int stage; cudaEvent_t a, b; };
-    std::vector<Mark> marks;
-    int64_t launches[SS_NSTAGES] = {0, 0, 0, 0, 0, 0};
-    double stage_ms[SS_NSTAGES] = {0, 0, 0, 0, 0, 0};
-};
-
-static cudaEvent_t next_event(ss_grid *g) {
-    if (g->ev_used == g->ev_pool.size()) {
-        cudaEvent_t e;
-        cudaEventCreate(&e);
-        g->ev_pool.push_back(e);
-    }
-    return g->ev_pool[g->ev_used++];
-}
-// brackets one stage with events when profiling is on
-struct StageScope {
-    ss_grid *g;
-    int stage;
-    cudaStream_t st;
-    cudaEvent_t a = nullptr;
-    StageScope(ss_grid *g_, int s_, cudaStream_t st_) : g(g_), stage(s_), st(st_) {
-        if (g->profiling) {
-            a = next_event(g);
-            cudaEventRecord(a, st);
-        }
-    }
-    ~StageScope() {
-        if (g->profiling) {
-            cudaEvent_t b = next_event(g);
-            cudaEventRecord(b, st);
-            g->marks.push_back({stage, a, b});
-        }
-    }
-};
 
 #define CUDA_TRY(expr)                                                                      \
     do {                                                                                    \
@@ -136,6 +63,48 @@ static int32_t upload_vec(ss_grid *g, V **dst, const std::vector<V> &src) {
     return SS_OK;
 }
 
+// FP64 host tables → the compute layout of the grid (TL_F64 / TL_DF64 / TL_F32)
+static std::vector<unsigned char> real_layout(const std::vector<double> &v, int tl) {
+    std::vector<unsigned char> out;
+    if (tl == TL_F64) {
+        out.resize(v.size() * 8);
+        std::memcpy(out.data(), v.data(), out.size());
+    } else if (tl == TL_F32) {
+        out.resize(v.size() * 4);
+        float *f = (float *)out.data();
+        for (size_t i = 0; i < v.size(); i++) f[i] = (float)v[i];
+    } else {
+        out.resize(v.size() * 8);
+        float *f = (float *)out.data();
+        for (size_t i = 0; i < v.size(); i++) {
+            f[2 * i] = (float)v[i];
+            f[2 * i + 1] = (float)(v[i] - (double)f[2 * i]);
+        }
+    }
+    if (out.empty()) out.resize(16, 0);
+    return out;
+}
+// interleaved (re, im) FP64 pairs → double2 / float2 / float4 (re.hi, re.lo, im.hi, im.lo)
+static std::vector<unsigned char> cplx_layout(const std::vector<double> &v, int tl) {
+    if (tl != TL_DF64) return real_layout(v, tl);
+    std::vector<unsigned char> out(v.size() * 8);
+    float *f = (float *)out.data();
+    for (size_t i = 0; i < v.size(); i++) {
+        f[2 * i] = (float)v[i];
+        f[2 * i + 1] = (float)(v[i] - (double)f[2 * i]);
+    }
+    if (out.empty()) out.resize(16, 0);
+    return out;
+}
+static int32_t upload_bytes(ss_grid *g, const void **dst, const std::vector<unsigned char> &src) {
+    void *p = nullptr;
+    int32_t st = dev_alloc(g, &p, src.size(), false);
+    if (st) return st;
+    CUDA_TRY(cudaMemcpy(p, src.data(), src.size(), cudaMemcpyHostToDevice));
+    *dst = p;
+    return SS_OK;
+}
+
 static void free_grid(ss_grid *g) {
     if (!g) return;
     if (g->stream) cudaStreamSynchronize(g->stream);
@@ -152,7 +121,8 @@ static int32_t build_grid(ss_grid *g) {
     g->rlz = p.geometry == SS_GEOM_RLZ;
     g->pOL = p.patchOffsetL;
     g->prec = p.precision;
-    g->esz = p.precision == SS_PREC_F64 ? 8 : 4;
+    g->tl = p.precision == SS_PREC_F32_REFINED ? TL_F32 : (p.precision == SS_PREC_F64_FAST ? TL_DF64 : TL_F64);
+    g->esz = p.precision == SS_PREC_F32_REFINED ? 4 : 8;
     int kz = 1, bk = 1;
     if (g->rlz) {
         kz = p.kDim;
@@ -198,8 +168,21 @@ static int32_t build_grid(ss_grid *g) {
         if ((st = upload_vec(g, &sd.L4, sh.L4))) return st;
         if ((st = upload_vec(g, &sd.dinv, dinv))) return st;
         if ((st = upload_vec(g, &sd.PQb, sh.PQb))) return st;
-        if ((st = upload_vec(g, &sd.sbw, sh.sbw))) return st;
-        if ((st = upload_vec(g, &sd.siw, sh.siw))) return st;
+        std::vector<float> l4f(sh.L4.size()), dinvf(dinv.size());
+        for (size_t i = 0; i < l4f.size(); i++) l4f[i] = (float)sh.L4[i];
+        for (size_t i = 0; i < dinvf.size(); i++) dinvf[i] = (float)dinv[i];
+        if ((st = upload_vec(g, &sd.L4f, l4f))) return st;
+        if ((st = upload_vec(g, &sd.dinvf, dinvf))) return st;
+        {
+            std::vector<float2> ab(sh.Aopen.size());
+            for (size_t i = 0; i < ab.size(); i++) {
+                float h = (float)sh.Aopen[i];
+                ab[i] = make_float2(h, (float)(sh.Aopen[i] - (double)h));
+            }
+            if ((st = upload_vec(g, &sd.Aband_x, ab))) return st;
+        }
+        if ((st = upload_bytes(g, &sd.sbw_t, real_layout(sh.sbw, g->tl)))) return st;
+        if ((st = upload_bytes(g, &sd.siw_t, real_layout(sh.siw, g->tl)))) return st;
         if ((st = upload_vec(g, &sd.si_m0, sh.si_m0))) return st;
     }
     int32_t st = upload_vec(g, &g->d_spl, sdev);
@@ -245,13 +228,11 @@ static int32_t build_grid(ss_grid *g) {
     if ((st = upload_vec(g, &g->d_fofs, fofs))) return st;
     if ((st = upload_vec(g, &g->d_plans, plans.plans))) return st;
     {
-        std::vector<double2> pv(pool.v.size() / 2);
-        for (size_t i = 0; i < pv.size(); i++) pv[i] = make_double2(pool.v[2 * i], pool.v[2 * i + 1]);
-        if (pv.empty()) pv.push_back(make_double2(0, 0));
-        if ((st = upload_vec(g, &g->d_pool, pv))) return st;
-        std::vector<double2> ph(phase.size() / 2);
-        for (size_t i = 0; i < ph.size(); i++) ph[i] = make_double2(phase[2 * i], phase[2 * i + 1]);
-        if ((st = upload_vec(g, &g->d_phase, ph))) return st;
+        const void *pp = nullptr, *ph = nullptr;
+        if ((st = upload_bytes(g, &pp, cplx_layout(pool.v, g->tl)))) return st;
+        if ((st = upload_bytes(g, &ph, cplx_layout(phase, g->tl)))) return st;
+        g->d_pool = (void *)pp;
+        g->d_phase = (void *)ph;
     }
     // buckets of rings by shared-memory need (largest first)
     {
@@ -301,14 +282,11 @@ static int32_t build_grid(ss_grid *g) {
             ChebDev &cd = cdev[v];
             std::memset(&cd, 0, sizeof cd);
             cd.N = ch.N; cd.bk = ch.bk; cd.nrank = ch.nrank; cd.half = ch.half; cd.dscale = ch.dscale;
-            if ((st = upload_vec(g, &cd.fwd, ch.fwd))) return st;
-            if ((st = upload_vec(g, &cd.inv_e, ch.inv_e))) return st;
-            if ((st = upload_vec(g, &cd.inv_o, ch.inv_o))) return st;
-            std::vector<double> gu = ch.gu, gv = ch.gv;
-            if (gu.empty()) gu.push_back(0.0);
-            if (gv.empty()) gv.push_back(0.0);
-            if ((st = upload_vec(g, &cd.gu, gu))) return st;
-            if ((st = upload_vec(g, &cd.gv, gv))) return st;
+            if ((st = upload_bytes(g, &cd.fwd_t, real_layout(ch.fwd, g->tl)))) return st;
+            if ((st = upload_bytes(g, &cd.inv_e_t, real_layout(ch.inv_e, g->tl)))) return st;
+            if ((st = upload_bytes(g, &cd.inv_o_t, real_layout(ch.inv_o, g->tl)))) return st;
+            if ((st = upload_bytes(g, &cd.gu_t, real_layout(ch.gu, g->tl)))) return st;
+            if ((st = upload_bytes(g, &cd.gv_t, real_layout(ch.gv, g->tl)))) return st;
         }
         if ((st = upload_vec(g, &g->d_cheb, cdev))) return st;
     }
@@ -334,18 +312,18 @@ static int32_t build_grid(ss_grid *g) {
 }
 
 // ---------------------------------------------------------------- launches
-template <typename T>
+template <typename P, typename T>
 static int32_t run_forward(ss_grid *g, cudaStream_t st) {
     const ss_dims &d = g->d;
     const int nv = (int)d.nvars, bk = (int)d.b_kDim;
     if (g->rlz) {
-        ChebLaunch P{};
-        P.in = g->phys; P.out = g->C; P.cheb = g->d_cheb; P.rings = g->d_rings;
-        P.jDim = d.jDim; P.np = d.n_physical; P.iDim = (int)d.iDim; P.bk = bk; P.nvars = nv;
+        ChebLaunch Cl{};
+        Cl.in = g->phys; Cl.out = g->C; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
+        Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = bk; Cl.nvars = nv;
         const int N = (int)d.kDim, half = (N + 1) / 2;
-        size_t smem = (size_t(64) * N + size_t(bk) * half) * sizeof(T);
+        size_t smem = (size_t(64) * (N | 1) + size_t(bk) * half) * sizeof(T);
         StageScope sc(g, SS_STAGE_CHEB_FWD, st);
-        CUDA_TRY(launch_cheb_forward<T>(P, smem, st));
+        CUDA_TRY((launch_cheb_forward<P, T>(Cl, smem, st)));
         g->launches[SS_STAGE_CHEB_FWD]++;
     }
     RingLaunch L{};
@@ -362,7 +340,7 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
         for (const RingBucket &bkt : g->buckets) {
             L.ring_list = g->d_ring_list + bkt.offset;
             size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
-            CUDA_TRY(launch_ring_forward<T>(L, bkt.count, g->nitems, smem, st));
+            CUDA_TRY((launch_ring_forward<P, T>(L, bkt.count, g->nitems, smem, g->ring_threads_fwd, st)));
             g->launches[SS_STAGE_RING_FWD]++;
         }
     }
@@ -375,13 +353,13 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
     S.nslots_z = g->nslots_z; S.bk = bk; S.filtered = g->filtered;
     {
         StageScope sc(g, SS_STAGE_SB, st);
-        CUDA_TRY(launch_sb_project<T>(S, g->nitems, st));
+        CUDA_TRY((launch_sb_project<P, T>(S, g->nitems, st)));
         g->launches[SS_STAGE_SB]++;
     }
     return SS_OK;
 }
 
-template <typename T>
+template <typename P, typename T>
 static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
     const ss_dims &d = g->d;
     const int nv = (int)d.nvars, bk = (int)d.b_kDim;
@@ -392,10 +370,12 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
     A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = bk; A.nitems = g->nitems;
     int nmax = 0;
     for (auto &sh : g->spl_host) nmax = std::max(nmax, sh.Min);
-    size_t smem = (size_t(32) * A.ld + size_t(5) * nmax) * sizeof(double);
+    const size_t ssz = (sizeof(T) == 4) ? 4 : 8;  // solve type: float (FP32 mode) or double
+    size_t smem = (size_t(32) * A.ld + size_t(5) * nmax) * ssz;
+    if (g->tl != TL_F64) smem += size_t(32) * A.ld * ssz;  // FP32 residuals / df64 coefficients
     {
         StageScope sc(g, SS_STAGE_SA_SI, st);
-        CUDA_TRY(launch_sa_si<T>(A, g->nitems, smem, st));
+        CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
         g->launches[SS_STAGE_SA_SI]++;
     }
 
@@ -412,22 +392,35 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
         for (const RingBucket &bkt : g->buckets) {
             L.ring_list = g->d_ring_list + bkt.offset;
             size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
-            CUDA_TRY(launch_ring_inverse<T>(L, bkt.count, g->nitems, sm, st));
+            CUDA_TRY((launch_ring_inverse<P, T>(L, bkt.count, g->nitems, sm, g->ring_threads_inv, st)));
             g->launches[SS_STAGE_RING_INV]++;
         }
     }
     if (g->rlz) {
-        ChebLaunch P{};
-        P.in = g->H; P.out = g->phys; P.cheb = g->d_cheb; P.rings = g->d_rings;
-        P.jDim = d.jDim; P.np = d.n_physical; P.iDim = (int)d.iDim; P.bk = bk; P.nvars = nv;
+        ChebLaunch Cl{};
+        Cl.in = g->H; Cl.out = g->phys; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
+        Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = bk; Cl.nvars = nv;
         const int N = (int)d.kDim, half = (N + 1) / 2, ne = (N + 1) / 2, no = std::max(N / 2, 1);
-        size_t sm = (size_t(128) * N + size_t(half) * ne + size_t(half) * no + size_t(64) * bk) * sizeof(T);
+        size_t sm = (size_t(128) * (N | 1) + size_t(half) * ne + size_t(half) * no + size_t(64) * (bk | 1)) * sizeof(T);
         StageScope sc(g, SS_STAGE_CHEB_INV, st);
-        CUDA_TRY(launch_cheb_inverse<T>(P, sm, st));
+        CUDA_TRY((launch_cheb_inverse<P, T>(Cl, sm, st)));
         g->launches[SS_STAGE_CHEB_INV]++;
     }
     return SS_OK;
 }
+
+namespace ss {
+int32_t grid_forward(ss_grid *g, cudaStream_t s) {
+    if (g->tl == TL_DF64) return run_forward<double, df64>(g, s);
+    if (g->tl == TL_F64) return run_forward<double, double>(g, s);
+    return run_forward<float, float>(g, s);
+}
+int32_t grid_inverse(ss_grid *g, cudaStream_t s) {
+    if (g->tl == TL_DF64) return run_inverse<double, df64>(g, s);
+    if (g->tl == TL_F64) return run_inverse<double, double>(g, s);
+    return run_inverse<float, float>(g, s);
+}
+}  // namespace ss
 
 // ---------------------------------------------------------------- helpers
 __global__ void convert_kernel_f64_to_f32(const double *in, float *out, size_t n) {
@@ -507,7 +500,10 @@ int32_t ss_grid_create(const ss_grid_params *params, ss_grid **out) {
     if (!params) { set_error("null params"); return SS_BAD_ARG; }
     const ss_grid_params &p = *params;
     if (p.geometry != SS_GEOM_RL && p.geometry != SS_GEOM_RLZ) { set_error("geometry must be RL or RLZ"); return SS_BAD_ARG; }
-    if (p.precision != SS_PREC_F64 && p.precision != SS_PREC_F32_REFINED) { set_error("unknown precision"); return SS_BAD_ARG; }
+    if (p.precision != SS_PREC_F64 && p.precision != SS_PREC_F32_REFINED && p.precision != SS_PREC_F64_FAST) {
+        set_error("unknown precision");
+        return SS_BAD_ARG;
+    }
     if (p.nvars < 1 || p.num_cells < 1 || p.mubar < 1 || p.patchOffsetL < 0) { set_error("bad sizes"); return SS_BAD_SHAPE; }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -607,12 +603,12 @@ int32_t ss_download_spectral(ss_grid *g, void *host, int32_t dtype, void *stream
 
 int32_t ss_spectral_transform(ss_grid *g, void *stream) {
     CHECK_GRID(g);
-    return g->esz == 8 ? run_forward<double>(g, pick(g, stream)) : run_forward<float>(g, pick(g, stream));
+    return grid_forward(g, pick(g, stream));
 }
 
 int32_t ss_grid_transform(ss_grid *g, void *stream) {
     CHECK_GRID(g);
-    return g->esz == 8 ? run_inverse<double>(g, pick(g, stream)) : run_inverse<float>(g, pick(g, stream));
+    return grid_inverse(g, pick(g, stream));
 }
 
 int32_t ss_grid_set_filter(ss_grid *g, int32_t var, const double *fw, const double *cw) {
@@ -761,7 +757,8 @@ extern "C" int32_t ss_spectral_transform_noalloc(const ss_grid *g, const double 
     L.nitems = g->nitems; L.nvars = (int)d.nvars; L.bk = 1; L.rlz = 0;
     for (const RingBucket &bkt : g->buckets) {
         L.ring_list = g->d_ring_list + bkt.offset;
-        CUDA_TRY(launch_ring_forward<double>(L, bkt.count, g->nitems, bkt.smem_fwd_f64, st));
+        if (g->tl == TL_DF64) CUDA_TRY((launch_ring_forward<double, df64>(L, bkt.count, g->nitems, bkt.smem_fwd_f64, g->ring_threads_fwd, st)));
+        else CUDA_TRY((launch_ring_forward<double, double>(L, bkt.count, g->nitems, bkt.smem_fwd_f64, g->ring_threads_fwd, st)));
     }
     SbLaunch S{};
     S.F = scratch; S.spec = d_spectral; S.spl = g->d_spl; S.fofs = g->d_fofs;
@@ -770,6 +767,7 @@ extern "C" int32_t ss_spectral_transform_noalloc(const ss_grid *g, const double 
     S.frows = g->frows; S.nspec = d.n_spectral;
     S.iDim = (int)d.iDim; S.b = (int)d.b_iDim; S.mubar = g->p.mubar; S.pOL = g->pOL; S.K = (int)d.kDim_wn;
     S.nslots_z = g->nslots_z; S.bk = 1; S.filtered = g->filtered;
-    CUDA_TRY(launch_sb_project<double>(S, g->nitems, st));
+    if (g->tl == TL_DF64) CUDA_TRY((launch_sb_project<double, df64>(S, g->nitems, st)));
+    else CUDA_TRY((launch_sb_project<double, double>(S, g->nitems, st)));
     return SS_OK;
 }

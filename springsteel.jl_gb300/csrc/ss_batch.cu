@@ -1,0 +1,428 @@
+// ss_batch.cu — many grids per launch sequence: batches under a CUDA graph
+// (with an autotuner for the ring-kernel CTA size), RL multi-patch chains
+// (PatchChain / multiGridTransform!, src/multipatch.jl), and radial tiles
+// with halo sums (sumSpectralTile!, src/tiling.jl:1048-1136).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ss_df64.cuh"
+#include "ss_grid.h"
+#include "ss_kernels.h"
+
+using namespace ss;
+
+#define CUDA_TRY(expr)                                                                      \
+    do {                                                                                    \
+        cudaError_t _e = (expr);                                                            \
+        if (_e != cudaSuccess) {                                                            \
+            set_error("%s failed: %s", #expr, cudaGetErrorString(_e));                      \
+            return (_e == cudaErrorMemoryAllocation) ? SS_OUT_OF_MEMORY : SS_CUDA_ERROR;   \
+        }                                                                                   \
+    } while (0)
+
+// ====================================================================== batch
+struct ss_batch {
+    std::vector<ss_grid *> grids;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaStream_t> side;  // fork-join branches of the captured graph
+    std::vector<cudaEvent_t> ev;
+    cudaGraph_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+static int32_t run_direction(ss_grid *g, int what, cudaStream_t st) {
+    int32_t r = SS_OK;
+    if (what & 1) r = grid_forward(g, st);
+    if (r == SS_OK && (what & 2)) r = grid_inverse(g, st);
+    return r;
+}
+
+// Autotuner: time each candidate CTA size of the ring kernels on the grid's
+// own data and keep the fastest per direction.
+static int32_t autotune_grid(ss_grid *g, cudaStream_t st) {
+    const int cand[3] = {64, 128, 256};
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    for (int dir = 1; dir <= 2; dir++) {
+        float best = 1e30f;
+        int best_t = 256;
+        for (int c = 0; c < 3; c++) {
+            if (dir == 1) g->ring_threads_fwd = cand[c];
+            else g->ring_threads_inv = cand[c];
+            int32_t r = run_direction(g, dir, st);  // warm-up
+            if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
+            CUDA_TRY(cudaEventRecord(a, st));
+            for (int rep = 0; rep < 2; rep++) {
+                r = run_direction(g, dir, st);
+                if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
+            }
+            CUDA_TRY(cudaEventRecord(b, st));
+            CUDA_TRY(cudaEventSynchronize(b));
+            float ms = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+            if (ms < best) { best = ms; best_t = cand[c]; }
+        }
+        if (dir == 1) g->ring_threads_fwd = best_t;
+        else g->ring_threads_inv = best_t;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return SS_OK;
+}
+
+extern "C" int32_t ss_batch_destroy(ss_batch *bt);
+extern "C" int32_t ss_batch_create(ss_grid *const *grids, int32_t n, int32_t flags, ss_batch **out) {
+    if (!out || !grids || n < 1) { set_error("bad batch arguments"); return SS_BAD_ARG; }
+    *out = nullptr;
+    ss_batch *bt = new ss_batch();
+    for (int i = 0; i < n; i++) {
+        if (!grids[i]) { delete bt; set_error("null grid in batch"); return SS_BAD_ARG; }
+        bt->grids.push_back(grids[i]);
+    }
+    bt->device = grids[0]->device;
+    cudaSetDevice(bt->device);
+    if (cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete bt;
+        set_error("cudaStreamCreate failed");
+        return SS_CUDA_ERROR;
+    }
+    const int nside = std::min(n, 8);
+    for (int i = 0; i < nside; i++) {
+        cudaStream_t s;
+        cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        bt->side.push_back(s);
+    }
+    for (int i = 0; i < nside + 1; i++) {
+        cudaEvent_t e;
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        bt->ev.push_back(e);
+    }
+    if (flags & 1) {
+        for (ss_grid *g : bt->grids) {
+            int32_t r = autotune_grid(g, bt->stream);
+            if (r) { ss_batch_destroy(bt); return r; }
+        }
+    }
+    *out = bt;
+    return SS_OK;
+}
+
+extern "C" int32_t ss_batch_destroy(ss_batch *bt) {
+    if (!bt) return SS_OK;
+    cudaSetDevice(bt->device);
+    cudaStreamSynchronize(bt->stream);
+    for (int i = 0; i < 4; i++) {
+        if (bt->exec[i]) cudaGraphExecDestroy(bt->exec[i]);
+        if (bt->graph[i]) cudaGraphDestroy(bt->graph[i]);
+    }
+    for (cudaStream_t s : bt->side) cudaStreamDestroy(s);
+    for (cudaEvent_t e : bt->ev) cudaEventDestroy(e);
+    cudaStreamDestroy(bt->stream);
+    delete bt;
+    return SS_OK;
+}
+
+// Enqueue every grid's transforms: grids round-robin over the side streams,
+// forked from and joined back into `st` (the graph gets parallel branches).
+static int32_t enqueue_batch(ss_batch *bt, int what, cudaStream_t st) {
+    const int nside = (int)bt->side.size();
+    CUDA_TRY(cudaEventRecord(bt->ev[0], st));
+    for (int i = 0; i < nside; i++) CUDA_TRY(cudaStreamWaitEvent(bt->side[i], bt->ev[0], 0));
+    for (size_t i = 0; i < bt->grids.size(); i++) {
+        int32_t r = run_direction(bt->grids[i], what, bt->side[i % nside]);
+        if (r) return r;
+    }
+    for (int i = 0; i < nside; i++) {
+        CUDA_TRY(cudaEventRecord(bt->ev[1 + i], bt->side[i]));
+        CUDA_TRY(cudaStreamWaitEvent(st, bt->ev[1 + i], 0));
+    }
+    return SS_OK;
+}
+
+extern "C" int32_t ss_batch_run(ss_batch *bt, int32_t what, int32_t use_graph, void *stream) {
+    if (!bt || what < 1 || what > 3) { set_error("bad batch run arguments"); return SS_BAD_ARG; }
+    cudaSetDevice(bt->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : bt->stream;
+    for (ss_grid *g : bt->grids)
+        if (g->profiling) { set_error("disable stage profiling on batched grids"); return SS_BAD_ARG; }
+    if (!use_graph) return enqueue_batch(bt, what, st);
+    if (!bt->exec[what]) {
+        // capture on the batch's own stream, then launch the graph on `st`
+        CUDA_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeRelaxed));
+        int32_t r = enqueue_batch(bt, what, bt->stream);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(bt->stream, &graph);
+        if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+        if (e != cudaSuccess) { set_error("graph capture failed: %s", cudaGetErrorString(e)); return SS_CUDA_ERROR; }
+        bt->graph[what] = graph;
+        CUDA_TRY(cudaGraphInstantiate(&bt->exec[what], graph, 0));
+    }
+    CUDA_TRY(cudaGraphLaunch(bt->exec[what], st));
+    return SS_OK;
+}
+
+extern "C" int32_t ss_batch_synchronize(ss_batch *bt) {
+    if (!bt) { set_error("null batch"); return SS_BAD_ARG; }
+    cudaSetDevice(bt->device);
+    CUDA_TRY(cudaStreamSynchronize(bt->stream));
+    return SS_OK;
+}
+
+extern "C" int32_t ss_batch_ring_threads(const ss_batch *bt, int32_t i, int32_t *fwd, int32_t *inv) {
+    if (!bt || i < 0 || i >= (int)bt->grids.size()) { set_error("bad batch index"); return SS_BAD_ARG; }
+    if (fwd) *fwd = bt->grids[i]->ring_threads_fwd;
+    if (inv) *inv = bt->grids[i]->ring_threads_inv;
+    return SS_OK;
+}
+
+// ====================================================================== chain
+struct IfaceDev {
+    int primary, secondary, pside, sside;
+    int node[3];
+    double C[9];
+};
+
+struct ss_chain {
+    std::vector<ss_grid *> g;
+    std::vector<IfaceDev> ifs;
+    std::vector<int> layer_of;
+    int nlayers = 0;
+    std::vector<double *> state;  // per patch: [v][3][b] spline-object ahat (device)
+    double *coupled = nullptr;
+    size_t coupled_len = 0;
+    int device = 0;
+    std::vector<cudaEvent_t> ev;  // ordering between the patches' streams and the chain's stream
+};
+
+static double grid_DX(const ss_grid *g) { return (g->p.iMax - g->p.iMin) / g->p.num_cells; }
+
+extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **out) {
+    if (!out || !grids || n < 2) { set_error("PatchChain requires at least 2 grids, got %d", n); return SS_BAD_ARG; }
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        if (!grids[i] || grids[i]->rlz || grids[i]->d.nvars != grids[0]->d.nvars) {
+            set_error("the chain supports RL patches with equal variable counts");
+            return SS_BAD_ARG;
+        }
+    }
+    ss_chain *c = new ss_chain();
+    c->device = grids[0]->device;
+    cudaSetDevice(c->device);
+    for (int i = 0; i < n; i++) c->g.push_back(grids[i]);
+    const int nv = (int)grids[0]->d.nvars;
+    for (int k = 0; k < n - 1; k++) {
+        IfaceDev f{};
+        // PatchChain (src/multipatch.jl:825-848): the coarser side is primary
+        if (grid_DX(grids[k]) >= grid_DX(grids[k + 1])) { f.primary = k; f.secondary = k + 1; f.pside = 1; f.sside = 0; }
+        else { f.primary = k + 1; f.secondary = k; f.pside = 0; f.sside = 1; }
+        const ss_grid *P = grids[f.primary], *S = grids[f.secondary];
+        const double pDX = grid_DX(P), sDX = grid_DX(S), ratio = pDX / sDX;
+        const double tol = 1e-12 * std::max(pDX, sDX);
+        static const double M1[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        static const double M2[9] = {0.5, 0.5, 0.0, 0.125, 0.75, 0.125, 0.0, 0.5, 0.5};
+        if (std::fabs(ratio - 1.0) < tol) std::memcpy(f.C, M1, sizeof M1);
+        else if (std::fabs(ratio - 2.0) < tol) std::memcpy(f.C, M2, sizeof M2);
+        else { delete c; set_error("Only 1:1 and 2:1 coarse-to-fine ratios are supported, got %g:1", ratio); return SS_BAD_ARG; }
+        for (int v = 0; v < nv; v++) {
+            if (!S->spl_host[v].r3x || P->spl_host[v].r3x) {
+                delete c;
+                set_error("chain interface %d: the secondary needs R3X (FixedBC) and the primary must not be R3X", k);
+                return SS_UNSUPPORTED_BC;
+            }
+        }
+        const int b = (int)P->d.b_iDim;
+        if (f.pside == 1) { f.node[0] = b - 3; f.node[1] = b - 2; f.node[2] = b - 1; }
+        else { f.node[0] = 0; f.node[1] = 1; f.node[2] = 2; }
+        c->ifs.push_back(f);
+    }
+    c->layer_of.assign(n, 0);
+    for (int it = 0; it < n + 2; it++) {
+        bool changed = false;
+        for (auto &f : c->ifs) {
+            int need = c->layer_of[f.primary] + 1;
+            if (c->layer_of[f.secondary] < need) { c->layer_of[f.secondary] = need; changed = true; }
+        }
+        if (!changed) break;
+    }
+    for (int v : c->layer_of) c->nlayers = std::max(c->nlayers, v + 1);
+    size_t maxq = 0;
+    for (auto &f : c->ifs) {
+        const ss_grid *P = grids[f.primary], *S = grids[f.secondary];
+        size_t nq = 1 + 2 * (size_t)std::min(P->d.kDim_wn, S->d.kDim_wn);
+        maxq = std::max(maxq, nq);
+    }
+    c->state.assign(n, nullptr);
+    for (int i = 0; i < n; i++) {
+        size_t bytes = (size_t)nv * 3 * grids[i]->d.b_iDim * sizeof(double);
+        if (cudaMalloc(&c->state[i], bytes) != cudaSuccess) { cudaGetLastError(); set_error("out of device memory"); return SS_OUT_OF_MEMORY; }
+        cudaMemset(c->state[i], 0, bytes);
+    }
+    c->coupled_len = (size_t)nv * maxq * 3;
+    if (cudaMalloc(&c->coupled, c->coupled_len * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("out of device memory");
+        return SS_OUT_OF_MEMORY;
+    }
+    // secondaries keep their per-wavenumber registry resident
+    for (auto &f : c->ifs) {
+        ss_grid *S = grids[f.secondary];
+        if (!S->d_ahat) {
+            size_t bytes = (size_t)S->d.nvars * S->d.n_blocks * S->d.b_iDim * sizeof(double);
+            if (cudaMalloc((void **)&S->d_ahat, bytes) != cudaSuccess) { cudaGetLastError(); set_error("out of device memory"); return SS_OUT_OF_MEMORY; }
+            cudaMemset(S->d_ahat, 0, bytes);
+            S->allocs.push_back(S->d_ahat);
+        }
+    }
+    for (int i = 0; i < n + 1; i++) {
+        cudaEvent_t e;
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        c->ev.push_back(e);
+    }
+    cudaDeviceSynchronize();
+    *out = c;
+    return SS_OK;
+}
+
+extern "C" int32_t ss_chain_destroy(ss_chain *c) {
+    if (!c) return SS_OK;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    for (double *p : c->state) cudaFree(p);
+    for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+    cudaFree(c->coupled);
+    delete c;
+    return SS_OK;
+}
+
+// update_interface! for an RL secondary (_rl_kernel!, src/multipatch.jl:417-478)
+static int32_t update_interface(ss_chain *c, const IfaceDev &f, cudaStream_t st) {
+    ss_grid *P = c->g[f.primary], *S = c->g[f.secondary];
+    ChainLaunch L{};
+    L.spec = P->spec;
+    L.spl = P->d_spl;
+    L.coupled = c->coupled;
+    L.state = c->state[f.secondary];
+    L.reg = S->d_ahat;
+    L.nspec_p = P->d.n_spectral;
+    L.nblocks_s = S->d.n_blocks;
+    L.b_p = (int)P->d.b_iDim;
+    L.b_s = (int)S->d.b_iDim;
+    L.ld = (L.b_p % 2) ? L.b_p : L.b_p + 1;
+    L.nq = 1 + 2 * (int)std::min(P->d.kDim_wn, S->d.kDim_wn);
+    L.nvars = (int)P->d.nvars;
+    L.side = f.sside;
+    for (int i = 0; i < 3; i++) L.node[i] = f.node[i];
+    std::memcpy(L.C, f.C, sizeof L.C);
+    int nmax = 0;
+    for (auto &sh : P->spl_host) nmax = std::max(nmax, sh.Min);
+    size_t smem = (size_t(32) * L.ld + size_t(5) * nmax) * sizeof(double);
+    if (P->esz == 8) CUDA_TRY(launch_chain_couple<double>(L, smem, st));
+    else CUDA_TRY(launch_chain_couple<float>(L, smem, st));
+    CUDA_TRY(launch_chain_assemble(L, st));
+    return SS_OK;
+}
+
+extern "C" int32_t ss_multi_grid_transform(ss_chain *c, void *stream) {
+    if (!c) { set_error("null chain"); return SS_BAD_ARG; }
+    cudaSetDevice(c->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->g[0]->stream;
+    // earlier work on every patch's own stream comes first
+    for (size_t i = 0; i < c->g.size(); i++) {
+        CUDA_TRY(cudaEventRecord(c->ev[i], c->g[i]->stream));
+        CUDA_TRY(cudaStreamWaitEvent(st, c->ev[i], 0));
+    }
+    // patches run on `st` in topological order (multiGridTransform!, src/multipatch.jl:769-786)
+    for (int L = 0; L < c->nlayers; L++) {
+        for (size_t i = 0; i < c->g.size(); i++)
+            if (c->layer_of[i] == L) {
+                int32_t r = grid_inverse(c->g[i], st);
+                if (r) return r;
+            }
+        for (auto &f : c->ifs)
+            if (c->layer_of[f.primary] == L) {
+                int32_t r = update_interface(c, f, st);
+                if (r) return r;
+            }
+    }
+    // and later work on each patch's own stream (downloads) comes after
+    CUDA_TRY(cudaEventRecord(c->ev[c->g.size()], st));
+    for (size_t i = 0; i < c->g.size(); i++) CUDA_TRY(cudaStreamWaitEvent(c->g[i]->stream, c->ev[c->g.size()], 0));
+    return SS_OK;
+}
+
+// ====================================================================== tiles
+// sumSpectralTile! (set = 0) / setSpectralTile!'s write (set = 1)
+extern "C" int32_t ss_tile_sum_spectral(ss_grid *patch, const ss_grid *tile, int32_t set, void *stream) {
+    if (!patch || !tile) { set_error("null grid"); return SS_BAD_ARG; }
+    if (patch->rlz != tile->rlz || patch->esz != tile->esz || patch->d.nvars != tile->d.nvars ||
+        patch->d.b_kDim != tile->d.b_kDim || patch->p.mubar != tile->p.mubar) {
+        set_error("tile and patch disagree in geometry, precision, variables or Chebyshev modes");
+        return SS_BAD_SHAPE;
+    }
+    const int offset = (tile->pOL - patch->pOL) / patch->p.mubar;  // spectralIndexL - 1
+    if (offset < 0 || offset + tile->d.b_iDim > patch->d.b_iDim || tile->d.kDim_wn > patch->d.kDim_wn) {
+        set_error("tile does not lie inside the patch");
+        return SS_BAD_SHAPE;
+    }
+    cudaSetDevice(patch->device);
+    TileLaunch T{};
+    T.patch = patch->spec;
+    T.tile = tile->spec;
+    T.nspec_p = patch->d.n_spectral;
+    T.nspec_t = tile->d.n_spectral;
+    T.b_p = (int)patch->d.b_iDim;
+    T.b_t = (int)tile->d.b_iDim;
+    T.blocks_p = 1 + 2 * (int)patch->d.kDim_wn;
+    T.blocks_t = 1 + 2 * (int)tile->d.kDim_wn;
+    T.bk = (int)patch->d.b_kDim;
+    T.nvars = (int)patch->d.nvars;
+    T.offset = offset;
+    T.set = set ? 1 : 0;
+    cudaStream_t st = stream ? (cudaStream_t)stream : patch->stream;
+    if (patch->esz == 8) CUDA_TRY(launch_tile_sum<double>(T, st));
+    else CUDA_TRY(launch_tile_sum<float>(T, st));
+    return SS_OK;
+}
+
+// Copy the tile's rings of one physical slot between patch and tile
+// (direction 0: patch → tile, 1: tile → patch); slot 0 = every slot.
+extern "C" int32_t ss_tile_copy_physical(ss_grid *patch, ss_grid *tile, int32_t slot, int32_t direction,
+                                         void *stream) {
+    if (!patch || !tile) { set_error("null grid"); return SS_BAD_ARG; }
+    if (patch->rlz != tile->rlz || patch->esz != tile->esz || patch->d.nvars != tile->d.nvars ||
+        patch->d.kDim != tile->d.kDim || slot < 0 || slot > patch->d.nslots) {
+        set_error("tile and patch disagree in geometry, precision, variables or levels");
+        return SS_BAD_SHAPE;
+    }
+    // rings of the tile start after the patch rings below the tile's offset
+    int64_t row0 = 0;
+    for (int ri = patch->pOL + 1; ri <= tile->pOL; ri++) row0 += 4 + 4 * ri;
+    row0 *= patch->d.kDim;
+    if (row0 + tile->d.n_physical > patch->d.n_physical) { set_error("tile does not lie inside the patch"); return SS_BAD_SHAPE; }
+    cudaSetDevice(patch->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : patch->stream;
+    const size_t es = patch->esz;
+    const int s0 = slot ? slot - 1 : 0, s1 = slot ? slot : (int)patch->d.nslots;
+    for (int s = s0; s < s1; s++)
+        for (int v = 0; v < patch->d.nvars; v++) {
+            char *pp = (char *)patch->phys + ((size_t)s * patch->d.nvars + v) * patch->d.n_physical * es + row0 * es;
+            char *tp = (char *)tile->phys + ((size_t)s * tile->d.nvars + v) * tile->d.n_physical * es;
+            if (direction == 0) CUDA_TRY(cudaMemcpyAsync(tp, pp, tile->d.n_physical * es, cudaMemcpyDeviceToDevice, st));
+            else CUDA_TRY(cudaMemcpyAsync(pp, tp, tile->d.n_physical * es, cudaMemcpyDeviceToDevice, st));
+        }
+    return SS_OK;
+}
+
+extern "C" int32_t ss_grid_zero_spectral(ss_grid *g, void *stream) {
+    if (!g) { set_error("null grid"); return SS_BAD_ARG; }
+    cudaSetDevice(g->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+    CUDA_TRY(cudaMemsetAsync(g->spec, 0, (size_t)g->d.n_spectral * g->d.nvars * g->esz, st));
+    return SS_OK;
+}

@@ -4,44 +4,18 @@
 // L = 4+4ri points (src/Fourier.jl:192-193, 388-395, 463-468).  Ring lengths
 // have arbitrary prime factors, so a length-N complex DFT (N = L/2 after real
 // packing) is evaluated either by mixed-radix Stockham autosort passes
-// (radices 4,2,3,5,7,11,13; every pass reads and writes shared memory with
-// unit-stride butterfly groups) or, when N has a prime factor > 13, by
-// Bluestein's chirp-z convolution of smooth length M >= 2N-1 whose two FFTs
-// are again Stockham passes.  Twiddles come from FP64-accurate tables built
-// on the host (ss_setup.cpp) and read through the read-only cache.
+// (radices 4,2,3,5,7,11,13 in registers) or, when N has a prime factor > 13,
+// by Bluestein's chirp-z convolution of smooth length M >= 2N-1 whose two FFTs
+// are again Stockham passes.  Twiddles come from FP64-accurate tables built on
+// the host (ss_setup.cpp), stored in the compute type's layout.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include "ss_internal.h"
+#include "ss_types.cuh"
 
 namespace ss {
-
-template <typename T>
-struct cpx {
-    T x, y;
-};
-
-template <typename T>
-__device__ __forceinline__ cpx<T> c_add(cpx<T> a, cpx<T> b) { return {a.x + b.x, a.y + b.y}; }
-template <typename T>
-__device__ __forceinline__ cpx<T> c_sub(cpx<T> a, cpx<T> b) { return {a.x - b.x, a.y - b.y}; }
-template <typename T>
-__device__ __forceinline__ cpx<T> c_mul(cpx<T> a, cpx<T> b) {
-    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
-}
-template <typename T>
-__device__ __forceinline__ cpx<T> c_conj(cpx<T> a) { return {a.x, -a.y}; }
-
-// cos/sin(2π j/R) tables of the odd-prime butterflies, filled by ss_fft_init_constants()
-__constant__ double c_rcos[14][14];
-__constant__ double c_rsin[14][14];
-
-template <typename T>
-__device__ __forceinline__ cpx<T> load_tw(const double2 *__restrict__ pool, int64_t i) {
-    double2 w = __ldg(pool + i);
-    return {(T)w.x, (T)w.y};
-}
 
 // In-register DFT of size R; SIGN = -1 forward (exp(-2πi ...)), +1 inverse.
 template <int R, int SIGN, typename T>
@@ -74,15 +48,15 @@ __device__ __forceinline__ void dft_small(cpx<T> *v) {
         for (int q = 0; q < H; q++) s0 = c_add(s0, a[q]);
 #pragma unroll
         for (int s = 1; s <= H; s++) {
-            cpx<T> re = x0, im = {T(0), T(0)};
+            cpx<T> re = x0, im = c_zero<T>();
 #pragma unroll
             for (int q = 1; q <= H; q++) {
                 const int e = (q * s) % R;
-                const T cs = (T)c_rcos[R][e], sn = (T)c_rsin[R][e];
-                re.x += a[q - 1].x * cs;
-                re.y += a[q - 1].y * cs;
-                im.x += b[q - 1].x * sn;
-                im.y += b[q - 1].y * sn;
+                const T cs = rcos<T>(R, e), sn = rsin<T>(R, e);
+                re.x = re.x + a[q - 1].x * cs;
+                re.y = re.y + a[q - 1].y * cs;
+                im.x = im.x + b[q - 1].x * sn;
+                im.y = im.y + b[q - 1].y * sn;
             }
             // forward: X_s = re - i*im, X_{R-s} = re + i*im  (inverse: signs swap)
             cpx<T> iim = {-im.y, im.x};
@@ -101,7 +75,7 @@ __device__ __forceinline__ void dft_small(cpx<T> *v) {
 // One Stockham pass: Ns = product of the radices already applied.
 template <int R, int SIGN, typename T>
 __device__ __forceinline__ void stockham_pass(const cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N,
-                                              int Ns, const double2 *__restrict__ tw) {
+                                              int Ns, const void *__restrict__ tw) {
     const int NR = N / R;
     const int tstride = N / (Ns * R);
     for (int j = threadIdx.x; j < NR; j += blockDim.x) {
@@ -113,7 +87,7 @@ __device__ __forceinline__ void stockham_pass(const cpx<T> *__restrict__ src, cp
             const int step = tstride * k;
 #pragma unroll
             for (int r = 1; r < R; r++) {
-                cpx<T> w = load_tw<T>(tw, (int64_t)r * step);
+                cpx<T> w = ld_cplx<T>(tw, (int64_t)r * step);
                 if (SIGN > 0) w.y = -w.y;
                 v[r] = c_mul(v[r], w);
             }
@@ -125,9 +99,14 @@ __device__ __forceinline__ void stockham_pass(const cpx<T> *__restrict__ src, cp
     }
 }
 
+template <typename T>
+__device__ __forceinline__ const void *tab_at(const void *pool, int64_t off) {
+    return (const void *)((const typename Tab<T>::cplx_t *)pool + off);
+}
+
 // Stockham DFT over ping-pong buffers; returns the buffer holding the result.
 template <int SIGN, typename T>
-__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const double2 *tw) {
+__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw) {
     int Ns = 1;
     for (int s = 0; s < nrad; s++) {
         const int R = rad[s];
@@ -153,30 +132,30 @@ __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nra
 // Length-N DFT of the N values in `a` (sign SIGN).  Both buffers hold
 // fft_buffer_len(plan) entries.  Returns the buffer with the N results.
 template <int SIGN, typename T>
-__device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const double2 *pool) {
-    if (!p.blu) return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, pool + p.tw);
+__device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool) {
+    if (!p.blu) return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw));
     const int N = p.N, M = p.M;
-    const double2 *chirp = pool + p.chirp;
-    const double2 *filt = pool + p.filt;
+    const void *chirp = tab_at<T>(pool, p.chirp);
+    const void *filt = tab_at<T>(pool, p.filt);
     // X_k = c_k Σ_j (x_j c_j) conj(c_{k-j}) with c_k = exp(-πi k²/N); the
     // inverse DFT is conj(forward(conj x)).
     for (int k = threadIdx.x; k < M; k += blockDim.x) {
-        cpx<T> v = {T(0), T(0)};
+        cpx<T> v = c_zero<T>();
         if (k < N) {
             v = a[k];
             if (SIGN > 0) v.y = -v.y;
-            v = c_mul(v, load_tw<T>(chirp, k));
+            v = c_mul(v, ld_cplx<T>(chirp, k));
         }
         a[k] = v;
     }
     __syncthreads();
-    cpx<T> *r = stockham<-1, T>(a, b, M, p.mrad, p.mnrad, pool + p.mtw);
-    for (int k = threadIdx.x; k < M; k += blockDim.x) r[k] = c_mul(r[k], load_tw<T>(filt, k));
+    cpx<T> *r = stockham<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw));
+    for (int k = threadIdx.x; k < M; k += blockDim.x) r[k] = c_mul(r[k], ld_cplx<T>(filt, k));
     __syncthreads();
     cpx<T> *other = (r == a) ? b : a;
-    cpx<T> *q = stockham<1, T>(r, other, M, p.mrad, p.mnrad, pool + p.mtw);
+    cpx<T> *q = stockham<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw));
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
-        cpx<T> v = c_mul(q[k], load_tw<T>(chirp, k));
+        cpx<T> v = c_mul(q[k], ld_cplx<T>(chirp, k));
         if (SIGN > 0) v.y = -v.y;
         q[k] = v;
     }

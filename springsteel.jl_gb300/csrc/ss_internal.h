@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <vector_types.h>
+
 #include "springsteel_gpu.h"
 
 #ifdef __CUDACC__
@@ -57,27 +59,34 @@ struct RingDesc {
     int64_t fofs;      // Σ_{r'<r} (1+2ri') (packed coefficient row start)
 };
 
+// Compute-type layouts of the device tables (ss_types.cuh): TL_F64 double,
+// TL_DF64 (hi, lo) binary32 pairs, TL_F32 float.
+enum { TL_F64 = 0, TL_DF64 = 1, TL_F32 = 2 };
+
 // Per-variable spline template on the device (FP64 factor, B-spline weights).
 struct SplineDev {
     int bDim, Min, rankL, rankR, lk, rk, r3x, _pad;
     double aL, bL, aR, bR;
-    double *L4;      // Min*4: L[j+d][j] at j*4+d   (FP64 banded Cholesky factor)
-    double *dinv;    // Min: 1/L[j][j]
-    double *PQb;     // bDim*7 full P+Q band (R3X only)
-    double *sbw;     // bDim*(4 mubar) SB weights (row mi, tap)
-    double *siw;     // 3*mishDim*4 SI weights (derivative, point, tap)
-    int *si_m0;      // mishDim: first coefficient index of the 4-tap window
+    double *L4;         // Min*4: L[j+d][j] at j*4+d   (FP64 banded Cholesky factor)
+    double *dinv;       // Min: 1/L[j][j]
+    double *PQb;        // bDim*7 full P+Q band (R3X only)
+    float *L4f;         // FP32-rounded factor (FP32 mode)
+    float *dinvf;
+    float2 *Aband_x;    // FP64 open-form Γ(P+Q)Γᵀ band as (hi, lo) pairs (FP32 refinement)
+    const void *sbw_t;  // bDim*(4 mubar) SB weights (row mi, tap), compute layout
+    const void *siw_t;  // 3*mishDim*4 SI weights (derivative, point, tap), compute layout
+    int *si_m0;         // mishDim: first coefficient index of the 4-tap window
 };
 
-// Per-variable Chebyshev column tables (src/Chebyshev.jl).
+// Per-variable Chebyshev column tables (src/Chebyshev.jl), compute layout.
 struct ChebDev {
     int N, bk, nrank, half;
-    double dscale;   // -0.5*(zmax - zmin)
-    double *fwd;     // bk × ceil(N/2): folded forward DCT-I rows (scale, filter folded)
-    double *inv_e;   // half_out × ne: inverse DCT-I, even-k columns
-    double *inv_o;   // half_out × no: inverse DCT-I, odd-k columns
-    double *gu;      // nrank × bk   (Γ = Σ u vᵀ restricted to the first bk rows)
-    double *gv;      // nrank × N
+    double dscale;        // -0.5*(zmax - zmin)
+    const void *fwd_t;    // bk × ceil(N/2): folded forward DCT-I rows (scale, filter folded)
+    const void *inv_e_t;  // half_out × ne: inverse DCT-I, even-k columns
+    const void *inv_o_t;  // half_out × no: inverse DCT-I, odd-k columns
+    const void *gu_t;     // nrank × bk   (Γ = Σ u vᵀ restricted to the first bk rows)
+    const void *gv_t;     // nrank × N
 };
 
 enum { BC_R0 = 0, BC_A1 = 1, BC_A2 = 2, BC_PER = 3, BC_R3 = 4 };
@@ -89,7 +98,7 @@ struct SplineHost {
     std::vector<double> qp, qw, mish;
     int Mdim, Min, rankL, rankR, lk, rk, r3x;
     double aL, bL, aR, bR;
-    std::vector<double> PQb, L4, sbw, siw;
+    std::vector<double> PQb, L4, Aopen, sbw, siw;  // Aopen: open-form band before factoring
     std::vector<int> si_m0;
 };
 int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, double l_q,

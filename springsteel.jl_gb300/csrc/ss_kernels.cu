@@ -6,15 +6,21 @@
 //     ring_forward   ring R2HC + 1/L + phase rotation → F rows       (FBtransform!)
 //     sb_project     12-tap B-spline projection per slot → spectral  (SBtransform!)
 //   gridTransform!     (src/transforms_cylindrical.jl:259-428, 659-853)
-//     sa_si          Γ fold + banded LLᵀ solve (FP64 factor) + Γᵀ (+ahat),
-//                    then f, ∂r, ∂rr at the mish points → G rows    (SAtransform!, SI*)
+//     sa_si          Γ fold + banded LLᵀ solve + Γᵀ (+ahat), then f, ∂r, ∂rr at the
+//                    mish points → G rows                             (SAtransform!, SI*)
 //     ring_inverse   phase rotation back + HC2R for f, ∂λ, ∂λλ, ∂r, ∂rr
 //     cheb_inverse   CA (Γ fold) + DCT-I for each ring output; f column also ∂z, ∂zz
+//
+// Every kernel is a template over the storage type P of physical/spectral
+// (double | float) and the compute type T (double | df64 | float); the
+// intermediate buffers C, F, G, H hold T values.
 //
 // Packed coefficient rows: ring r (ri = r + patchOffsetL) owns 1+2ri entries
 // [DC, re1, im1, re2, im2, …] — the order of the reference's spectral slots.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 
 #include "ss_fft.cuh"
@@ -24,24 +30,38 @@ namespace ss {
 
 // ------------------------------------------------------------ constants
 void fft_init_constants() {
-    static bool done = false;
-    if (done) return;
+    static bool done[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && done[dev]) return;
     double c[14][14] = {}, s[14][14] = {};
+    float cf[14][14] = {}, sf[14][14] = {};
+    float2 cx[14][14] = {}, sx[14][14] = {};
     for (int R = 2; R < 14; R++)
         for (int j = 0; j < R; j++) {
-            double a = -2.0 * 3.14159265358979323846 * j / R;  // exp(-2πi j/R) = cos a + i sin a
-            c[R][j] = cos(a);
-            s[R][j] = -sin(a);  // sin(2π j/R)
+            // cos(2π j/R), sin(2π j/R), reduced to the first half turn
+            int jj = (2 * j > R) ? R - j : j;
+            double a = 2.0 * 3.14159265358979323846 * jj / R;
+            c[R][j] = std::cos(a);
+            s[R][j] = (2 * j > R) ? -std::sin(a) : std::sin(a);
+            cf[R][j] = (float)c[R][j];
+            sf[R][j] = (float)s[R][j];
+            cx[R][j] = make_float2((float)c[R][j], (float)(c[R][j] - (double)(float)c[R][j]));
+            sx[R][j] = make_float2((float)s[R][j], (float)(s[R][j] - (double)(float)s[R][j]));
         }
-    cudaMemcpyToSymbol(c_rcos, c, sizeof c);
-    cudaMemcpyToSymbol(c_rsin, s, sizeof s);
-    done = true;
+    cudaMemcpyToSymbol(c_rcos_d, c, sizeof c);
+    cudaMemcpyToSymbol(c_rsin_d, s, sizeof s);
+    cudaMemcpyToSymbol(c_rcos_f, cf, sizeof cf);
+    cudaMemcpyToSymbol(c_rsin_f, sf, sizeof sf);
+    cudaMemcpyToSymbol(c_rcos_x, cx, sizeof cx);
+    cudaMemcpyToSymbol(c_rsin_x, sx, sizeof sx);
+    if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
 // ====================================================================
 // ring_forward: one CTA per (ring, item); item = v*bk + zb
 // ====================================================================
-template <typename T>
+template <typename P, typename T>
 __global__ void __launch_bounds__(256) ring_forward_kernel(RingLaunch L) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ring = L.ring_list[blockIdx.x];
@@ -54,20 +74,20 @@ __global__ void __launch_bounds__(256) ring_forward_kernel(RingLaunch L) {
     cpx<T> *B = A + buf;
     const int Lr = rd.L, N = Lr / 2;
 
-    const T *in;
     if (L.rlz) {
         const int v = item / L.bk, zb = item % L.bk;
-        in = (const T *)L.in + (size_t)v * L.bk * L.jDim + (size_t)L.bk * rd.jofs + (size_t)zb * Lr;
+        const T *in = (const T *)L.in + (size_t)v * L.bk * L.jDim + (size_t)L.bk * rd.jofs + (size_t)zb * Lr;
+        for (int n = threadIdx.x; n < N; n += blockDim.x) A[n] = {in[2 * n], in[2 * n + 1]};
     } else {
-        in = (const T *)L.in + (size_t)item * L.in_item_stride + rd.jofs;
+        const P *in = (const P *)L.in + (size_t)item * L.in_item_stride + rd.jofs;
+        for (int n = threadIdx.x; n < N; n += blockDim.x)
+            A[n] = {to_compute<T>(in[2 * n]), to_compute<T>(in[2 * n + 1])};
     }
-    for (int n = threadIdx.x; n < N; n += blockDim.x) A[n] = {in[2 * n], in[2 * n + 1]};
     __syncthreads();
     cpx<T> *Z = dft<-1, T>(A, B, pl, L.pool);
 
     T *out = (T *)L.out + (size_t)item * L.frows + rd.fofs;
-    const double2 *ph = L.phase + rd.phase;
-    const T invL = T(1.0) / T(Lr);
+    const T invL = T(1.0f) / T((float)Lr);
     for (int k = threadIdx.x; k <= rd.ri; k += blockDim.x) {
         cpx<T> zk = Z[k];
         cpx<T> zn = c_conj(Z[(N - k) % N]);
@@ -75,17 +95,16 @@ __global__ void __launch_bounds__(256) ring_forward_kernel(RingLaunch L) {
             out[0] = (zk.x + zk.y) * invL;
             continue;
         }
-        T bre = T(0), bim = T(0);
+        T bre = T(0.0f), bim = T(0.0f);
         if (k <= rd.kmax) {
-            cpx<T> e = {T(0.5) * (zk.x + zn.x), T(0.5) * (zk.y + zn.y)};
-            cpx<T> d = {T(0.5) * (zk.x - zn.x), T(0.5) * (zk.y - zn.y)};
+            cpx<T> e = {scale_f(zk.x + zn.x, 0.5f), scale_f(zk.y + zn.y, 0.5f)};
+            cpx<T> d = {scale_f(zk.x - zn.x, 0.5f), scale_f(zk.y - zn.y, 0.5f)};
             cpx<T> o = {d.y, -d.x};  // d / i
-            cpx<T> X = c_add(e, c_mul(load_tw<T>(L.pool + rd.utw, k), o));
+            cpx<T> X = c_add(e, c_mul(ld_cplx<T>(L.pool, rd.utw + k), o));
             T re = X.x * invL, im = X.y * invL;
-            double2 cs = __ldg(ph + (k - 1));
-            T c = (T)cs.x, s = (T)cs.y;
-            bre = c * re + s * im;
-            bim = -s * re + c * im;
+            cpx<T> cs = ld_cplx<T>(L.phase, rd.phase + (k - 1));
+            bre = cs.x * re + cs.y * im;
+            bim = -(cs.y * re) + cs.x * im;
         }
         out[2 * k - 1] = bre;
         out[2 * k] = bim;
@@ -97,7 +116,7 @@ __global__ void __launch_bounds__(256) ring_forward_kernel(RingLaunch L) {
 // read the ring's coefficient row, undo the phase rotation (FAtransform!),
 // and run HC2R for the variants: d=0 → f, ∂λ, ∂λλ; d=1 → ∂r; d=2 → ∂rr.
 // ====================================================================
-template <typename T>
+template <typename P, typename T>
 __global__ void __launch_bounds__(256) ring_inverse_kernel(RingLaunch L) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ring = L.ring_list[blockIdx.x];
@@ -111,62 +130,65 @@ __global__ void __launch_bounds__(256) ring_inverse_kernel(RingLaunch L) {
     cpx<T> *B = A + buf;
     cpx<T> *Xs = B + buf;  // rotated spectrum X_k, k = 0..kmax
     const int Lr = rd.L, N = Lr / 2, kmax = rd.kmax;
-    const double2 *ph = L.phase + rd.phase;
 
     for (int d = 0; d < 3; d++) {
         const T *g = (const T *)L.in + ((size_t)d * L.nitems + item) * L.frows + rd.fofs;
         // FAtransform!: a_re = c br - s bi, a_im = s br + c bi (phase_filter.jl:154-190)
         for (int k = threadIdx.x; k <= kmax; k += blockDim.x) {
             if (k == 0) {
-                Xs[0] = {g[0], T(0)};
+                Xs[0] = {g[0], T(0.0f)};
             } else {
                 T br = g[2 * k - 1], bi = g[2 * k];
-                double2 cs = __ldg(ph + (k - 1));
-                T c = (T)cs.x, s = (T)cs.y;
-                Xs[k] = {c * br - s * bi, s * br + c * bi};
+                cpx<T> cs = ld_cplx<T>(L.phase, rd.phase + (k - 1));
+                Xs[k] = {cs.x * br - cs.y * bi, cs.y * br + cs.x * bi};
             }
         }
         __syncthreads();
         const int nvar = (d == 0) ? 3 : 1;
         for (int dl = 0; dl < nvar; dl++) {
-            // packed spectrum Zp_k = E_k + i O_k, k < N (HC2R of length L via length-N inverse DFT)
+            // packed spectrum Zp_k = E_k + i O_k, k < N (HC2R of length L via a length-N inverse DFT)
             for (int k = threadIdx.x; k < N; k += blockDim.x) {
-                cpx<T> xa = {T(0), T(0)}, xb = {T(0), T(0)};
+                cpx<T> xa = c_zero<T>(), xb = c_zero<T>();
                 if (k <= kmax) xa = Xs[k];
                 if (N - k <= kmax && k > 0) xb = c_conj(Xs[N - k]);
                 if (dl > 0) {
-                    // FIxcoefficients: X_k → i k X_k (twice for ∂λλ)
-                    T ka = T(k), kb = T(k) - T(N);  // signed wavenumber of index k+N is k+N-L = k-N
+                    // FIxcoefficients: X_k → i κ X_k (twice for ∂λλ); κ = k for index k,
+                    // κ = k - N for index k + N (its signed wavenumber k + N - L)
+                    const float ka = (float)k, kb = (float)(k - N);
                     if (dl == 1) {
-                        xa = {-ka * xa.y, ka * xa.x};
-                        xb = {-kb * xb.y, kb * xb.x};
+                        xa = {scale_f(xa.y, -ka), scale_f(xa.x, ka)};
+                        xb = {scale_f(xb.y, -kb), scale_f(xb.x, kb)};
                     } else {
-                        xa = {-ka * ka * xa.x, -ka * ka * xa.y};
-                        xb = {-kb * kb * xb.x, -kb * kb * xb.y};
+                        xa = {scale_f(scale_f(xa.x, -ka), ka), scale_f(scale_f(xa.y, -ka), ka)};
+                        xb = {scale_f(scale_f(xb.x, -kb), kb), scale_f(scale_f(xb.y, -kb), kb)};
                     }
                 }
                 cpx<T> e = c_add(xa, xb);
-                cpx<T> o = c_mul(c_sub(xa, xb), c_conj(load_tw<T>(L.pool + rd.utw, k)));
+                cpx<T> o = c_mul(c_sub(xa, xb), c_conj(ld_cplx<T>(L.pool, rd.utw + k)));
                 A[k] = {e.x - o.y, e.y + o.x};
             }
             __syncthreads();
             cpx<T> *z = dft<1, T>(A, B, pl, L.pool);
-            T *dst;
-            int slot;  // 1-based physical slot (RL) / ring variant (RLZ)
+            int slot;  // 1-based physical slot
             if (d == 0) slot = (dl == 0) ? 1 : (dl == 1 ? 4 : 5);
             else slot = (d == 1) ? 2 : 3;
             if (L.rlz) {
                 // H[variant][v][r][zb][l], variant: 0 f, 1 ∂λ, 2 ∂λλ, 3 ∂r, 4 ∂rr
-                int var = (d == 0) ? dl : (d == 1 ? 3 : 4);
-                dst = (T *)L.out + ((size_t)var * L.nvars + v) * L.bk * L.jDim + (size_t)L.bk * rd.jofs +
-                      (size_t)zb * Lr;
+                const int var = (d == 0) ? dl : (d == 1 ? 3 : 4);
+                T *dst = (T *)L.out + ((size_t)var * L.nvars + v) * L.bk * L.jDim + (size_t)L.bk * rd.jofs +
+                         (size_t)zb * Lr;
+                for (int n = threadIdx.x; n < N; n += blockDim.x) {
+                    cpx<T> w = z[n];
+                    dst[2 * n] = w.x;
+                    dst[2 * n + 1] = w.y;
+                }
             } else {
-                dst = (T *)L.out + ((size_t)(slot - 1) * L.nvars + v) * L.np + rd.jofs;
-            }
-            for (int n = threadIdx.x; n < N; n += blockDim.x) {
-                cpx<T> w = z[n];
-                dst[2 * n] = w.x;
-                dst[2 * n + 1] = w.y;
+                P *dst = (P *)L.out + ((size_t)(slot - 1) * L.nvars + v) * L.np + rd.jofs;
+                for (int n = threadIdx.x; n < N; n += blockDim.x) {
+                    cpx<T> w = z[n];
+                    dst[2 * n] = to_storage<P>(w.x);
+                    dst[2 * n + 1] = to_storage<P>(w.y);
+                }
             }
             __syncthreads();
         }
@@ -177,126 +199,169 @@ __global__ void __launch_bounds__(256) ring_inverse_kernel(RingLaunch L) {
 // sb_project: spectral[(zb*(1+2K) + s)*b + mi] = Σ_taps w(mi,tap) F[row][s]
 // block (32 slots, 8 rows of outputs); 64 outputs per CTA in mi
 // ====================================================================
-template <typename T>
-__global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch P) {
+template <typename P, typename T>
+__global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch S) {
     __shared__ T tile[32][65];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int s0 = blockIdx.x * 32, m0 = blockIdx.y * 64;
     const int item = blockIdx.z;
-    const int v = item / P.bk, zb = item % P.bk;
+    const int v = item / S.bk, zb = item % S.bk;
     const int s = s0 + tx;
-    const SplineDev &sp = P.spl[v];
-    const int taps = 4 * P.mubar;
-    const T *F = (const T *)P.F + (size_t)item * P.frows;
+    const SplineDev &sp = S.spl[v];
+    const int taps = 4 * S.mubar;
+    const T *F = (const T *)S.F + (size_t)item * S.frows;
     for (int q = 0; q < 8; q++) {
         const int mi = m0 + ty + 8 * q;
-        T acc = T(0);
-        if (mi < P.b && s < P.nslots_z) {
-            const double *w = sp.sbw + (size_t)mi * taps;
-            const int row0 = P.mubar * (mi - 3);
+        T acc = T(0.0f);
+        if (mi < S.b && s < S.nslots_z) {
+            const int row0 = S.mubar * (mi - 3);
             for (int t = 0; t < taps; t++) {
                 const int row = row0 + t;  // radial mish index (0-based ring r-1)
-                if (row < 0 || row >= P.iDim) continue;
-                const int ri = row + 1 + P.pOL;
-                if (s >= 1 + 2 * ri) continue;  // wavenumber k > ri: reference zero-fills
-                acc += (T)__ldg(w + t) * F[P.fofs[row] + s];
+                if (row < 0 || row >= S.iDim) continue;
+                const int ri = row + 1 + S.pOL;
+                if (s >= 1 + 2 * ri) continue;  // wavenumber k > ri: the reference zero-fills
+                acc = acc + ld_real<T>(sp.sbw_t, (int64_t)mi * taps + t) * F[S.fofs[row] + s];
             }
         }
         tile[tx][ty + 8 * q] = acc;
     }
     __syncthreads();
-    T *spec = (T *)P.spec + (size_t)v * P.nspec + (size_t)zb * P.nslots_z * P.b;
-    const double *fw = P.fw ? P.fw + (size_t)v * (P.K + 1) : nullptr;
-    const double *cw = P.cw ? P.cw + (size_t)v * P.bk : nullptr;
+    P *spec = (P *)S.spec + (size_t)v * S.nspec + (size_t)zb * S.nslots_z * S.b;
+    const double *fw = S.fw ? S.fw + (size_t)v * (S.K + 1) : nullptr;
+    const double *cw = S.cw ? S.cw + (size_t)v * S.bk : nullptr;
     const int tid = ty * 32 + tx;
     for (int e = tid; e < 32 * 64; e += 256) {
         const int sl = e / 64, ml = e % 64;
         const int ss = s0 + sl, mi = m0 + ml;
-        if (ss < P.nslots_z && mi < P.b) {
+        if (ss < S.nslots_z && mi < S.b) {
             T val = tile[sl][ml];
-            if (P.filtered) {
-                double wgt = (fw ? fw[(ss + 1) / 2] : 1.0) * (cw ? cw[zb] : 1.0);
-                if (wgt != 1.0) val = (wgt == 0.0) ? T(0) : val * (T)wgt;
+            if (S.filtered) {
+                const double wgt = (fw ? fw[(ss + 1) / 2] : 1.0) * (cw ? cw[zb] : 1.0);
+                if (wgt != 1.0) val = (wgt == 0.0) ? T(0.0f) : val * to_compute<T>(wgt);
             }
-            spec[(size_t)ss * P.b + mi] = val;
+            spec[(size_t)ss * S.b + mi] = to_storage<P>(val);
         }
     }
 }
 
 // ====================================================================
-// sa_si: per 32-slot tile: Γ b → L⁻ᵀL⁻¹ → Γᵀ (+ahat) in FP64 (SAtransform!,
-// src/CubicBSpline.jl:1368-1396) then 4-tap SI/SIx/SIxx at the mish points.
+// sa_si: per 32-slot tile, SAtransform! (src/CubicBSpline.jl:1368-1396)
+//   FP64 modes: Γ b → L⁻ᵀL⁻¹ → Γᵀ (+ahat) in binary64;
+//   FP32 mode:  binary32 solve with the FP32-rounded factor, one residual
+//               r = Γb − A x in df64 against the FP64 open-form matrix, a
+//               correction solve, x += dx;
+// then the 4-tap SI/SIx/SIxx at the mish points in the compute type.
 // ====================================================================
-template <typename T>
-__global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch P) {
+template <typename S>
+__device__ __forceinline__ void gamma_fold(const SplineDev &sp, S *x, int Md, int n) {
+    const int rL = sp.rankL;
+    const S b0 = x[0], b1 = x[1], bM1 = x[Md - 1], bM2 = x[Md - 2];
+    for (int i = 0; i < n; i++) x[i] = x[i + rL];
+    if (sp.lk == BC_A1) { x[0] += (S)sp.aL * b0; x[1] += (S)sp.bL * b0; }
+    else if (sp.lk == BC_A2) { x[0] += (S)sp.aL * b0 + (S)sp.bL * b1; }
+    if (sp.rk == BC_A1) { x[n - 1] += (S)sp.aR * bM1; x[n - 2] += (S)sp.bR * bM1; }
+    else if (sp.rk == BC_A2) { x[n - 1] += (S)sp.aR * bM1 + (S)sp.bR * bM2; }
+}
+template <typename S>
+__device__ __forceinline__ void gamma_unfold(const SplineDev &sp, S *x, int Md, int n) {
+    const int rL = sp.rankL;
+    const S s0v = x[0], s1v = x[1], sM1 = x[n - 1], sM2 = x[n - 2];
+    for (int i = n - 1; i >= 0; i--) x[i + rL] = x[i];
+    for (int j = 0; j < rL; j++) x[j] = S(0);
+    for (int j = Md - sp.rankR; j < Md; j++) x[j] = S(0);
+    if (sp.lk == BC_A1) x[0] = (S)sp.aL * s0v + (S)sp.bL * s1v;
+    else if (sp.lk == BC_A2) { x[0] = (S)sp.aL * s0v; x[1] = (S)sp.bL * s0v; }
+    if (sp.rk == BC_A1) x[Md - 1] = (S)sp.aR * sM1 + (S)sp.bR * sM2;
+    else if (sp.rk == BC_A2) { x[Md - 2] = (S)sp.bR * sM1; x[Md - 1] = (S)sp.aR * sM1; }
+}
+// forward L y = v, backward Lᵀ x = y in place (src/banded_cholesky.jl:202-231)
+template <typename S>
+__device__ __forceinline__ void band_solve(const S *Ls, const S *Di, S *x, int n) {
+    S y1 = S(0), y2 = S(0), y3 = S(0);
+    for (int i = 0; i < n; i++) {
+        S acc = x[i];
+        if (i >= 3) acc -= Ls[(i - 3) * 4 + 3] * y3;
+        if (i >= 2) acc -= Ls[(i - 2) * 4 + 2] * y2;
+        if (i >= 1) acc -= Ls[(i - 1) * 4 + 1] * y1;
+        const S yi = acc * Di[i];
+        x[i] = yi;
+        y3 = y2; y2 = y1; y1 = yi;
+    }
+    S x1 = S(0), x2 = S(0), x3 = S(0);
+    for (int i = n - 1; i >= 0; i--) {
+        S acc = x[i];
+        if (i + 1 < n) acc -= Ls[i * 4 + 1] * x1;
+        if (i + 2 < n) acc -= Ls[i * 4 + 2] * x2;
+        if (i + 3 < n) acc -= Ls[i * 4 + 3] * x3;
+        const S xi = acc * Di[i];
+        x[i] = xi;
+        x3 = x2; x2 = x1; x1 = xi;
+    }
+}
+
+template <typename P, typename T>
+__global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr bool kF32 = std::is_same<T, float>::value;
+    using S = typename std::conditional<kF32, float, double>::type;  // solve type
     const int item = blockIdx.y;
-    const int v = item / P.bk, zb = item % P.bk;
-    const SplineDev &sp = P.spl[v];
-    const int b = P.b, ld = P.ld, n = sp.Min;
-    double *X = reinterpret_cast<double *>(smem_raw);  // 32 × ld
-    double *Ls = X + 32 * ld;                          // 4n factor
-    double *Di = Ls + 4 * n;                           // n reciprocals
+    const int v = item / A.bk, zb = item % A.bk;
+    const SplineDev &sp = A.spl[v];
+    const int b = A.b, ld = A.ld, n = sp.Min;
+    S *X = reinterpret_cast<S *>(smem_raw);  // 32 × ld
+    S *Ls = X + 32 * ld;                     // 4n factor
+    S *Di = Ls + 4 * n;                      // n reciprocals
+    S *R = Di + n;                           // 32 × ld: FP32 residuals / df64 coefficients for SI
+    constexpr bool kSameX = kF32 || std::is_same<T, double>::value;
+    T *XT = kSameX ? reinterpret_cast<T *>(X) : reinterpret_cast<T *>(R);
     const int s0 = blockIdx.x * 32;
-    const T *spec = (const T *)P.spec + (size_t)v * P.nspec + ((size_t)zb * P.nslots_z + s0) * b;
-    const int nsl = min(32, P.nslots_z - s0);
-    for (int e = threadIdx.x; e < nsl * b; e += blockDim.x) X[(e / b) * ld + (e % b)] = (double)spec[e];
-    for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) Ls[e] = sp.L4[e];
-    for (int e = threadIdx.x; e < n; e += blockDim.x) Di[e] = sp.dinv[e];
+    const P *spec = (const P *)A.spec + (size_t)v * A.nspec + ((size_t)zb * A.nslots_z + s0) * b;
+    const int nsl = min(32, A.nslots_z - s0);
+    for (int e = threadIdx.x; e < nsl * b; e += blockDim.x) X[(e / b) * ld + (e % b)] = (S)spec[e];
+    for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) Ls[e] = kF32 ? (S)sp.L4f[e] : (S)sp.L4[e];
+    for (int e = threadIdx.x; e < n; e += blockDim.x) Di[e] = kF32 ? (S)sp.dinvf[e] : (S)sp.dinv[e];
     __syncthreads();
 
     if (threadIdx.x < nsl) {
-        double *x = X + threadIdx.x * ld;
-        const int Md = b, rL = sp.rankL;
-        if (sp.r3x && P.ahat) {
-            const double *ah = P.ahat + ((size_t)v * P.nblocks + (size_t)zb * P.nslots_z + s0 + threadIdx.x) * b;
+        S *x = X + threadIdx.x * ld;
+        const int Md = b;
+        const double *ah = (sp.r3x && A.ahat)
+                               ? A.ahat + ((size_t)v * A.nblocks + (size_t)zb * A.nslots_z + s0 + threadIdx.x) * b
+                               : nullptr;
+        if (ah) {
             // b̃ = b − PQ·ahat (PQ = full P+Q, band 3); row i only changes b_i
             for (int i = 0; i < Md; i++) {
                 double acc = 0.0;
                 for (int j = max(0, i - 3); j <= min(Md - 1, i + 3); j++) acc += sp.PQb[i * 7 + (j - i + 3)] * ah[j];
-                x[i] = x[i] - acc;
+                x[i] = (S)((double)x[i] - acc);
             }
         }
-        // Γ b (src/CubicBSpline.jl:427-458)
-        const double b0 = x[0], b1 = x[1], bM1 = x[Md - 1], bM2 = x[Md - 2];
-        for (int i = 0; i < n; i++) x[i] = x[i + rL];
-        if (sp.lk == BC_A1) { x[0] += sp.aL * b0; x[1] += sp.bL * b0; }
-        else if (sp.lk == BC_A2) { x[0] += sp.aL * b0 + sp.bL * b1; }
-        if (sp.rk == BC_A1) { x[n - 1] += sp.aR * bM1; x[n - 2] += sp.bR * bM1; }
-        else if (sp.rk == BC_A2) { x[n - 1] += sp.aR * bM1 + sp.bR * bM2; }
-        // forward L y = Γb, backward Lᵀ x = y (src/banded_cholesky.jl:202-231)
-        double y1 = 0, y2 = 0, y3 = 0;  // y[i-1], y[i-2], y[i-3]
-        for (int i = 0; i < n; i++) {
-            double sacc = x[i];
-            if (i >= 3) sacc -= Ls[(i - 3) * 4 + 3] * y3;
-            if (i >= 2) sacc -= Ls[(i - 2) * 4 + 2] * y2;
-            if (i >= 1) sacc -= Ls[(i - 1) * 4 + 1] * y1;
-            double yi = sacc * Di[i];
-            x[i] = yi;
-            y3 = y2; y2 = y1; y1 = yi;
+        gamma_fold(sp, x, Md, n);
+        if constexpr (kF32) {
+            S *r = R + threadIdx.x * ld;
+            for (int i = 0; i < n; i++) r[i] = x[i];  // keep Γb
+            band_solve(Ls, Di, x, n);
+            // residual r = Γb − A x with A the FP64 open-form band, in df64
+            for (int i = 0; i < n; i++) {
+                df64 acc = df64(r[i]);
+                for (int j = max(0, i - 3); j <= min(n - 1, i + 3); j++) {
+                    const int lo = min(i, j), dd = abs(i - j);
+                    const float2 a = __ldg(sp.Aband_x + lo * 4 + dd);
+                    acc = acc - df_mul_f(df64(a.x, a.y), x[j]);
+                }
+                r[i] = acc.hi + acc.lo;
+            }
+            band_solve(Ls, Di, r, n);
+            for (int i = 0; i < n; i++) x[i] = x[i] + r[i];
+        } else {
+            band_solve(Ls, Di, x, n);
         }
-        double x1 = 0, x2 = 0, x3 = 0;  // x[i+1], x[i+2], x[i+3]
-        for (int i = n - 1; i >= 0; i--) {
-            double sacc = x[i];
-            if (i + 1 < n) sacc -= Ls[i * 4 + 1] * x1;
-            if (i + 2 < n) sacc -= Ls[i * 4 + 2] * x2;
-            if (i + 3 < n) sacc -= Ls[i * 4 + 3] * x3;
-            double xi = sacc * Di[i];
-            x[i] = xi;
-            x3 = x2; x2 = x1; x1 = xi;
-        }
-        // Γᵀ x (src/CubicBSpline.jl:461-500)
-        const double s0v = x[0], s1v = x[1], sM1 = x[n - 1], sM2 = x[n - 2];
-        for (int i = n - 1; i >= 0; i--) x[i + rL] = x[i];
-        for (int j = 0; j < rL; j++) x[j] = 0.0;
-        for (int j = Md - sp.rankR; j < Md; j++) x[j] = 0.0;
-        if (sp.lk == BC_A1) x[0] = sp.aL * s0v + sp.bL * s1v;
-        else if (sp.lk == BC_A2) { x[0] = sp.aL * s0v; x[1] = sp.bL * s0v; }
-        if (sp.rk == BC_A1) x[Md - 1] = sp.aR * sM1 + sp.bR * sM2;
-        else if (sp.rk == BC_A2) { x[Md - 2] = sp.bR * sM1; x[Md - 1] = sp.aR * sM1; }
-        if (sp.r3x && P.ahat) {
-            const double *ah = P.ahat + ((size_t)v * P.nblocks + (size_t)zb * P.nslots_z + s0 + threadIdx.x) * b;
-            for (int i = 0; i < Md; i++) x[i] += ah[i];
+        gamma_unfold(sp, x, Md, n);
+        if (ah)
+            for (int i = 0; i < Md; i++) x[i] = (S)((double)x[i] + ah[i]);
+        if constexpr (!kSameX) {
+            T *xt = XT + threadIdx.x * ld;
+            for (int i = 0; i < Md; i++) xt[i] = to_compute<T>((double)x[i]);
         }
     }
     __syncthreads();
@@ -304,18 +369,19 @@ __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch P) {
     // SI at the iDim mish points for the slots each ring carries
     const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
     const int s = s0 + lane;
-    const double *xa = X + lane * ld;
-    for (int r = grp; r < P.iDim; r += 4) {
-        const int ri = r + 1 + P.pOL;
+    const T *xa = XT + lane * ld;
+    for (int r = grp; r < A.iDim; r += 4) {
+        const int ri = r + 1 + A.pOL;
         if (lane >= nsl || s >= 1 + 2 * ri) continue;
         const int m0 = sp.si_m0[r];
-        const double a0 = xa[m0], a1 = xa[m0 + 1], a2 = xa[m0 + 2], a3 = xa[m0 + 3];
-        const size_t orow = P.fofs[r] + s;
+        const T a0 = xa[m0], a1 = xa[m0 + 1], a2 = xa[m0 + 2], a3 = xa[m0 + 3];
+        const size_t orow = A.fofs[r] + s;
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            const double *w = sp.siw + ((size_t)d * P.iDim + r) * 4;
-            double u = w[0] * a0 + w[1] * a1 + w[2] * a2 + w[3] * a3;
-            ((T *)P.G)[((size_t)d * P.nitems + item) * P.frows + orow] = (T)u;
+            const int64_t w = ((int64_t)d * A.iDim + r) * 4;
+            T u = ld_real<T>(sp.siw_t, w) * a0 + ld_real<T>(sp.siw_t, w + 1) * a1 +
+                  ld_real<T>(sp.siw_t, w + 2) * a2 + ld_real<T>(sp.siw_t, w + 3) * a3;
+            ((T *)A.G)[((size_t)d * A.nitems + item) * A.frows + orow] = u;
         }
     }
 }
@@ -324,41 +390,46 @@ __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch P) {
 // cheb_forward: DCT-I of each kz-point column, scaled 1/(2(kz-1)), first bk modes
 // (CBtransform!, src/Chebyshev.jl:417-426).  CTA = 64 consecutive columns.
 // ====================================================================
-template <typename T>
-__global__ void __launch_bounds__(256) cheb_forward_kernel(ChebLaunch P) {
+__device__ __forceinline__ int ring_of_column(const RingDesc *rings, int iDim, int64_t q) {
+    int lo = 0, hi = iDim - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rings[mid].jofs <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <typename P, typename T>
+__global__ void __launch_bounds__(256) cheb_forward_kernel(ChebLaunch C) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int v = blockIdx.y;
-    const ChebDev &cb = P.cheb[v];
+    const ChebDev &cb = C.cheb[v];
     const int N = cb.N, bk = cb.bk, half = cb.half;
-    T *xs = reinterpret_cast<T *>(smem_raw);  // 64 × N
-    T *fw = xs + 64 * N;                        // bk × half
+    const int ldx = N | 1;                      // odd column stride: no bank conflicts
+    T *xs = reinterpret_cast<T *>(smem_raw);  // 64 × ldx
+    T *fw = xs + 64 * ldx;                      // bk × half
     const int64_t c0 = (int64_t)blockIdx.x * 64;
-    const int ncol = (int)((P.jDim - c0) < 64 ? (P.jDim - c0) : 64);
-    const T *in = (const T *)P.in + (size_t)v * P.np + c0 * N;
-    for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) xs[e] = in[e];
-    for (int e = threadIdx.x; e < bk * half; e += blockDim.x) fw[e] = (T)cb.fwd[e];
+    const int ncol = (int)((C.jDim - c0) < 64 ? (C.jDim - c0) : 64);
+    const P *in = (const P *)C.in + (size_t)v * C.np + c0 * N;
+    for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) xs[(e / N) * ldx + (e % N)] = to_compute<T>(in[e]);
+    for (int e = threadIdx.x; e < bk * half; e += blockDim.x) fw[e] = ld_real<T>(cb.fwd_t, e);
     __syncthreads();
     const int col = threadIdx.x & 63, kg = threadIdx.x >> 6;  // 4 groups of modes
     if (col < ncol) {
         const int64_t q = c0 + col;
-        // ring of column q (binary search in ring start table)
-        int lo = 0, hi = P.iDim - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (P.rings[mid].jofs <= q) lo = mid; else hi = mid - 1;
-        }
-        const RingDesc &rd = P.rings[lo];
+        const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
         const int l = (int)(q - rd.jofs);
-        T *out = (T *)P.out + (size_t)v * P.bk * P.jDim + (size_t)P.bk * rd.jofs + l;
-        const T *x = xs + col * N;
+        T *out = (T *)C.out + (size_t)v * C.bk * C.jDim + (size_t)C.bk * rd.jofs + l;
+        const T *x = xs + col * ldx;
         for (int k = kg; k < bk; k += 4) {
             const T *row = fw + k * half;
-            T acc = T(0);
+            T acc = T(0.0f);
             const bool odd = k & 1;
             for (int j = 0; j < half; j++) {
                 const int jj = N - 1 - j;
                 T e = (jj == j) ? x[j] : (odd ? x[j] - x[jj] : x[j] + x[jj]);
-                acc += row[j] * e;
+                acc = acc + row[j] * e;
             }
             out[(size_t)k * rd.L] = acc;
         }
@@ -370,82 +441,84 @@ __global__ void __launch_bounds__(256) cheb_forward_kernel(ChebLaunch P) {
 // CItransform! (DCT-I); variant 0 also CIx/CIxx (recurrence, src/Chebyshev.jl:636-646).
 // CTA = 64 consecutive columns of one variable; grid.z = ring variant.
 // ====================================================================
-template <typename T>
-__global__ void __launch_bounds__(256) cheb_inverse_kernel(ChebLaunch P) {
+template <typename P, typename T>
+__global__ void __launch_bounds__(256) cheb_inverse_kernel(ChebLaunch C) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int64_t col_base[64];  // H offset of column (ring start + l) for z_b = 0
+    __shared__ int col_L[64];
     const int v = blockIdx.y, var = blockIdx.z;
-    const ChebDev &cb = P.cheb[v];
+    const ChebDev &cb = C.cheb[v];
     const int N = cb.N, bk = cb.bk, half = cb.half;
     const int ne = (N + 1) / 2, no = N / 2;
-    T *as = reinterpret_cast<T *>(smem_raw);  // 64 × N coefficients
-    T *us = as + 64 * N;                        // 64 × N outputs
-    T *ie = us + 64 * N;                        // half × ne
+    const int ldn = N | 1, ldb = bk | 1;        // odd strides: no bank conflicts
+    T *as = reinterpret_cast<T *>(smem_raw);  // 64 × ldn coefficients
+    T *us = as + 64 * ldn;                      // 64 × ldn outputs
+    T *ie = us + 64 * ldn;                      // half × ne
     T *io = ie + half * ne;                     // half × no
-    T *bs = io + half * (no > 0 ? no : 1);      // 64 × bk inputs
+    T *bs = io + half * (no > 0 ? no : 1);      // 64 × ldb inputs
     const int64_t c0 = (int64_t)blockIdx.x * 64;
-    const int ncol = (int)((P.jDim - c0) < 64 ? (P.jDim - c0) : 64);
-    for (int e = threadIdx.x; e < half * ne; e += blockDim.x) ie[e] = (T)cb.inv_e[e];
-    for (int e = threadIdx.x; e < half * no; e += blockDim.x) io[e] = (T)cb.inv_o[e];
+    const int ncol = (int)((C.jDim - c0) < 64 ? (C.jDim - c0) : 64);
+    for (int e = threadIdx.x; e < half * ne; e += blockDim.x) ie[e] = ld_real<T>(cb.inv_e_t, e);
+    for (int e = threadIdx.x; e < half * no; e += blockDim.x) io[e] = ld_real<T>(cb.inv_o_t, e);
+    if (threadIdx.x < ncol) {
+        const int64_t q = c0 + threadIdx.x;
+        const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
+        col_base[threadIdx.x] = (int64_t)C.bk * rd.jofs + (q - rd.jofs);
+        col_L[threadIdx.x] = rd.L;
+    }
+    __syncthreads();
     // gather the bk ring outputs of each column
-    const T *H = (const T *)P.in + ((size_t)var * P.nvars + v) * P.bk * P.jDim;
+    const T *H = (const T *)C.in + ((size_t)var * C.nvars + v) * C.bk * C.jDim;
     for (int e = threadIdx.x; e < ncol * bk; e += blockDim.x) {
         const int zb = e / ncol, col = e % ncol;
-        const int64_t q = c0 + col;
-        int lo = 0, hi = P.iDim - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (P.rings[mid].jofs <= q) lo = mid; else hi = mid - 1;
-        }
-        const RingDesc &rd = P.rings[lo];
-        bs[col * bk + zb] = H[(size_t)P.bk * rd.jofs + (size_t)zb * rd.L + (q - rd.jofs)];
+        bs[col * ldb + zb] = H[col_base[col] + (int64_t)zb * col_L[col]];
     }
     __syncthreads();
     const int col = threadIdx.x & 63, jg = threadIdx.x >> 6;
     // CA: a_j = b_j (j < bk) + Σ_p (u_p·b) v_p[j]
     if (col < ncol) {
-        const T *bb = bs + col * bk;
-        T sp[2] = {T(0), T(0)};
+        const T *bb = bs + col * ldb;
+        T sp[2] = {T(0.0f), T(0.0f)};
         for (int p = 0; p < cb.nrank; p++) {
-            T acc = T(0);
-            for (int i = 0; i < bk; i++) acc += (T)cb.gu[p * bk + i] * bb[i];
+            T acc = T(0.0f);
+            for (int i = 0; i < bk; i++) acc = acc + ld_real<T>(cb.gu_t, (int64_t)p * bk + i) * bb[i];
             sp[p] = acc;
         }
         for (int j = jg; j < N; j += 4) {
-            T aj = (j < bk) ? bb[j] : T(0);
-            for (int p = 0; p < cb.nrank; p++) aj += (T)cb.gv[p * N + j] * sp[p];
-            as[col * N + j] = aj;
+            T aj = (j < bk) ? bb[j] : T(0.0f);
+            for (int p = 0; p < cb.nrank; p++) aj = aj + ld_real<T>(cb.gv_t, (int64_t)p * N + j) * sp[p];
+            as[col * ldn + j] = aj;
         }
     }
     __syncthreads();
     const int nd = (var == 0) ? 3 : 1;
+    const T dsc = to_compute<T>(cb.dscale);
     for (int dd = 0; dd < nd; dd++) {
         if (dd > 0) {
-            // CIxcoefficients in place (src/Chebyshev.jl:636-646):
-            // ax[N-1] = 0, ax[i] = 2(i+1) a[i+1] + ax[i+2] for i = N-2..0, then ax /= dscale
+            // CIxcoefficients in place: ax[N-1] = 0, ax[i] = 2(i+1) a[i+1] + ax[i+2], then ax /= dscale
             if (jg == 0 && col < ncol) {
-                T *a = as + col * N;
+                T *a = as + col * ldn;
                 T a_next = a[N - 1];
-                a[N - 1] = T(0);
-                T ax1 = T(0), ax2 = T(0);  // ax[i+1], ax[i+2]
+                a[N - 1] = T(0.0f);
+                T ax1 = T(0.0f), ax2 = T(0.0f);  // ax[i+1], ax[i+2]
                 for (int i = N - 2; i >= 0; i--) {
-                    T axi = T(2.0 * (i + 1)) * a_next + ax2;
+                    T axi = scale_f(a_next, (float)(2 * (i + 1))) + ax2;
                     a_next = a[i];
                     a[i] = axi;
                     ax2 = ax1;
                     ax1 = axi;
                 }
-                const T sc = (T)cb.dscale;
-                for (int j = 0; j < N; j++) a[j] = a[j] / sc;
+                for (int j = 0; j < N; j++) a[j] = a[j] / dsc;
             }
             __syncthreads();
         }
         if (col < ncol) {
-            const T *a = as + col * N;
-            T *u = us + col * N;
+            const T *a = as + col * ldn;
+            T *u = us + col * ldn;
             for (int j = jg; j < half; j += 4) {
-                T E = T(0), O = T(0);
-                for (int k = 0; k < ne; k++) E += ie[j * ne + k] * a[2 * k];
-                for (int k = 0; k < no; k++) O += io[j * no + k] * a[2 * k + 1];
+                T E = T(0.0f), O = T(0.0f);
+                for (int k = 0; k < ne; k++) E = E + ie[j * ne + k] * a[2 * k];
+                for (int k = 0; k < no; k++) O = O + io[j * no + k] * a[2 * k + 1];
                 u[j] = E + O;
                 if (N - 1 - j != j) u[N - 1 - j] = E - O;
             }
@@ -455,8 +528,8 @@ __global__ void __launch_bounds__(256) cheb_inverse_kernel(ChebLaunch P) {
         int slot;
         if (var == 0) slot = (dd == 0) ? 1 : (dd == 1 ? 6 : 7);
         else slot = (var == 1) ? 4 : (var == 2 ? 5 : (var == 3 ? 2 : 3));
-        T *dst = (T *)P.out + ((size_t)(slot - 1) * P.nvars + v) * P.np + c0 * N;
-        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) dst[e] = us[e];
+        P *dst = (P *)C.out + ((size_t)(slot - 1) * C.nvars + v) * C.np + c0 * N;
+        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) dst[e] = to_storage<P>(us[(e / N) * ldn + (e % N)]);
         __syncthreads();
     }
 }
@@ -464,59 +537,168 @@ __global__ void __launch_bounds__(256) cheb_inverse_kernel(ChebLaunch P) {
 // ====================================================================
 // launchers
 // ====================================================================
-template <typename T>
-cudaError_t launch_ring_forward(const RingLaunch &L, int nrings, int nitems, size_t smem, cudaStream_t st) {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(ring_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    ring_forward_kernel<T><<<dim3(nrings, nitems), 256, smem, st>>>(L);
+template <typename K>
+static void set_smem(K kernel, size_t smem) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+template <typename P, typename T>
+cudaError_t launch_ring_forward(const RingLaunch &L, int nrings, int nitems, size_t smem, int threads,
+                                cudaStream_t st) {
+    set_smem(ring_forward_kernel<P, T>, smem);
+    ring_forward_kernel<P, T><<<dim3(nrings, nitems), threads, smem, st>>>(L);
     return cudaGetLastError();
 }
-template <typename T>
-cudaError_t launch_ring_inverse(const RingLaunch &L, int nrings, int nitems, size_t smem, cudaStream_t st) {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(ring_inverse_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    ring_inverse_kernel<T><<<dim3(nrings, nitems), 256, smem, st>>>(L);
+template <typename P, typename T>
+cudaError_t launch_ring_inverse(const RingLaunch &L, int nrings, int nitems, size_t smem, int threads,
+                                cudaStream_t st) {
+    set_smem(ring_inverse_kernel<P, T>, smem);
+    ring_inverse_kernel<P, T><<<dim3(nrings, nitems), threads, smem, st>>>(L);
     return cudaGetLastError();
 }
-template <typename T>
-cudaError_t launch_sb_project(const SbLaunch &P, int nitems, cudaStream_t st) {
-    dim3 grid((P.nslots_z + 31) / 32, (P.b + 63) / 64, nitems);
-    sb_project_kernel<T><<<grid, dim3(32, 8), 0, st>>>(P);
+template <typename P, typename T>
+cudaError_t launch_sb_project(const SbLaunch &S, int nitems, cudaStream_t st) {
+    dim3 grid((S.nslots_z + 31) / 32, (S.b + 63) / 64, nitems);
+    sb_project_kernel<P, T><<<grid, dim3(32, 8), 0, st>>>(S);
     return cudaGetLastError();
 }
-template <typename T>
-cudaError_t launch_sa_si(const SaLaunch &P, int nitems, size_t smem, cudaStream_t st) {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(sa_si_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((P.nslots_z + 31) / 32, nitems);
-    sa_si_kernel<T><<<grid, 128, smem, st>>>(P);
+template <typename P, typename T>
+cudaError_t launch_sa_si(const SaLaunch &A, int nitems, size_t smem, cudaStream_t st) {
+    set_smem(sa_si_kernel<P, T>, smem);
+    dim3 grid((A.nslots_z + 31) / 32, nitems);
+    sa_si_kernel<P, T><<<grid, 128, smem, st>>>(A);
     return cudaGetLastError();
 }
-template <typename T>
-cudaError_t launch_cheb_forward(const ChebLaunch &P, size_t smem, cudaStream_t st) {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(cheb_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((unsigned)((P.jDim + 63) / 64), P.nvars);
-    cheb_forward_kernel<T><<<grid, 256, smem, st>>>(P);
+template <typename P, typename T>
+cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st) {
+    set_smem(cheb_forward_kernel<P, T>, smem);
+    dim3 grid((unsigned)((C.jDim + 63) / 64), C.nvars);
+    cheb_forward_kernel<P, T><<<grid, 256, smem, st>>>(C);
     return cudaGetLastError();
 }
-template <typename T>
-cudaError_t launch_cheb_inverse(const ChebLaunch &P, size_t smem, cudaStream_t st) {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(cheb_inverse_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((unsigned)((P.jDim + 63) / 64), P.nvars, 5);
-    cheb_inverse_kernel<T><<<grid, 256, smem, st>>>(P);
+template <typename P, typename T>
+cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t st) {
+    set_smem(cheb_inverse_kernel<P, T>, smem);
+    dim3 grid((unsigned)((C.jDim + 63) / 64), C.nvars, 5);
+    cheb_inverse_kernel<P, T><<<grid, 256, smem, st>>>(C);
     return cudaGetLastError();
 }
 
-#define SS_INSTANTIATE(T)                                                                                   \
-    template cudaError_t launch_ring_forward<T>(const RingLaunch &, int, int, size_t, cudaStream_t);       \
-    template cudaError_t launch_ring_inverse<T>(const RingLaunch &, int, int, size_t, cudaStream_t);       \
-    template cudaError_t launch_sb_project<T>(const SbLaunch &, int, cudaStream_t);                        \
-    template cudaError_t launch_sa_si<T>(const SaLaunch &, int, size_t, cudaStream_t);                     \
-    template cudaError_t launch_cheb_forward<T>(const ChebLaunch &, size_t, cudaStream_t);                 \
-    template cudaError_t launch_cheb_inverse<T>(const ChebLaunch &, size_t, cudaStream_t);
-SS_INSTANTIATE(double)
-SS_INSTANTIATE(float)
+// ====================================================================
+// RL chain coupling: SA of 32 primary slots per CTA (FP64), the three
+// interface coefficients, times the 3×3 coupling matrix
+// (COUPLING_MATRIX_1X / _2X, src/multipatch.jl:21-33).
+// ====================================================================
+template <typename P>
+__global__ void __launch_bounds__(32) chain_couple_kernel(ChainLaunch C) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int v = blockIdx.y;
+    const SplineDev &sp = C.spl[v];
+    const int b = C.b_p, ld = C.ld, n = sp.Min;
+    double *X = reinterpret_cast<double *>(smem_raw);
+    double *Ls = X + 32 * ld;
+    double *Di = Ls + 4 * n;
+    const int q0 = blockIdx.x * 32;
+    const int nsl = min(32, C.nq - q0);
+    const P *spec = (const P *)C.spec + (size_t)v * C.nspec_p + (size_t)q0 * b;
+    for (int e = threadIdx.x; e < nsl * b; e += blockDim.x) X[(e / b) * ld + (e % b)] = (double)spec[e];
+    for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) Ls[e] = sp.L4[e];
+    for (int e = threadIdx.x; e < n; e += blockDim.x) Di[e] = sp.dinv[e];
+    __syncthreads();
+    if (threadIdx.x < nsl) {
+        double *x = X + threadIdx.x * ld;
+        gamma_fold(sp, x, b, n);
+        band_solve(Ls, Di, x, n);
+        gamma_unfold(sp, x, b, n);
+        const double e0 = x[C.node[0]], e1 = x[C.node[1]], e2 = x[C.node[2]];
+        double *out = C.coupled + ((size_t)v * C.nq + q0 + threadIdx.x) * 3;
+        for (int r = 0; r < 3; r++) out[r] = C.C[r * 3] * e0 + C.C[r * 3 + 1] * e1 + C.C[r * 3 + 2] * e2;
+    }
+}
+
+// registry[q] = (spline-object ahat with this interface's side replaced by the
+// coupled values of slot q): _write_interface_ahat! + _set_wavenumber_ahat!
+// copy the whole shared ahat vector, src/multipatch.jl:533-560
+__global__ void chain_assemble_kernel(ChainLaunch C) {
+    const int64_t total = (int64_t)C.nvars * C.nq * C.b_s;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % C.b_s);
+        const int q = (int)((e / C.b_s) % C.nq);
+        const int v = (int)(e / ((int64_t)C.b_s * C.nq));
+        const int obj = (q == 0) ? 0 : ((q & 1) ? 1 : 2);
+        double val = C.state[((size_t)v * 3 + obj) * C.b_s + i];
+        const double *cp = C.coupled + ((size_t)v * C.nq + q) * 3;
+        if (C.side == 0 && i < 3) val = cp[i];
+        if (C.side == 1 && i >= C.b_s - 3) val = cp[i - (C.b_s - 3)];
+        C.reg[((size_t)v * C.nblocks_s + q) * C.b_s + i] = val;
+    }
+}
+// after the loop over wavenumbers each spline object keeps its last slot's values
+__global__ void chain_state_kernel(ChainLaunch C) {
+    const int v = blockIdx.x, obj = threadIdx.x / 3, r = threadIdx.x % 3;
+    if (v >= C.nvars || obj >= 3) return;
+    int q_last = -1;
+    if (obj == 0) q_last = 0;
+    else if (C.nq >= 3) q_last = (obj == 1) ? C.nq - 2 : C.nq - 1;
+    if (q_last < 0) return;
+    double *st = C.state + ((size_t)v * 3 + obj) * C.b_s + (C.side == 0 ? 0 : C.b_s - 3);
+    st[r] = C.coupled[((size_t)v * C.nq + q_last) * 3 + r];
+}
+
+template <typename P>
+cudaError_t launch_chain_couple(const ChainLaunch &C, size_t smem, cudaStream_t st) {
+    set_smem(chain_couple_kernel<P>, smem);
+    chain_couple_kernel<P><<<dim3((C.nq + 31) / 32, C.nvars), 32, smem, st>>>(C);
+    return cudaGetLastError();
+}
+cudaError_t launch_chain_assemble(const ChainLaunch &C, cudaStream_t st) {
+    const int64_t total = (int64_t)C.nvars * C.nq * C.b_s;
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, 4096);
+    chain_assemble_kernel<<<blocks, 256, 0, st>>>(C);
+    chain_state_kernel<<<C.nvars, 9, 0, st>>>(C);
+    return cudaGetLastError();
+}
+template cudaError_t launch_chain_couple<double>(const ChainLaunch &, size_t, cudaStream_t);
+template cudaError_t launch_chain_couple<float>(const ChainLaunch &, size_t, cudaStream_t);
+
+// ====================================================================
+// tile halo sum: patch spectral blocks += tile spectral blocks at the tile's
+// spectralIndexL offset (sumSpectralTile!); set = 1 overwrites instead.
+// ====================================================================
+template <typename P>
+__global__ void tile_sum_kernel(TileLaunch T) {
+    const int64_t per_var = (int64_t)T.bk * T.blocks_t * T.b_t;
+    const int64_t total = per_var * T.nvars;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int v = (int)(e / per_var);
+        int64_t r = e % per_var;
+        const int m = (int)(r % T.b_t);
+        r /= T.b_t;
+        const int blk = (int)(r % T.blocks_t);
+        const int zb = (int)(r / T.blocks_t);
+        const P tv = ((const P *)T.tile)[(size_t)v * T.nspec_t + ((size_t)zb * T.blocks_t + blk) * T.b_t + m];
+        P *pp = (P *)T.patch + (size_t)v * T.nspec_p + ((size_t)zb * T.blocks_p + blk) * T.b_p + T.offset + m;
+        *pp = T.set ? tv : (*pp + tv);
+    }
+}
+template <typename P>
+cudaError_t launch_tile_sum(const TileLaunch &T, cudaStream_t st) {
+    const int64_t total = (int64_t)T.bk * T.blocks_t * T.b_t * T.nvars;
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, 8192);
+    tile_sum_kernel<P><<<blocks, 256, 0, st>>>(T);
+    return cudaGetLastError();
+}
+template cudaError_t launch_tile_sum<double>(const TileLaunch &, cudaStream_t);
+template cudaError_t launch_tile_sum<float>(const TileLaunch &, cudaStream_t);
+
+#define SS_INSTANTIATE(P, T)                                                                                 \
+    template cudaError_t launch_ring_forward<P, T>(const RingLaunch &, int, int, size_t, int, cudaStream_t); \
+    template cudaError_t launch_ring_inverse<P, T>(const RingLaunch &, int, int, size_t, int, cudaStream_t); \
+    template cudaError_t launch_sb_project<P, T>(const SbLaunch &, int, cudaStream_t);                      \
+    template cudaError_t launch_sa_si<P, T>(const SaLaunch &, int, size_t, cudaStream_t);                   \
+    template cudaError_t launch_cheb_forward<P, T>(const ChebLaunch &, size_t, cudaStream_t);               \
+    template cudaError_t launch_cheb_inverse<P, T>(const ChebLaunch &, size_t, cudaStream_t);
+SS_INSTANTIATE(double, double)
+SS_INSTANTIATE(double, df64)
+SS_INSTANTIATE(float, float)
 
 }  // namespace ss

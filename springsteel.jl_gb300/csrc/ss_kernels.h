@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "ss_internal.h"
+#include "ss_df64.cuh"
 
 namespace ss {
 
@@ -13,8 +14,8 @@ struct RingLaunch {
     const RingDesc *rings;     // descriptors; variable v uses rings[v*ring_var_stride + r]
     int64_t ring_var_stride;   // iDim for RL (per-variable kmax), 0 for RLZ (shared rings)
     const FftPlan *plans;
-    const double2 *pool;       // FP64 twiddle pool
-    const double2 *phase;      // cos(k ymin), sin(k ymin) pool
+    const void *pool;          // twiddle pool (compute layout)
+    const void *phase;         // cos(k ymin), sin(k ymin) pool (compute layout)
     const void *in;
     void *out;
     int64_t in_item_stride;    // RL forward: physical stride between variables (np)
@@ -53,19 +54,48 @@ struct ChebLaunch {
     int iDim, bk, nvars;
 };
 
+// RL chain coupling (update_interface!, src/multipatch.jl:417-478)
+struct ChainLaunch {
+    const void *spec;          // primary spectral (P)
+    const SplineDev *spl;      // primary splines (per variable)
+    double *coupled;           // [v][q][3] coupled border coefficients
+    double *state;             // secondary spline-object ahat: [v][3][b_s] (k0, real, imag)
+    double *reg;               // secondary per-wavenumber registry: [v][nblocks_s][b_s]
+    int64_t nspec_p, nblocks_s;
+    int b_p, b_s, ld, nq, nvars, side;  // side of the secondary: 0 left, 1 right
+    int node[3];
+    double C[9];
+};
+// tile halo sum (sumSpectralTile!, src/tiling.jl:1048-1136)
+struct TileLaunch {
+    void *patch;               // patch spectral (P)
+    const void *tile;          // tile spectral (P)
+    int64_t nspec_p, nspec_t;
+    int b_p, b_t, blocks_p, blocks_t, bk, nvars, offset, set;
+};
+
 void fft_init_constants();
 
-template <typename T>
-cudaError_t launch_ring_forward(const RingLaunch &L, int nrings, int nitems, size_t smem, cudaStream_t st);
-template <typename T>
-cudaError_t launch_ring_inverse(const RingLaunch &L, int nrings, int nitems, size_t smem, cudaStream_t st);
-template <typename T>
-cudaError_t launch_sb_project(const SbLaunch &P, int nitems, cudaStream_t st);
-template <typename T>
-cudaError_t launch_sa_si(const SaLaunch &P, int nitems, size_t smem, cudaStream_t st);
-template <typename T>
-cudaError_t launch_cheb_forward(const ChebLaunch &P, size_t smem, cudaStream_t st);
-template <typename T>
-cudaError_t launch_cheb_inverse(const ChebLaunch &P, size_t smem, cudaStream_t st);
+template <typename P>
+cudaError_t launch_chain_couple(const ChainLaunch &C, size_t smem, cudaStream_t st);
+cudaError_t launch_chain_assemble(const ChainLaunch &C, cudaStream_t st);
+template <typename P>
+cudaError_t launch_tile_sum(const TileLaunch &T, cudaStream_t st);
+
+// P: storage type of physical/spectral; T: compute type (double | df64 | float)
+template <typename P, typename T>
+cudaError_t launch_ring_forward(const RingLaunch &L, int nrings, int nitems, size_t smem, int threads,
+                                cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_ring_inverse(const RingLaunch &L, int nrings, int nitems, size_t smem, int threads,
+                                cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_sb_project(const SbLaunch &S, int nitems, cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_sa_si(const SaLaunch &A, int nitems, size_t smem, cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t st);
 
 }  // namespace ss

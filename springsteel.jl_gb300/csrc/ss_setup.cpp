@@ -191,6 +191,7 @@ int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, doub
                 A[size_t(j - 1) * 4 + (i - j)] = v;
             }
         }
+    s.Aopen = A;
     // _band_factor3! (src/banded_cholesky.jl:166-197)
     for (int j = 0; j < n; j++) {
         double d = A[j * 4];

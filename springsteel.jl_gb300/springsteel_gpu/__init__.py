@@ -277,7 +277,7 @@ class SpringsteelGridParameters:
     def __init__(self, geometry="RL", iMin=0.0, iMax=0.0, num_cells=0, mubar=3, quadrature="gauss",
                  l_q=None, BCL=None, BCR=None, kMin=0.0, kMax=0.0, kDim=0, b_kDim=None, BCB=None, BCT=None,
                  vars=None, max_wavenumber=None, fourier_filter=None, chebyshev_filter=None,
-                 spectralIndexL=1, patchOffsetL=None, precision="f64"):
+                 spectralIndexL=1, patchOffsetL=None, precision="f64", **derived):
         geom = {"RL": "RL", "Spline1D_Fourier": "RL", "RLZ": "RLZ"}.get(geometry, geometry)
         if geom not in ("RL", "RLZ"):
             raise ValueError("only RL and RLZ geometries run on the GPU path (got %r)" % geometry)
@@ -312,7 +312,7 @@ class SpringsteelGridParameters:
         nv = len(names)
         quad = {"gauss": abi.SS_QUAD_GAUSS, "regular": abi.SS_QUAD_REGULAR}[self.quadrature]
         prec = {"f64": abi.SS_PREC_F64, "f32": abi.SS_PREC_F32_REFINED,
-                "f32_refined": abi.SS_PREC_F32_REFINED}[self.precision]
+                "f32_refined": abi.SS_PREC_F32_REFINED, "f64_fast": abi.SS_PREC_F64_FAST}[self.precision]
         geom = abi.SS_GEOM_RL if self.geometry == "RL" else abi.SS_GEOM_RLZ
         kw = dict(
             mubar=self.mubar, quadrature=quad, precision=prec, patchOffsetL=self.patchOffsetL,
@@ -345,7 +345,7 @@ class SpringsteelGrid:
         d = abi.ss_dims()
         _check(lib.ss_grid_dims(h, C.byref(d)))
         self.dims = d.as_dict()
-        self.dtype = np.float64 if gp.precision == "f64" else np.float32
+        self.dtype = np.float32 if gp.precision in ("f32", "f32_refined") else np.float64
         self._apply_filters()
 
     # -- lifetime
@@ -504,3 +504,189 @@ def getGridpoints(grid):
             zz = np.tile(zm, L)
             pts.append(np.column_stack([rr, ll, zz]))
     return np.asfortranarray(np.vstack(pts))
+
+
+# ----------------------------------------------------------------- batches
+class Batch:
+    """Many grids transformed by one launch sequence (optionally a CUDA graph)."""
+
+    def __init__(self, grids, autotune=False):
+        self.grids = list(grids)
+        lib = load_library()
+        arr = (C.c_void_p * len(self.grids))(*[g.handle for g in self.grids])
+        h = C.c_void_p()
+        _check(lib.ss_batch_create(arr, len(self.grids), 1 if autotune else 0, C.byref(h)))
+        self._h = h
+
+    def run(self, what=3, use_graph=True, stream=None):
+        """what: 1 spectralTransform!, 2 gridTransform!, 3 both."""
+        _check(load_library().ss_batch_run(self._h, int(what), 1 if use_graph else 0, stream))
+
+    def synchronize(self):
+        _check(load_library().ss_batch_synchronize(self._h))
+
+    def ring_threads(self, i):
+        f, v = C.c_int32(), C.c_int32()
+        _check(load_library().ss_batch_ring_threads(self._h, int(i), C.byref(f), C.byref(v)))
+        return f.value, v.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().ss_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------- multipatch
+class PatchChain:
+    """PatchChain(grids) (src/multipatch.jl:825-848) on the device."""
+
+    def __init__(self, grids):
+        self.patches = list(grids)
+        lib = load_library()
+        arr = (C.c_void_p * len(self.patches))(*[g.handle for g in self.patches])
+        h = C.c_void_p()
+        _check(lib.ss_chain_create(arr, len(self.patches), C.byref(h)))
+        self._h = h
+
+    def multiGridTransform(self, stream=None):
+        """multiGridTransform! (src/multipatch.jl:769-786)."""
+        _check(load_library().ss_multi_grid_transform(self._h, stream))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().ss_chain_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def compute_patch_offsets(boundaries, cells, mubar=3):
+    """_compute_patch_offsets (src/multipatch.jl:998-1014) for cylindrical grids."""
+    offsets, cumulative = [], 0
+    if boundaries[0] > 0:
+        dx_first = (boundaries[1] - boundaries[0]) / cells[0]
+        cumulative = int(round(boundaries[0] / dx_first)) * mubar
+    for c in cells:
+        offsets.append(cumulative)
+        cumulative += c * mubar
+    return offsets
+
+
+def chain_grid_params(boundaries, cells, vars=None, BCL=None, BCR=None, mubar=3, l_q=None, precision="f64"):
+    """Per-patch parameters of a chain (_create_chain, src/multipatch.jl:1018-1111):
+    at each interface the finer side gets FixedBC (R3X), the coarser NaturalBC;
+    patch offsets follow _compute_patch_offsets."""
+    n = len(boundaries) - 1
+    cells = [cells] * n if isinstance(cells, int) else list(cells)
+    vars = vars or {"u": 1}
+    dx = [(boundaries[k + 1] - boundaries[k]) / cells[k] for k in range(n)]
+    for k in range(n - 1):
+        ratio = max(dx[k], dx[k + 1]) / min(dx[k], dx[k + 1])
+        tol = 1e-10 * max(dx[k], dx[k + 1])
+        if not (abs(ratio - 1.0) < tol or abs(ratio - 2.0) < tol):
+            raise ValueError("Adjacent DX ratio between patches %d and %d is %.4g:1, must be 1:1 or 2:1" %
+                             (k + 1, k + 2, ratio))
+    bl = [{"default": NaturalBC()} for _ in range(n)]
+    br = [{"default": NaturalBC()} for _ in range(n)]
+    for k in range(n - 1):
+        if dx[k] >= dx[k + 1]:
+            bl[k + 1] = {"default": FixedBC()}
+        else:
+            br[k] = {"default": FixedBC()}
+    bl[0] = BCL or {"default": NaturalBC()}
+    br[-1] = BCR or {"default": NaturalBC()}
+    offs = compute_patch_offsets(boundaries, cells, mubar)
+    return [SpringsteelGridParameters(geometry="RL", iMin=boundaries[k], iMax=boundaries[k + 1], num_cells=cells[k],
+                                      mubar=mubar, vars=vars, BCL=bl[k], BCR=br[k], l_q=l_q,
+                                      patchOffsetL=offs[k], precision=precision) for k in range(n)]
+
+
+# ----------------------------------------------------------------- tiles
+def calcTileSizes(gp, num_tiles):
+    """calcTileSizes for cylindrical grids (src/tiling.jl:185-259): tile parameters
+    balanced by ring points, at least 3 cells per tile."""
+    if gp.num_cells / num_tiles < 3.0:
+        raise ValueError("Too many tiles for this grid (need at least 3 cells per tile)")
+    DX = (gp.iMax - gp.iMin) / gp.num_cells
+    iMins, iMaxs = [0.0] * num_tiles, [0.0] * num_tiles
+    nc, siL = [0] * num_tiles, [1] * num_tiles
+    if num_tiles == 1:
+        iMins[0], iMaxs[0], nc[0] = gp.iMin, gp.iMax, gp.num_cells
+    else:
+        lpoints = [4 + 4 * (r + gp.patchOffsetL) for r in range(1, gp.iDim + 1)]
+        jDim = sum(lpoints)
+        q, r_rem = divmod(jDim, num_tiles)
+        targets = [q + 1 if i < r_rem else q for i in range(num_tiles)]
+        target = 1.0
+        nc = [0] * num_tiles
+        while any(c < 3 for c in nc) and target > 0.1:
+            t = num_tiles - 1
+            cell_count = 0
+            target -= 0.1
+            tile_count = [0] * num_tiles
+            nc = [0] * num_tiles
+            tile_min = int(target * targets[0])
+            for ri in range(gp.iDim, 0, -1):
+                tile_count[t] += lpoints[ri - 1]
+                if ri % 3 == 0:
+                    cell_count += 1
+                    if cell_count >= 3 and tile_count[t] >= tile_min:
+                        nc[t] = cell_count
+                        cell_count = 0
+                        t -= 1
+                if t < 0:
+                    break
+            nc[0] = gp.num_cells - sum(nc[1:])
+        if any(c < 3 for c in nc):
+            raise ValueError("Too many tiles for this grid (need at least 3 cells per tile)")
+        iMins[0] = gp.iMin
+        iMaxs[0] = nc[0] * DX + iMins[0]
+        for i in range(1, num_tiles - 1):
+            iMins[i] = iMaxs[i - 1]
+            iMaxs[i] = nc[i] * DX + iMins[i]
+            siL[i] = nc[i - 1] + siL[i - 1]
+        iMins[-1] = iMaxs[-2]
+        iMaxs[-1] = gp.iMax
+        siL[-1] = nc[-2] + siL[-2]
+        nc[-1] = gp.num_cells - sum(nc[:-1])
+    tiles = []
+    for i in range(num_tiles):
+        kw = dict(gp.__dict__)
+        for k in ("iDim", "b_iDim", "patchOffsetL"):
+            kw.pop(k, None)
+        kw.update(iMin=iMins[i], iMax=iMaxs[i], num_cells=nc[i], spectralIndexL=siL[i])
+        tiles.append(SpringsteelGridParameters(**kw))
+    return tiles
+
+
+def sumSpectralTile_b(patch, tile, stream=None):
+    """sumSpectralTile!(patch, tile) (src/tiling.jl:1048-1136) on the device."""
+    _check(load_library().ss_tile_sum_spectral(patch.handle, tile.handle, 0, stream))
+
+
+def setSpectralTile_b(patch, tile, stream=None):
+    """setSpectralTile!: zero the patch spectral, then write the tile's blocks."""
+    _check(load_library().ss_grid_zero_spectral(patch.handle, stream))
+    _check(load_library().ss_tile_sum_spectral(patch.handle, tile.handle, 1, stream))
+
+
+def tile_physical_from_patch(patch, tile, slot=1, stream=None):
+    _check(load_library().ss_tile_copy_physical(patch.handle, tile.handle, int(slot), 0, stream))
+
+
+def tile_physical_to_patch(patch, tile, slot=0, stream=None):
+    _check(load_library().ss_tile_copy_physical(patch.handle, tile.handle, int(slot), 1, stream))
+
+
+def zero_spectral(grid, stream=None):
+    _check(load_library().ss_grid_zero_spectral(grid.handle, stream))

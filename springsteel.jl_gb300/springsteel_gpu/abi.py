@@ -28,6 +28,7 @@ SS_GEOM_RL = 1
 SS_GEOM_RLZ = 2
 SS_PREC_F64 = 0
 SS_PREC_F32_REFINED = 1
+SS_PREC_F64_FAST = 2
 SS_DTYPE_F64 = 0
 SS_DTYPE_F32 = 1
 SS_QUAD_GAUSS = 0
@@ -150,6 +151,9 @@ EXPORTED = [
     "ss_spectral_transform", "ss_grid_transform", "ss_grid_set_filter", "ss_grid_set_ahat",
     "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
     "ss_spectral_transform_noalloc",
+    "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads",
+    "ss_chain_create", "ss_chain_destroy", "ss_multi_grid_transform",
+    "ss_tile_sum_spectral", "ss_tile_copy_physical", "ss_grid_zero_spectral",
 ]
 
 STAGES = ["cheb_forward", "ring_forward", "sb_project", "sa_si", "ring_inverse", "cheb_inverse"]
@@ -181,6 +185,17 @@ def bind(lib):
         "ss_grid_profile": ([vp, i32], i32),
         "ss_grid_profile_read": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)], i32),
         "ss_spectral_transform_noalloc": ([vp, vp, vp, vp], i32),
+        "ss_batch_create": ([vp, i32, i32, C.POINTER(vp)], i32),
+        "ss_batch_destroy": ([vp], i32),
+        "ss_batch_run": ([vp, i32, i32, vp], i32),
+        "ss_batch_synchronize": ([vp], i32),
+        "ss_batch_ring_threads": ([vp, i32, C.POINTER(i32), C.POINTER(i32)], i32),
+        "ss_chain_create": ([vp, i32, C.POINTER(vp)], i32),
+        "ss_chain_destroy": ([vp], i32),
+        "ss_multi_grid_transform": ([vp, vp], i32),
+        "ss_tile_sum_spectral": ([vp, vp, i32, vp], i32),
+        "ss_tile_copy_physical": ([vp, vp, i32, i32, vp], i32),
+        "ss_grid_zero_spectral": ([vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -1,0 +1,109 @@
+"""GPU batches (CUDA graph, autotuner), RL chain coupling and radial tiles."""
+import numpy as np
+import pytest
+
+import oracle as O
+import springsteel_gpu as S
+from springsteel_gpu import fields
+from test_gpu_parity import TOL64, slot_errors
+
+pytestmark = pytest.mark.gpu
+
+
+def _fill(g, seed):
+    pts = S.getGridpoints(g)
+    nv = g.dims["nvars"]
+    u = np.empty((pts.shape[0], nv), order="F")
+    for v in range(nv):
+        u[:, v] = fields.blob_sum(pts, seed=seed * 10 + v, nblobs=6, wmin=3.0, wmax=12.0,
+                                  zmax=max(g.params.kMax, 1.0))
+    g.set_physical(u, slot=1)
+    return u
+
+
+def test_config3_chain_parity():
+    ps = S.chain_grid_params([0.0, 40.0, 100.0, 140.0], [40, 120, 40], vars={"u": 1, "w": 2})
+    gs = [S.createGrid(p) for p in ps]
+    os_ = [O.OracleGrid(p.to_abi()) for p in ps]
+    specs = []
+    for i, (g, o) in enumerate(zip(gs, os_)):
+        u = _fill(g, seed=i + 1)
+        ph = np.zeros(o.physical_shape, order="F")
+        ph[:, :, 0] = u
+        specs.append(o.spectral_transform(ph))
+        S.spectralTransform_b(g)
+    chain = S.PatchChain(gs)
+    och = O.OracleChain(os_)
+    # two calls in a row: the second sees the shared spline-object ahat state the
+    # first left behind, as the reference's reused spline objects do
+    for _ in range(2):
+        chain.multiGridTransform()
+        ref = och.multi_grid_transform(specs)
+        for p, g, r in zip(ps, gs, ref):
+            errs = slot_errors(g.get_physical(), r, p)
+            assert np.all(errs <= TOL64), errs
+
+
+def test_two_patch_chain_linear_exactness():
+    gp1 = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=50.0, num_cells=10)
+    gp2 = S.SpringsteelGridParameters(geometry="RL", iMin=50.0, iMax=75.0, num_cells=10,
+                                      BCL={"u": S.FixedBC()}, BCR={"u": S.NaturalBC()})
+    gs = [S.createGrid(gp) for gp in (gp1, gp2)]
+    for g in gs:
+        pts = S.getGridpoints(g)
+        g.set_physical((3 * pts[:, 0] + 7)[:, None], slot=1)
+        S.spectralTransform_b(g)
+    S.PatchChain(gs).multiGridTransform()
+    pts2 = S.getGridpoints(gs[1])
+    assert np.max(np.abs(gs[1].get_physical()[:, 0, 0] - (3 * pts2[:, 0] + 7))) < 1e-8
+
+
+@pytest.mark.parametrize("use_graph,autotune", [(True, False), (False, True), (True, True)])
+def test_batch_matches_single_grid_calls(use_graph, autotune):
+    rng = np.random.default_rng(7)
+    grids, refs = [], []
+    for i in range(6):
+        nc = int(rng.integers(8, 30))
+        nv = int(rng.integers(1, 4))
+        gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=float(nc), num_cells=nc,
+                                         vars={"v%d" % k: k + 1 for k in range(nv)})
+        g = S.createGrid(gp)
+        _fill(g, seed=i)
+        S.spectralTransform_b(g)
+        S.gridTransform_b(g)
+        refs.append(g.get_physical())
+        grids.append(g)
+    batch = S.Batch(grids, autotune=autotune)
+    for _ in range(2):  # capture, then replay
+        batch.run(what=3, use_graph=use_graph)
+        batch.synchronize()
+    for g, r in zip(grids, refs):
+        assert np.array_equal(g.get_physical(), r)
+    if autotune:
+        assert all(t in (64, 128, 256) for i in range(6) for t in batch.ring_threads(i))
+
+
+def test_rlz_tiles_halo_sum_equals_patch():
+    gp = fields.config2_params(num_cells=40, nvars=2)
+    patch = S.createGrid(gp)
+    _fill(patch, seed=9)
+    S.spectralTransform_b(patch)
+    ref = patch.get_spectral()
+    ref_phys = None
+    S.gridTransform_b(patch)
+    ref_phys = patch.get_physical()
+    tiles = [S.createGrid(tp) for tp in S.calcTileSizes(gp, 8)]
+    S.zero_spectral(patch)
+    for t in tiles:
+        S.tile_physical_from_patch(patch, t, slot=1)
+        S.spectralTransform_b(t, stream=patch.stream())
+        S.sumSpectralTile_b(patch, t, stream=patch.stream())
+    got = patch.get_spectral()
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+    S.gridTransform_b(patch)
+    errs = slot_errors(patch.get_physical(), ref_phys, gp)
+    assert np.all(errs <= TOL64), errs
+    # tiles read their share of the inverse result back
+    for t in tiles:
+        S.tile_physical_from_patch(patch, t, slot=0)
+    assert np.isfinite(tiles[-1].get_physical()).all()

@@ -18,6 +18,10 @@ from springsteel_gpu import fields
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
+# SS_PREC_F64_FAST: binary64 data, double-float (48-bit) FFT/DCT arithmetic; the
+# derivative slots amplify its 2^-48 rounding (by k ≤ K for ∂λ, by the Chebyshev
+# recurrence for ∂z), so its stated bound is 2e-11.
+TOL_FAST = 2e-11
 
 
 def _rel(a, b):
@@ -72,20 +76,23 @@ def slot_errors(phys_g, phys_o, gp):
 
 def _assert_parity(spec_g, spec_o, phys_g, phys_o, gp, tol=TOL64):
     nv = spec_o.shape[1]
-    for v in range(nv):
-        e = _rel(spec_g[:, v], spec_o[:, v])
-        assert e <= tol, ("spectral", v, e)
+    espec = [_rel(spec_g[:, v], spec_o[:, v]) for v in range(nv)]
     errs = slot_errors(phys_g, phys_o, gp)
+    print("parity %s %s: spectral max %.2e, slots max %s" % (gp.geometry, gp.precision, max(espec),
+                                                              np.array2string(errs.max(axis=0), precision=2)))
+    for v in range(nv):
+        assert espec[v] <= tol, ("spectral", v, espec[v])
     bad = [(v, s + 1, errs[v, s]) for v in range(nv) for s in range(errs.shape[1]) if not errs[v, s] <= tol]
     assert not bad, bad
 
 
-def test_rl_config1_parity():
-    gp = fields.config1_params()
+@pytest.mark.parametrize("precision", ["f64", "f64_fast"])
+def test_rl_config1_parity(precision):
+    gp = fields.config1_params(precision=precision)
     pts = S.getGridpoints(S.createGrid(gp))
     u = fields.gaussian_ring_field(pts, seed=1)
     _, _, sg, so, pg, po = _run_both(gp, u[:, None])
-    _assert_parity(sg, so, pg, po, gp)
+    _assert_parity(sg, so, pg, po, gp, tol=TOL64 if precision == "f64" else TOL_FAST)
 
 
 def test_rl_gridpoints_match_oracle():
@@ -149,13 +156,14 @@ def test_rlz_parity_bcs(bcb, bct):
     _assert_parity(sg, so, pg, po, gp)
 
 
-def test_rlz_config2_shape_reduced():
+@pytest.mark.parametrize("precision", ["f64", "f64_fast"])
+def test_rlz_config2_shape_reduced(precision):
     # the configuration-2 layout (kz = 32, 5 variables, Dirichlet in z) at 40 cells
-    gp = fields.config2_params(num_cells=40)
+    gp = fields.config2_params(num_cells=40, precision=precision)
     pts = S.getGridpoints(S.createGrid(gp))
     u = fields.rlz_blob_fields(pts, 5, zmax=20000.0)
     _, _, sg, so, pg, po = _run_both(gp, u)
-    _assert_parity(sg, so, pg, po, gp)
+    _assert_parity(sg, so, pg, po, gp, tol=TOL64 if precision == "f64" else TOL_FAST)
 
 
 def test_rlz_patch_offset_and_filters():
