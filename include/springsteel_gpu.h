@@ -252,6 +252,66 @@ int32_t ss_spectral_transform_noalloc(const ss_grid *grid, const double *d_physi
 int32_t ss_grid_profile(ss_grid *grid, int32_t enable);
 int32_t ss_grid_profile_read(ss_grid *grid, double *ms, int64_t *launches);
 
+/* ---- elliptic solve on RL grids ------------------------------------------
+ * Replaces SpringsteelProblem(grid, L*u => f; backend, preconditioner) and
+ * solve / solve! (src/solver_problem.jl:311-339, :474-529; Krylov backend
+ * :99-109, :172-179, :207-222) for L = ∂rr + (1/r)∂r + (1/r²)∂λλ − k²(r) on an
+ * RL grid, whose Kron assembly the reference does not support
+ * (src/solver.jl:339-363).  Per Fourier wavenumber m the radial Galerkin
+ * system G_m x = Γ_m b_m is built from the reference's spline matrices
+ * (src/CubicBSpline.jl:1729-1816) and Γ fold (src/solver.jl:721-756), with
+ * u'(0) = 0 (m = 0), u(0) = 0 (m ≥ 1) and u(R) = 0.
+ * ss_problem_create: k2 = k²(r) at the iDim mish points (native FP64 RL grid).
+ * ss_solve: f is read from physical slot 1; u and its derivatives are written
+ * to every physical slot (gridTransform! layout); spectral holds the
+ * coefficients a.  Methods: direct banded LU, GMRES with the :diag (Jacobi)
+ * right preconditioner, flexible GMRES with the learned MLP preconditioner
+ * (z = D⁻¹(v + N(v))); its unconverged systems fall back to Jacobi GMRES, then
+ * to the direct solve (stats->fallback_systems). */
+typedef struct ss_problem ss_problem;
+typedef struct ss_mlp ss_mlp;
+enum { SS_SOLVER_DIRECT = 0, SS_SOLVER_GMRES_JACOBI = 1, SS_SOLVER_FGMRES_MLP = 2 };
+typedef struct {
+    int32_t method, systems, converged, max_iterations, fallback_systems, _pad;
+    double mean_iterations, max_rel_residual; /* ‖c − G x‖ / ‖c‖ per radial system */
+    double ms;                                /* device time of the radial solve stage */
+} ss_solve_stats;
+int32_t ss_problem_create(ss_grid *grid, const double *k2, ss_problem **out);
+int32_t ss_problem_destroy(ss_problem *problem);
+int32_t ss_problem_dims(const ss_problem *problem, int32_t *nsys, int32_t *nmax, int32_t *K, int32_t *bandwidth);
+int32_t ss_problem_operator_band(const ss_problem *problem, int32_t m, double *band, int32_t *n, int32_t *kl);
+int32_t ss_problem_set_mlp(ss_problem *problem, ss_mlp *mlp, int32_t max_wavenumber);
+int32_t ss_solve(ss_problem *problem, int32_t method, double tol, int32_t max_iter, int32_t restart,
+                 ss_solve_stats *stats, void *stream);
+int32_t ss_problem_export(const ss_problem *problem, double *rhs, double *x, double *res, int32_t *iters);
+int32_t ss_problem_collect_training(ss_problem *problem, ss_mlp *mlp, const double *points, const double *blobs,
+                                   const int32_t *offsets, int32_t nfields, int32_t max_wavenumber);
+
+/* ---- learned preconditioner network --------------------------------------
+ * No reference counterpart (the reference's preconditioners are :none and
+ * :diag).  3 dense layers 256 → 256 → 256 → 256, ReLU between, BF16 weights
+ * and activations with FP32 accumulation on the tensor cores (tcgen05); FP32
+ * master weights and Adam state.  Parameters are W[layer][out][in] and
+ * b[layer][out] as FP32 host arrays (3·256·256 and 3·256 values).  Row
+ * arrays are rows × 256 FP32.  ss_mlp_gradients takes rows a multiple of
+ * 128, the target rows and the used width per row, and returns dL/dW, dL/db
+ * of L = (1/rows) Σ_rows Σ_{i<n} (out_i − target_i)². */
+typedef struct {
+    int32_t epochs, _pad;
+    int64_t steps, rows;
+    double first_epoch_loss, last_epoch_loss, ms;
+} ss_train_stats;
+int32_t ss_mlp_create(int32_t device, uint64_t seed, ss_mlp **out);
+int32_t ss_mlp_destroy(ss_mlp *mlp);
+int32_t ss_mlp_set_params(ss_mlp *mlp, const float *W, const float *b);
+int32_t ss_mlp_get_params(const ss_mlp *mlp, float *W, float *b);
+int32_t ss_mlp_forward(ss_mlp *mlp, const float *in, float *out, int64_t rows);
+int32_t ss_mlp_gradients(ss_mlp *mlp, const float *in, const float *target, const int32_t *n, int64_t rows,
+                         float *dW, float *db, double *loss);
+int32_t ss_mlp_dataset_rows(const ss_mlp *mlp, int64_t *rows);
+int32_t ss_mlp_dataset_clear(ss_mlp *mlp);
+int32_t ss_mlp_train(ss_mlp *mlp, int32_t epochs, int32_t batch, float lr, uint64_t seed, ss_train_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -380,3 +380,46 @@ class OracleChain:
         if getattr(self, "h", None):
             lib().or_chain_destroy(self.h)
             self.h = None
+
+
+class OracleElliptic:
+    """Per-wavenumber elliptic solve on an RL oracle grid (see ss_oracle.c)."""
+
+    def __init__(self, grid, k2):
+        L = lib()
+        for name, args in (("or_elliptic_create", [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+                           ("or_elliptic_operator", [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_int32)]),
+                           ("or_elliptic_solve_spectral", [C.c_void_p, C.c_void_p]),
+                           ("or_grid_transform_coeffs", [C.c_void_p, C.c_void_p, C.c_void_p])):
+            getattr(L, name).argtypes = args
+            getattr(L, name).restype = C.c_int32
+        L.or_elliptic_destroy.argtypes = [C.c_void_p]
+        L.or_elliptic_destroy.restype = None
+        self.grid = grid
+        self._k2 = _f64(k2)
+        h = C.c_void_p()
+        _check(L.or_elliptic_create(grid.h.value, _ptr(self._k2), C.byref(h)))
+        self.h = h
+
+    def operator(self, m):
+        b = self.grid.dims["b_iDim"]
+        G = np.zeros(b * b)
+        n = C.c_int32()
+        _check(lib().or_elliptic_operator(self.h, int(m), _ptr(G), C.byref(n)))
+        return G[: n.value * n.value].reshape(n.value, n.value, order="F")
+
+    def solve(self, f_phys):
+        """f at the gridpoints (n_physical, nvars) → physical (n_physical, nvars, 5) of u."""
+        g = self.grid
+        ph = np.zeros(g.physical_shape, order="F")
+        ph[:, :, 0] = np.asarray(f_phys).reshape(ph.shape[0], -1)
+        spec = np.asfortranarray(g.spectral_transform(ph))
+        _check(lib().or_elliptic_solve_spectral(self.h, _ptr(spec)))
+        out = np.zeros(g.physical_shape, order="F")
+        _check(lib().or_grid_transform_coeffs(g.h, _ptr(spec), _ptr(out)))
+        return out, spec
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_elliptic_destroy(self.h)
+            self.h = None

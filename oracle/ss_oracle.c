@@ -1007,6 +1007,7 @@ struct or_grid {
     int has_ahat;
     double **fw, **cw;  /* filter weights per variable (NULL: none) */
     double *rmish;
+    int skip_sa;        /* inverse driver takes spline coefficients a directly */
 };
 
 static int ring_L(const or_grid *g, int r) { return 4 + 4 * (r + g->pOL); } /* _cyl_ring_dims, factory.jl:153-156 */
@@ -1307,7 +1308,8 @@ int32_t or_grid_transform(or_grid *g, const double *spec, double *phys) {
 #pragma omp for schedule(static)
             for (long q = 0; q < (long)bk * slots; q++) {
                 const double *ah = (g->has_ahat && g->ahat[v]) ? g->ahat[v] + (size_t)q * b : NULL;
-                spline_sa(s, sp + (size_t)q * b, ah, a, t, t + b, t + 2 * b);
+                if (g->skip_sa) memcpy(a, sp + (size_t)q * b, sizeof(double) * (size_t)b);
+                else spline_sa(s, sp + (size_t)q * b, ah, a, t, t + b, t + 2 * b);
                 for (int d = 0; d < 3; d++)
                     for (int r = 0; r < iDim; r++)
                         prof[(size_t)d * psz + (size_t)q * iDim + r] = si_point(s, a, s->mish[r], d);
@@ -1524,4 +1526,157 @@ int32_t or_multi_grid_transform(or_chain *c, const double **spectral, double **p
             if (c->layer_of[c->ifs[k].primary] == L) chain_update_interface(c, &c->ifs[k], spectral[c->ifs[k].primary]);
     }
     return SS_OK;
+}
+
+/* ======================================================================
+ * Elliptic per-wavenumber solve on RL grids
+ * (∂rr + (1/r)∂r + (1/r²)∂λλ − k²(r)) u = f
+ *
+ * The reference has no RL elliptic solve (its Kron assembly uses ring 1 only,
+ * src/solver.jl:354-359).  Per Fourier wavenumber m the radial problem
+ *   u_m'' + u_m'/r − (m²/r² + k²(r)) u_m = f_m
+ * is discretised with the reference's own pieces: the B-spline values and
+ * derivatives at the mish points (spline_basis_matrix / _1st_ / _2nd_,
+ * src/CubicBSpline.jl:1729-1816), tested with the SB projection weights
+ * (_build_sb_matrix, :1000-1030, the same Galerkin form as the P+Q system),
+ * and the Γ fold of the boundary conditions (src/solver.jl:721-756):
+ *   G_m = Γ_m [Σ_i w_{·,i} (Lφ_j)(r_i)] Γ_mᵀ,  G_m x = Γ_m b_m,  a = Γ_mᵀ x
+ * where b_m is the spectral B-vector of f (spectralTransform!).  Axis
+ * regularity: u_0'(0) = 0 (R1T1), u_m(0) = 0 for m ≥ 1 (R1T0); u(R) = 0
+ * (R1T0) at the outer edge.  Direct solve: dense LU with partial pivoting.
+ * ====================================================================== */
+
+struct or_elliptic {
+    or_grid *g;
+    or_spline *s0, *s1;   /* m = 0 and m ≥ 1 templates (Γ differs) */
+    double *k2;           /* k²(r) at the mish points */
+};
+typedef struct or_elliptic or_elliptic;
+
+int32_t or_elliptic_create(or_grid *g, const double *k2, or_elliptic **out) {
+    *out = NULL;
+    if (g->geom != SS_GEOM_RL) { set_err("the elliptic solve needs an RL grid"); return SS_BAD_ARG; }
+    const or_spline *t = g->spl[0];
+    ss_spline_bc r1t0 = {SS_SBC_RANK1, 0, -4.0, -1.0}, r1t1 = {SS_SBC_RANK1, 0, 0.0, 1.0};
+    or_elliptic *e = (or_elliptic *)calloc(1, sizeof *e);
+    e->g = g;
+    int st = or_spline_create(t->xmin, t->xmax, t->nc, t->mubar, t->quad, t->l_q, &r1t1, &r1t0, &e->s0);
+    if (st == SS_OK) st = or_spline_create(t->xmin, t->xmax, t->nc, t->mubar, t->quad, t->l_q, &r1t0, &r1t0, &e->s1);
+    if (st) { or_spline_destroy(e->s0); free(e); return st; }
+    e->k2 = (double *)malloc(sizeof(double) * (size_t)t->mishDim);
+    memcpy(e->k2, k2, sizeof(double) * (size_t)t->mishDim);
+    *out = e;
+    return SS_OK;
+}
+void or_elliptic_destroy(or_elliptic *e) {
+    if (!e) return;
+    or_spline_destroy(e->s0); or_spline_destroy(e->s1); free(e->k2); free(e);
+}
+
+/* dense G_m (Min × Min, column-major) */
+int32_t or_elliptic_operator(const or_elliptic *e, int32_t m, double *G, int32_t *n_out) {
+    const or_spline *s = m == 0 ? e->s0 : e->s1;
+    int b = s->bDim, n = s->Min;
+    double *Gf = (double *)calloc((size_t)b * b, sizeof(double));
+    for (int mc = 0; mc < s->nc; mc++)
+        for (int mu = 0; mu < s->mubar; mu++) {
+            int i = mu + s->mubar * mc;
+            double x = s->mish[i];
+            double m2 = (double)m * (double)m;
+            double c1 = 1.0 / x, c0 = -(m2 / (x * x) + e->k2[i]);
+            long xm = (long)ceil((x - s->xmin - (2.0 * s->DX)) * s->DXrecip);
+            for (long jj = xm; jj <= xm + 3; jj++) {
+                if (jj < -1 || jj > s->nc + 1) continue;
+                double Lphi = basis(s, (int)jj, x, 2) + c1 * basis(s, (int)jj, x, 1) + c0 * basis(s, (int)jj, x, 0);
+                for (int ti = (mc - 1 > -1 ? mc - 1 : -1); ti <= mc + 2; ti++) {
+                    if (ti < -1 || ti > s->nc + 1) continue;
+                    double w = s->DX * s->qwts[mu] * basis(s, ti, x, 0);
+                    Gf[(ti + 1) + (size_t)(jj + 1) * b] += w * Lphi;
+                }
+            }
+        }
+    /* G = Γ Gf Γᵀ */
+    for (int c = 1; c <= n; c++)
+        for (int r = 1; r <= n; r++) {
+            double acc = 0.0;
+            for (int a = 1; a <= b; a++) {
+                double ga = gamma_at(s, r, a);
+                if (ga == 0.0) continue;
+                for (int bb = 1; bb <= b; bb++) {
+                    double gb = gamma_at(s, c, bb);
+                    if (gb == 0.0) continue;
+                    acc += ga * Gf[(a - 1) + (size_t)(bb - 1) * b] * gb;
+                }
+            }
+            G[(r - 1) + (size_t)(c - 1) * n] = acc;
+        }
+    free(Gf);
+    *n_out = n;
+    return SS_OK;
+}
+
+static int dense_lu_solve(double *A, int n, double *x) {
+    /* in place LU with partial pivoting, then the solve of A x = x */
+    for (int k = 0; k < n; k++) {
+        int p = k;
+        double mx = fabs(A[k + (size_t)k * n]);
+        for (int i = k + 1; i < n; i++)
+            if (fabs(A[i + (size_t)k * n]) > mx) { mx = fabs(A[i + (size_t)k * n]); p = i; }
+        if (mx == 0.0) { set_err("singular operator"); return SS_NOT_SPD; }
+        if (p != k) {
+            for (int j = 0; j < n; j++) { double t = A[k + (size_t)j * n]; A[k + (size_t)j * n] = A[p + (size_t)j * n]; A[p + (size_t)j * n] = t; }
+            double t = x[k]; x[k] = x[p]; x[p] = t;
+        }
+        for (int i = k + 1; i < n; i++) {
+            double l = A[i + (size_t)k * n] / A[k + (size_t)k * n];
+            A[i + (size_t)k * n] = l;
+            for (int j = k + 1; j < n; j++) A[i + (size_t)j * n] -= l * A[k + (size_t)j * n];
+            x[i] -= l * x[k];
+        }
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        double s = x[i];
+        for (int j = i + 1; j < n; j++) s -= A[i + (size_t)j * n] * x[j];
+        x[i] = s / A[i + (size_t)i * n];
+    }
+    return SS_OK;
+}
+
+/* spectral B-vectors of f (spectralTransform!) → coefficients a per slot; the
+ * caller's spectral array is overwritten with a (the input of the SI stage). */
+int32_t or_elliptic_solve_spectral(const or_elliptic *e, double *spec) {
+    or_grid *g = e->g;
+    int b = g->b;
+    long slots = 1 + 2L * g->K;
+    int nmax = e->s0->Min > e->s1->Min ? e->s0->Min : e->s1->Min;
+    double *G = (double *)malloc(sizeof(double) * (size_t)nmax * nmax);
+    double *G0 = (double *)malloc(sizeof(double) * (size_t)nmax * nmax);
+    double *x = (double *)malloc(sizeof(double) * (size_t)b);
+    int lastm = -1, n = 0;
+    for (int v = 0; v < g->nvars; v++) {
+        double *sp = spec + (size_t)g->nspec * v;
+        for (long q = 0; q < slots; q++) {
+            int m = (int)((q + 1) / 2);
+            const or_spline *s = m == 0 ? e->s0 : e->s1;
+            if (m != lastm) { or_elliptic_operator(e, m, G0, &n); lastm = m; }
+            memcpy(G, G0, sizeof(double) * (size_t)n * n);
+            gamma_apply(s, sp + (size_t)q * b, x);
+            int st = dense_lu_solve(G, n, x);
+            if (st) { free(G); free(G0); free(x); return st; }
+            gamma_adjoint(s, x, sp + (size_t)q * b);
+        }
+        lastm = -1;
+    }
+    free(G); free(G0); free(x);
+    return SS_OK;
+}
+
+/* a-coefficients in spectral layout → physical (the SI + ring stages of gridTransform!) */
+int32_t or_grid_transform_coeffs(or_grid *g, const double *acoef, double *phys) {
+    /* SA with the identity: run the inverse driver on a grid whose SA is skipped */
+    int saved = g->skip_sa;
+    g->skip_sa = 1;
+    int st = or_grid_transform(g, acoef, phys);
+    g->skip_sa = saved;
+    return st;
 }

@@ -50,6 +50,15 @@ void or_chain_destroy(or_chain *c);
 /* spectral[i] / physical[i]: arrays of patch i (layouts as or_grid_transform) */
 int32_t or_multi_grid_transform(or_chain *c, const double **spectral, double **physical);
 
+/* Elliptic per-wavenumber solve on RL grids (no reference counterpart: built
+ * from the reference's B-spline pieces; see ss_oracle.c) */
+typedef struct or_elliptic or_elliptic;
+int32_t or_elliptic_create(or_grid *g, const double *k2, or_elliptic **out);
+void or_elliptic_destroy(or_elliptic *e);
+int32_t or_elliptic_operator(const or_elliptic *e, int32_t m, double *G, int32_t *n_out);
+int32_t or_elliptic_solve_spectral(const or_elliptic *e, double *spec);
+int32_t or_grid_transform_coeffs(or_grid *g, const double *acoef, double *phys);
+
 /* ---- 1-D primitives for the known-answer tests -------------------------- */
 typedef struct or_spline or_spline;
 int32_t or_spline_create(double xmin, double xmax, int32_t num_cells, int32_t mubar,

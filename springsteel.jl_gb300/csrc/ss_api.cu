@@ -360,14 +360,14 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
 }
 
 template <typename P, typename T>
-static int32_t run_inverse(ss_grid *g, cudaStream_t st) {
+static int32_t run_inverse(ss_grid *g, cudaStream_t st, int coeffs = 0) {
     const ss_dims &d = g->d;
     const int nv = (int)d.nvars, bk = (int)d.b_kDim;
     SaLaunch A{};
     A.spec = g->spec; A.G = g->G; A.spl = g->d_spl; A.fofs = g->d_fofs; A.ahat = g->d_ahat;
     A.frows = g->frows; A.nspec = d.n_spectral; A.nblocks = d.n_blocks;
     A.iDim = (int)d.iDim; A.b = (int)d.b_iDim; A.ld = (A.b % 2) ? A.b : A.b + 1;
-    A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = bk; A.nitems = g->nitems;
+    A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = bk; A.nitems = g->nitems; A.coeffs = coeffs;
     int nmax = 0;
     for (auto &sh : g->spl_host) nmax = std::max(nmax, sh.Min);
     const size_t ssz = (sizeof(T) == 4) ? 4 : 8;  // solve type: float (FP32 mode) or double
@@ -419,6 +419,11 @@ int32_t grid_inverse(ss_grid *g, cudaStream_t s) {
     if (g->tl == TL_DF64) return run_inverse<double, df64>(g, s);
     if (g->tl == TL_F64) return run_inverse<double, double>(g, s);
     return run_inverse<float, float>(g, s);
+}
+int32_t grid_inverse_coeffs(ss_grid *g, cudaStream_t s) {
+    if (g->tl == TL_DF64) return run_inverse<double, df64>(g, s, 1);
+    if (g->tl == TL_F64) return run_inverse<double, double>(g, s, 1);
+    return run_inverse<float, float>(g, s, 1);
 }
 }  // namespace ss
 

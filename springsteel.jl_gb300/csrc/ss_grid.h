@@ -92,4 +92,6 @@ namespace ss {
 // per-grid launch entry points shared by the single-grid, batch and chain paths
 int32_t grid_forward(ss_grid *g, cudaStream_t st);
 int32_t grid_inverse(ss_grid *g, cudaStream_t st);
+// SI + ring (+ column) stages only: the spectral array holds spline coefficients a
+int32_t grid_inverse_coeffs(ss_grid *g, cudaStream_t st);
 }  // namespace ss

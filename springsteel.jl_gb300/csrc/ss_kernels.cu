@@ -25,6 +25,7 @@
 
 #include "ss_fft.cuh"
 #include "ss_kernels.h"
+#include "ss_spline_dev.cuh"
 
 namespace ss {
 
@@ -252,53 +253,6 @@ __global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch S) {
 //               correction solve, x += dx;
 // then the 4-tap SI/SIx/SIxx at the mish points in the compute type.
 // ====================================================================
-template <typename S>
-__device__ __forceinline__ void gamma_fold(const SplineDev &sp, S *x, int Md, int n) {
-    const int rL = sp.rankL;
-    const S b0 = x[0], b1 = x[1], bM1 = x[Md - 1], bM2 = x[Md - 2];
-    for (int i = 0; i < n; i++) x[i] = x[i + rL];
-    if (sp.lk == BC_A1) { x[0] += (S)sp.aL * b0; x[1] += (S)sp.bL * b0; }
-    else if (sp.lk == BC_A2) { x[0] += (S)sp.aL * b0 + (S)sp.bL * b1; }
-    if (sp.rk == BC_A1) { x[n - 1] += (S)sp.aR * bM1; x[n - 2] += (S)sp.bR * bM1; }
-    else if (sp.rk == BC_A2) { x[n - 1] += (S)sp.aR * bM1 + (S)sp.bR * bM2; }
-}
-template <typename S>
-__device__ __forceinline__ void gamma_unfold(const SplineDev &sp, S *x, int Md, int n) {
-    const int rL = sp.rankL;
-    const S s0v = x[0], s1v = x[1], sM1 = x[n - 1], sM2 = x[n - 2];
-    for (int i = n - 1; i >= 0; i--) x[i + rL] = x[i];
-    for (int j = 0; j < rL; j++) x[j] = S(0);
-    for (int j = Md - sp.rankR; j < Md; j++) x[j] = S(0);
-    if (sp.lk == BC_A1) x[0] = (S)sp.aL * s0v + (S)sp.bL * s1v;
-    else if (sp.lk == BC_A2) { x[0] = (S)sp.aL * s0v; x[1] = (S)sp.bL * s0v; }
-    if (sp.rk == BC_A1) x[Md - 1] = (S)sp.aR * sM1 + (S)sp.bR * sM2;
-    else if (sp.rk == BC_A2) { x[Md - 2] = (S)sp.bR * sM1; x[Md - 1] = (S)sp.aR * sM1; }
-}
-// forward L y = v, backward Lᵀ x = y in place (src/banded_cholesky.jl:202-231)
-template <typename S>
-__device__ __forceinline__ void band_solve(const S *Ls, const S *Di, S *x, int n) {
-    S y1 = S(0), y2 = S(0), y3 = S(0);
-    for (int i = 0; i < n; i++) {
-        S acc = x[i];
-        if (i >= 3) acc -= Ls[(i - 3) * 4 + 3] * y3;
-        if (i >= 2) acc -= Ls[(i - 2) * 4 + 2] * y2;
-        if (i >= 1) acc -= Ls[(i - 1) * 4 + 1] * y1;
-        const S yi = acc * Di[i];
-        x[i] = yi;
-        y3 = y2; y2 = y1; y1 = yi;
-    }
-    S x1 = S(0), x2 = S(0), x3 = S(0);
-    for (int i = n - 1; i >= 0; i--) {
-        S acc = x[i];
-        if (i + 1 < n) acc -= Ls[i * 4 + 1] * x1;
-        if (i + 2 < n) acc -= Ls[i * 4 + 2] * x2;
-        if (i + 3 < n) acc -= Ls[i * 4 + 3] * x3;
-        const S xi = acc * Di[i];
-        x[i] = xi;
-        x3 = x2; x2 = x1; x1 = xi;
-    }
-}
-
 template <typename P, typename T>
 __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -322,7 +276,13 @@ __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
     for (int e = threadIdx.x; e < n; e += blockDim.x) Di[e] = kF32 ? (S)sp.dinvf[e] : (S)sp.dinv[e];
     __syncthreads();
 
-    if (threadIdx.x < nsl) {
+    if (threadIdx.x < nsl && A.coeffs) {
+        if constexpr (!kSameX) {
+            S *x = X + threadIdx.x * ld;
+            T *xt = XT + threadIdx.x * ld;
+            for (int i = 0; i < b; i++) xt[i] = to_compute<T>((double)x[i]);
+        }
+    } else if (threadIdx.x < nsl) {
         S *x = X + threadIdx.x * ld;
         const int Md = b;
         const double *ah = (sp.r3x && A.ahat)

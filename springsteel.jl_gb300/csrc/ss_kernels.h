@@ -43,6 +43,7 @@ struct SaLaunch {
     const double *ahat;        // [v][block][b] or null
     int64_t frows, nspec, nblocks;
     int iDim, b, ld, pOL, nslots_z, bk, nitems;
+    int coeffs;                // 1: spectral holds spline coefficients a (skip SAtransform!)
 };
 
 struct ChebLaunch {

@@ -690,3 +690,7 @@ def tile_physical_to_patch(patch, tile, slot=0, stream=None):
 
 def zero_spectral(grid, stream=None):
     _check(load_library().ss_grid_zero_spectral(grid.handle, stream))
+
+
+# ----------------------------------------------------------------- elliptic solve
+from .solver import MLPPreconditioner, SpringsteelProblem, solve  # noqa: E402

@@ -154,7 +154,29 @@ EXPORTED = [
     "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads",
     "ss_chain_create", "ss_chain_destroy", "ss_multi_grid_transform",
     "ss_tile_sum_spectral", "ss_tile_copy_physical", "ss_grid_zero_spectral",
+    "ss_problem_create", "ss_problem_destroy", "ss_problem_dims", "ss_problem_operator_band",
+    "ss_problem_set_mlp", "ss_solve", "ss_problem_export", "ss_problem_collect_training",
+    "ss_mlp_create", "ss_mlp_destroy", "ss_mlp_set_params", "ss_mlp_get_params", "ss_mlp_forward",
+    "ss_mlp_gradients", "ss_mlp_dataset_rows", "ss_mlp_dataset_clear", "ss_mlp_train",
 ]
+
+SS_SOLVER_DIRECT = 0
+SS_SOLVER_GMRES_JACOBI = 1
+SS_SOLVER_FGMRES_MLP = 2
+MLP_WIDTH = 256
+MLP_LAYERS = 3
+
+
+class ss_solve_stats(C.Structure):
+    _fields_ = [("method", C.c_int32), ("systems", C.c_int32), ("converged", C.c_int32),
+                ("max_iterations", C.c_int32), ("fallback_systems", C.c_int32), ("_pad", C.c_int32),
+                ("mean_iterations", C.c_double), ("max_rel_residual", C.c_double), ("ms", C.c_double)]
+
+
+class ss_train_stats(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("_pad", C.c_int32), ("steps", C.c_int64), ("rows", C.c_int64),
+                ("first_epoch_loss", C.c_double), ("last_epoch_loss", C.c_double), ("ms", C.c_double)]
+
 
 STAGES = ["cheb_forward", "ring_forward", "sb_project", "sa_si", "ring_inverse", "cheb_inverse"]
 
@@ -196,6 +218,23 @@ def bind(lib):
         "ss_tile_sum_spectral": ([vp, vp, i32, vp], i32),
         "ss_tile_copy_physical": ([vp, vp, i32, i32, vp], i32),
         "ss_grid_zero_spectral": ([vp, vp], i32),
+        "ss_problem_create": ([vp, vp, C.POINTER(vp)], i32),
+        "ss_problem_destroy": ([vp], i32),
+        "ss_problem_dims": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
+        "ss_problem_operator_band": ([vp, i32, vp, C.POINTER(i32), C.POINTER(i32)], i32),
+        "ss_problem_set_mlp": ([vp, vp, i32], i32),
+        "ss_solve": ([vp, i32, C.c_double, i32, i32, C.POINTER(ss_solve_stats), vp], i32),
+        "ss_problem_export": ([vp, vp, vp, vp, vp], i32),
+        "ss_problem_collect_training": ([vp, vp, vp, vp, vp, i32, i32], i32),
+        "ss_mlp_create": ([i32, C.c_uint64, C.POINTER(vp)], i32),
+        "ss_mlp_destroy": ([vp], i32),
+        "ss_mlp_set_params": ([vp, vp, vp], i32),
+        "ss_mlp_get_params": ([vp, vp, vp], i32),
+        "ss_mlp_forward": ([vp, vp, vp, C.c_int64], i32),
+        "ss_mlp_gradients": ([vp, vp, vp, vp, C.c_int64, vp, vp, C.POINTER(C.c_double)], i32),
+        "ss_mlp_dataset_rows": ([vp, C.POINTER(C.c_int64)], i32),
+        "ss_mlp_dataset_clear": ([vp], i32),
+        "ss_mlp_train": ([vp, i32, i32, C.c_float, C.c_uint64, C.POINTER(ss_train_stats)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

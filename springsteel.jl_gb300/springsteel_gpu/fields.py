@@ -80,3 +80,61 @@ def rlz_blob_fields(points, nvars, base_seed=2, zmax=20000.0, noise=0.0):
     for v in range(nvars):
         out[:, v] = blob_sum(points, seed=base_seed * 1000 + v, zmax=zmax, noise=noise)
     return out
+
+
+# ----------------------------------------------------------------- elliptic solve
+def config5_params(num_cells=200, rmax=100.0):
+    """RL, 200 cells on r ∈ [0, 100], rings of 4+4r, one variable, native FP64."""
+    return SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=float(rmax), num_cells=num_cells,
+                                     BCL={"default": NaturalBC()}, BCR={"default": NaturalBC()},
+                                     vars={"u": 1}, precision="f64")
+
+
+def k2_profile(r, seed, rmax=None):
+    """k²(r) = Σ_{i<3} a_i exp(−(r − c_i)²/s_i²) > 0: a ~ U[0.002, 0.02], c ~ U[0, rmax],
+    s ~ U[rmax/10, rmax/3]."""
+    r = np.asarray(r, np.float64)
+    rmax = float(r.max()) if rmax is None else float(rmax)
+    rng = np.random.default_rng(seed)
+    out = np.zeros_like(r)
+    for _ in range(3):
+        a = rng.uniform(0.002, 0.02)
+        c = rng.uniform(0.0, rmax)
+        s = rng.uniform(rmax / 10.0, rmax / 3.0)
+        out += a * np.exp(-((r - c) / s) ** 2)
+    return out
+
+
+def elliptic_blobs(seed, rmax=100.0, nmin=1, nmax=12, wmin=5.0, wmax=30.0):
+    """Forcing of one elliptic sample: 1–12 blobs (xc, yc, w, A), centres uniform in the
+    disc, widths U[wmin, wmax], amplitudes N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    nb = int(rng.integers(nmin, nmax + 1))
+    out = np.empty((nb, 4))
+    for i in range(nb):
+        rc = rmax * np.sqrt(rng.uniform())
+        tc = rng.uniform(0.0, 2 * np.pi)
+        out[i] = (rc * np.cos(tc), rc * np.sin(tc), rng.uniform(wmin, wmax), rng.normal())
+    return out
+
+
+def blob_field(points, blobs):
+    """Σ A exp(−[(x − xc)² + (y − yc)²]/w²) at (r, λ) points."""
+    r, lam = points[:, 0], points[:, 1]
+    x, y = r * np.cos(lam), r * np.sin(lam)
+    out = np.zeros(r.shape)
+    for xc, yc, w, A in np.asarray(blobs).reshape(-1, 4):
+        out += A * np.exp(-((x - xc) ** 2 + (y - yc) ** 2) / (w * w))
+    return out
+
+
+def radial_mish(gp):
+    """The iDim radial Gauss points x = iMin + (mc + q_μ) DX (src/CubicBSpline.jl:887-897)."""
+    nc, mb = gp.num_cells, gp.mubar
+    DX = (gp.iMax - gp.iMin) / nc
+    if gp.quadrature == "gauss":
+        nodes = np.polynomial.legendre.leggauss(mb)[0] if mb != 3 else np.array([-np.sqrt(0.6), 0.0, np.sqrt(0.6)])
+        q = (nodes + 1.0) / 2.0
+    else:
+        q = (2 * np.arange(1, mb + 1) - 1) / (2 * mb)
+    return np.array([gp.iMin + mc * DX + q[mu] * DX for mc in range(nc) for mu in range(mb)])

@@ -41,6 +41,32 @@ def test_struct_layout_matches_header():
     assert C.sizeof(abi.ss_dims) == 12 * 8
 
 
+def test_solver_struct_layout_matches_header():
+    assert C.sizeof(abi.ss_solve_stats) == 6 * 4 + 3 * 8
+    assert C.sizeof(abi.ss_train_stats) == 2 * 4 + 2 * 8 + 3 * 8
+
+
+def test_solver_null_arguments_rejected():
+    lib = S.load_library()
+    assert lib.ss_problem_create(None, None, None) == abi.SS_BAD_ARG
+    assert lib.ss_solve(None, 0, 1e-10, 10, 10, None, None) == abi.SS_BAD_ARG
+    assert lib.ss_mlp_create(0, 0, None) == abi.SS_BAD_ARG
+    assert lib.ss_mlp_forward(None, None, None, 0) == abi.SS_BAD_ARG
+    assert lib.ss_mlp_train(None, 1, 128, 1e-3, 0, None) == abi.SS_BAD_ARG
+    assert lib.ss_problem_destroy(None) == abi.SS_OK
+    assert lib.ss_mlp_destroy(None) == abi.SS_OK
+
+
+def test_mlp_without_gpu_fails_loudly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(S.SpringsteelError) as e:
+        S.MLPPreconditioner(seed=0)
+    assert e.value.status == abi.SS_NO_DEVICE
+
+
 def test_version_and_error_string():
     lib = S.load_library()
     assert lib.ss_version() == 1

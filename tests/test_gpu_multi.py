@@ -61,20 +61,22 @@ def test_two_patch_chain_linear_exactness():
 @pytest.mark.parametrize("use_graph,autotune", [(True, False), (False, True), (True, True)])
 def test_batch_matches_single_grid_calls(use_graph, autotune):
     rng = np.random.default_rng(7)
-    grids, refs = [], []
+    grids, refs, inputs = [], [], []
     for i in range(6):
         nc = int(rng.integers(8, 30))
         nv = int(rng.integers(1, 4))
         gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=float(nc), num_cells=nc,
                                          vars={"v%d" % k: k + 1 for k in range(nv)})
         g = S.createGrid(gp)
-        _fill(g, seed=i)
+        inputs.append(_fill(g, seed=i))
         S.spectralTransform_b(g)
         S.gridTransform_b(g)
         refs.append(g.get_physical())
         grids.append(g)
     batch = S.Batch(grids, autotune=autotune)
-    for _ in range(2):  # capture, then replay
+    for _ in range(2):  # capture, then replay; gridTransform! overwrites the value slot
+        for g, u in zip(grids, inputs):
+            g.set_physical(u, slot=1)
         batch.run(what=3, use_graph=use_graph)
         batch.synchronize()
     for g, r in zip(grids, refs):
@@ -83,27 +85,59 @@ def test_batch_matches_single_grid_calls(use_graph, autotune):
         assert all(t in (64, 128, 256) for i in range(6) for t in batch.ring_threads(i))
 
 
-def test_rlz_tiles_halo_sum_equals_patch():
+def _sum_spectral_tile(patch_spec, tile_spec, pp, tp):
+    """sumSpectralTile! for RLZ (src/tiling.jl:1101-1136) on host arrays."""
+    siL = tp.spectralIndexL
+    bp, bt, bk = pp.b_iDim, tp.b_iDim, tp.b_kDim
+    kp, kt = pp.iDim + pp.patchOffsetL, tp.iDim + tp.patchOffsetL
+    sp, st = bp * (1 + 2 * kp), bt * (1 + 2 * kt)
+    for zb in range(bk):
+        for blk in range(1 + 2 * kt):
+            p0 = zb * sp + blk * bp + siL - 1
+            t0 = zb * st + blk * bt
+            patch_spec[p0:p0 + bt, :] += tile_spec[t0:t0 + bt, :]
+
+
+def test_rlz_tiles_halo_sum_matches_oracle():
     gp = fields.config2_params(num_cells=40, nvars=2)
     patch = S.createGrid(gp)
-    _fill(patch, seed=9)
+    u = _fill(patch, seed=9)
     S.spectralTransform_b(patch)
-    ref = patch.get_spectral()
-    ref_phys = None
-    S.gridTransform_b(patch)
-    ref_phys = patch.get_physical()
-    tiles = [S.createGrid(tp) for tp in S.calcTileSizes(gp, 8)]
+    b_patch = patch.get_spectral()  # B-vectors: quadrature sums, so tile halos add up to them
+    tps = S.calcTileSizes(gp, 8)
+    tiles = [S.createGrid(tp) for tp in tps]
+    assert sum(tp.num_cells for tp in tps) == gp.num_cells
     S.zero_spectral(patch)
     for t in tiles:
         S.tile_physical_from_patch(patch, t, slot=1)
         S.spectralTransform_b(t, stream=patch.stream())
         S.sumSpectralTile_b(patch, t, stream=patch.stream())
+    patch.synchronize()
     got = patch.get_spectral()
-    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+    # oracle: each tile's own spectralTransform! on its rows of the field, summed by the reference's layout
+    ref = np.zeros_like(b_patch)
+    row0 = 0
+    tile_specs = []
+    for tp in tps:
+        o = O.OracleGrid(tp.to_abi())
+        n = o.physical_shape[0]
+        ph = np.zeros(o.physical_shape, order="F")
+        ph[:, :, 0] = u[row0:row0 + n]
+        row0 += n
+        tile_specs.append(o.spectral_transform(ph))
+        _sum_spectral_tile(ref, tile_specs[-1], gp, tp)
+    assert row0 == u.shape[0]
+    scale = np.max(np.abs(ref))
+    assert np.max(np.abs(got - ref)) <= TOL64 * scale
+    assert np.max(np.abs(got - b_patch)) <= TOL64 * scale
+    # the halo-summed spectral array evaluates through the patch like any other
     S.gridTransform_b(patch)
-    errs = slot_errors(patch.get_physical(), ref_phys, gp)
+    oref = O.OracleGrid(gp.to_abi()).grid_transform(ref)
+    errs = slot_errors(patch.get_physical(), oref, gp)
     assert np.all(errs <= TOL64), errs
-    # tiles read their share of the inverse result back
-    for t in tiles:
-        S.tile_physical_from_patch(patch, t, slot=0)
-    assert np.isfinite(tiles[-1].get_physical()).all()
+    # setSpectralTile! zeroes the patch, then writes one tile's blocks
+    S.setSpectralTile_b(patch, tiles[0], stream=patch.stream())
+    patch.synchronize()
+    one = np.zeros_like(ref)
+    _sum_spectral_tile(one, tile_specs[0], gp, tps[0])
+    assert np.max(np.abs(patch.get_spectral() - one)) <= TOL64 * np.max(np.abs(one))
