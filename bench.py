@@ -46,7 +46,104 @@ WORKLOADS = {
     # small case for profiling captures (same kernels, a few hundred MB)
     "rlz100-f64": dict(num_cells=100, kDim=32, nvars=2, precision="f64"),
     "rlz200-f32": dict(num_cells=200, kDim=64, nvars=2, precision="f32"),
+    # learned-preconditioner elliptic solve on the 200-cell RL grid (separate JSON line)
+    "elliptic-rl200": dict(num_cells=200, rmax=100.0, train_fields=20000, train_random=20000, eval_seeds=1000,
+                           k2_seed=5, restart=30, tol=1e-10),
 }
+
+
+def run_elliptic(args):
+    """ms per elliptic solve to ‖c − Gx‖/‖c‖ ≤ 1e-10 on every radial system, for the direct
+    banded LU, Jacobi-preconditioned GMRES and flexible GMRES with the learned
+    preconditioner.  The network is trained first (untimed) on direct solutions of
+    `train_fields` forcing fields and `train_random` sets of random right-hand sides;
+    the held-out forcing seeds start at 10⁶.  Per solve and method: upload f from
+    pinned host memory, ss_solve (transform, radial solves, inverse transform),
+    download u (all 5 slots); device time of the radial solve stage from the
+    library's events, wall time around the whole call."""
+    import torch
+
+    import springsteel_gpu as S
+    from springsteel_gpu import abi, fields
+
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    w = WORKLOADS["elliptic-rl200"]
+    n_eval = min(w["eval_seeds"], max(args.steps, 1) * 100) if args.steps < 10 else w["eval_seeds"]
+    gp = fields.config5_params(num_cells=w["num_cells"], rmax=w["rmax"])
+    grid = S.createGrid(gp)
+    k2 = fields.k2_profile(fields.radial_mish(gp), seed=w["k2_seed"], rmax=w["rmax"])
+    prob = S.SpringsteelProblem(grid, k2, tol=w["tol"], restart=w["restart"], maxiter=20000)
+    pts = S.getGridpoints(grid)
+    net = S.MLPPreconditioner(seed=1)
+    t0 = time.perf_counter()
+    for i in range(0, w["train_fields"], 1000):
+        blobs = [fields.elliptic_blobs(s, rmax=w["rmax"]) for s in range(i, min(i + 1000, w["train_fields"]))]
+        prob.collect_training(net, blobs, points=pts)
+    for s in range(w["train_random"]):
+        prob.collect_random(net, 1, seed=s, smooth=s % 5)
+    collect_s = time.perf_counter() - t0
+    train = []
+    for ep, lr in ((2, 1e-3), (2, 3e-4), (2, 1e-4)):
+        train.append(net.train(epochs=ep, batch=8192, lr=lr, seed=ep))
+    prob.attach(net)
+    n = grid.dims["n_physical"]
+    h_f = torch.empty(n, dtype=torch.float64).pin_memory()
+    h_u = torch.empty(n * 5, dtype=torch.float64).pin_memory()
+    lib = S.load_library()
+
+    def one(method):
+        grid.synchronize()
+        t = time.perf_counter()
+        S._check(lib.ss_upload_physical(grid.handle, C.c_void_p(h_f.data_ptr()), abi.SS_DTYPE_F64, 1, None))
+        st = S.solve(prob, method=method)
+        S._check(lib.ss_download_physical(grid.handle, C.c_void_p(h_u.data_ptr()), abi.SS_DTYPE_F64, 0, None))
+        st["wall_ms"] = (time.perf_counter() - t) * 1e3
+        return st
+
+    def forcing(seed):
+        h_f.numpy()[:] = fields.blob_field(pts, fields.elliptic_blobs(seed, rmax=w["rmax"]))
+
+    methods = {"direct": "direct", "jacobi_gmres": "diag", "learned_fgmres": "mlp"}
+    for s in range(max(args.warmup, 3)):
+        forcing(10 ** 6 - 1 - s)
+        for m in methods.values():
+            one(m)
+    res, per = {}, {k: [] for k in methods}
+    with ClockSampler(local) as clk:
+        for s in range(n_eval):
+            forcing(10 ** 6 + s)  # host-side field synthesis, outside every timed call
+            for name, m in methods.items():
+                per[name].append(one(m))
+        for name in methods:
+            sts = per[name]
+            res[name] = {
+                "device_ms": statistics.mean(s["ms"] for s in sts),
+                "wall_ms": statistics.mean(s["wall_ms"] for s in sts),
+                "max_iterations": statistics.mean(s["max_iterations"] for s in sts),
+                "mean_iterations": statistics.mean(s["mean_iterations"] for s in sts),
+                "all_converged": all(s["converged"] == s["systems"] for s in sts),
+                "worst_rel_residual": max(s["max_rel_residual"] for s in sts),
+                "fallback_systems": sum(s["fallback_systems"] for s in sts),
+            }
+    line = {
+        "metric": "ms per elliptic solve to 1e-10 (learned FGMRES)", "value": res["learned_fgmres"]["wall_ms"],
+        "unit": "ms", "n_gpus": 1, "steps": n_eval, "warmup": max(args.warmup, 3),
+        "ms_per_step": res["learned_fgmres"]["wall_ms"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (solve), bf16/fp32 (network)", "data": "synthetic",
+        "config": {"workload": "elliptic-rl200", "grid": "RL, 200 cells, r in [0, 100], rings of 4+4r",
+                   "radial_systems": prob.nsys, "unknowns_per_system": prob.nmax, "held_out_seeds": n_eval,
+                   "train_fields": w["train_fields"], "train_random_sets": w["train_random"],
+                   "train_rows": net.dataset_rows(), "restart": w["restart"], "tol": w["tol"]},
+        "methods": res, "training": {"collect_s": collect_s, "phases": train},
+        "clocks": clk.summary(),
+        "e2e": {"value": res["learned_fgmres"]["wall_ms"], "unit": "ms", "h2d_bytes_per_step": n * 8,
+                "d2h_bytes_per_step": n * 5 * 8},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def _params(wl):
@@ -360,6 +457,8 @@ def main():
     ap.add_argument("--workload", default="rlz200-f64", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.workload == "elliptic-rl200":
+        return run_elliptic(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -286,6 +286,8 @@ int32_t ss_solve(ss_problem *problem, int32_t method, double tol, int32_t max_it
 int32_t ss_problem_export(const ss_problem *problem, double *rhs, double *x, double *res, int32_t *iters);
 int32_t ss_problem_collect_training(ss_problem *problem, ss_mlp *mlp, const double *points, const double *blobs,
                                    const int32_t *offsets, int32_t nfields, int32_t max_wavenumber);
+int32_t ss_problem_collect_random(ss_problem *problem, ss_mlp *mlp, int32_t nsets, uint64_t seed, int32_t smooth,
+                                  int32_t max_wavenumber);
 
 /* ---- learned preconditioner network --------------------------------------
  * No reference counterpart (the reference's preconditioners are :none and

@@ -249,6 +249,118 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tc_kernel(GemmArgs g) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kMlpWidth) : "memory");
 }
 
+// ---------------------------------------------------------------- fused inference
+// All three layers in one launch: a CTA keeps its 128 input rows (64 KB bf16)
+// in shared memory, stages each layer's 256 × 256 weights (128 KB), issues 16
+// tcgen05.mma (K = 16 each) into TMEM, and writes the ReLU'd bf16 activations
+// back over its input tile for the next layer.  256 threads: warps w and w + 4
+// share TMEM lanes 32(w mod 4)… and split the 256 columns in halves.
+constexpr int kInferThreads = 256;
+constexpr uint32_t kTileX = kMlpTileM * kMlpWidth * 2;     // 64 KB
+constexpr uint32_t kTileW = kMlpWidth * kMlpWidth * 2;     // 128 KB
+constexpr size_t kInferSmem = kTileX + kTileW + 1024;
+
+// full-K (256) core-matrix layout: 8-row groups 4 KB apart, core matrices along K 128 B apart
+__device__ __forceinline__ uint32_t cm_offset(int row, int col) {
+    return (uint32_t)((((row >> 3) * 32 + (col >> 3)) * 128) + (row & 7) * 16 + (col & 7) * 2);
+}
+
+__device__ __forceinline__ void stage_full(uint8_t *dst, const __nv_bfloat16 *src, int64_t row0, int rows) {
+    const int pieces = rows * 32;
+    for (int p = threadIdx.x; p < pieces; p += kInferThreads) {
+        const int row = p >> 5, kg = p & 31;
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src + (row0 + row) * kMlpWidth + kg * 8));
+        *reinterpret_cast<uint4 *>(dst + cm_offset(row, kg * 8)) = v;
+    }
+}
+
+__global__ void __launch_bounds__(kInferThreads) mlp_infer_kernel(const __nv_bfloat16 *in, const __nv_bfloat16 *Wb,
+                                                                  const float *bias, float *out, int *err) {
+    extern __shared__ __align__(1024) uint8_t smem_dyn[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_slot;
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
+    uint8_t *sX = base, *sW = base + kTileX;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t m0 = (int64_t)blockIdx.x * kMlpTileM;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(kMlpWidth)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    stage_full(sX, in, m0, kMlpTileM);
+    bool ok = true;
+    uint32_t phase = 0u;
+    const int row = (warp & 3) * 32 + lane, cbase = (warp >> 2) * (kMlpWidth / 2);
+    for (int l = 0; l < kMlpLayers; l++) {
+        stage_full(sW, Wb + (size_t)l * kMlpWidth * kMlpWidth, 0, kMlpWidth);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = smem_u32(sX), b0 = smem_u32(sW);
+#pragma unroll
+            for (int s = 0; s < kMlpWidth / 16; s++) {
+                const uint64_t ad = smem_desc(a0 + s * 256, 128, 4096);
+                const uint64_t bd = smem_desc(b0 + s * 256, 128, 4096);
+                const uint32_t acc = s > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&bar))
+                         : "memory");
+        }
+        bool done = mbar_wait(&bar, phase);
+        if (!done) done = mbar_wait(&bar, phase);
+        ok = ok && done;
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const float *bl = bias + l * kMlpWidth;
+        for (int cc = 0; cc < kMlpWidth / 64; cc++) {
+            const int c0 = cbase + cc * 32;
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0, v);
+            if (!ok) continue;
+            if (l + 1 < kMlpLayers) {
+                __align__(16) __nv_bfloat16 y[32];
+#pragma unroll
+                for (int i = 0; i < 32; i++) {
+                    const float z = v[i] + bl[c0 + i];
+                    y[i] = __float2bfloat16(z > 0.f ? z : 0.f);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    *reinterpret_cast<uint4 *>(sX + cm_offset(row, c0 + 8 * q)) = reinterpret_cast<const uint4 *>(y)[q];
+            } else {
+                float *o = out + (m0 + row) * kMlpWidth + c0;
+#pragma unroll
+                for (int i = 0; i < 32; i += 4)
+                    *reinterpret_cast<float4 *>(o + i) =
+                        make_float4(v[i] + bl[c0 + i], v[i + 1] + bl[c0 + i + 1], v[i + 2] + bl[c0 + i + 2],
+                                    v[i + 3] + bl[c0 + i + 3]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();  // activations written, TMEM read: the next layer may overwrite both
+    }
+    if (!ok && lane == 0) atomicExch(err, 1);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kMlpWidth) : "memory");
+}
+
 int32_t launch_gemm_tc(const GemmArgs &g, int splits, cudaStream_t st) {
     if (g.M <= 0 || g.M % kMlpTileM || g.ksplit <= 0 || g.ksplit % kMlpChunkK || splits < 1) {
         set_error("GEMM shape M=%d ksplit=%d not tiled by 128 x 64", g.M, g.ksplit);
@@ -460,15 +572,15 @@ int32_t mlp_forward(ss_mlp *m, const __nv_bfloat16 *in, float *out, int64_t rows
     int32_t r = mlp_reserve(m, rows);
     if (r) return r;
     const int M = (int)((rows + kMlpTileM - 1) / kMlpTileM * kMlpTileM);
-    GemmArgs g = gemm(in, kMlpWidth, m->Wb, kMlpWidth, M, kMlpWidth, GEMM_RELU, m->err);
-    g.bias = m->b; g.Yb = m->Y1;
-    if ((r = launch_gemm_tc(g, 1, st))) return r;
-    g = gemm(m->Y1, kMlpWidth, m->Wb + kWL, kMlpWidth, M, kMlpWidth, GEMM_RELU, m->err);
-    g.bias = m->b + kMlpWidth; g.Yb = m->Y2;
-    if ((r = launch_gemm_tc(g, 1, st))) return r;
-    g = gemm(m->Y2, kMlpWidth, m->Wb + 2 * kWL, kMlpWidth, M, kMlpWidth, GEMM_STORE, m->err);
-    g.bias = m->b + 2 * kMlpWidth; g.Cf = out; g.ldc = kMlpWidth;
-    return launch_gemm_tc(g, 1, st);
+    if (((uintptr_t)in & 15) || ((uintptr_t)out & 15)) { set_error("MLP rows must be 16-byte aligned"); return SS_BAD_SHAPE; }
+    static bool attr = false;
+    if (!attr) {
+        CUDA_TRY(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
+        attr = true;
+    }
+    mlp_infer_kernel<<<M / kMlpTileM, kInferThreads, kInferSmem, st>>>(in, m->Wb, m->b, out, m->err);
+    CUDA_TRY(cudaGetLastError());
+    return SS_OK;
 }
 
 // one forward/backward pass over the batch in X0/X0t/T/nrow (B rows, multiple of 128);

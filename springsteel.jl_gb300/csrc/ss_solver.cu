@@ -17,6 +17,13 @@
 // z = D⁻¹(v + N(v)) with N the learned MLP (Jacobi plus a learned
 // correction).  Systems the flexible solve leaves unconverged fall back to
 // Jacobi GMRES from where it stopped, then to the direct solve.
+//
+// Device layout: one warp per radial system.  Lane l holds elements
+// i = l + 32e (e < 8, so n ≤ 256) of every vector in registers; the banded
+// operator (7 diagonals per row, one copy per wavenumber) and the Krylov
+// bases V, Z (per system, rows of nmax doubles) live in global memory, which
+// the 129 MB L2 keeps resident (1201 systems × 31 × 201 doubles ≈ 60 MB).
+// Reductions are warp shuffles; no block barrier appears on the solve path.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -112,11 +119,19 @@ struct GammaDev {
     double aL, bL, aR, bR;
 };
 
+// band geometry the warp kernels are compiled for: 3 sub- and 3 superdiagonals
+// (cubic B-splines), so U of the pivoted LU has 7 diagonals
+constexpr int KL = 3, KU = 3, WG = KL + KU + 1, WU = KL + KU + 1;
+constexpr int kPer = 8;               // vector elements per lane: n ≤ 256
+constexpr int kMaxN = 32 * kPer;
+constexpr int kSysPerBlock = 4;       // warps (systems) per CTA
+constexpr int kMaxRestart = 100;
+
 }  // namespace ss
 
 struct ss_problem {
     ss_grid *g = nullptr;
-    int K = 0, nsys = 0, nmax = 0, kl = 0, ku = 0, wG = 0, wU = 0;
+    int K = 0, nsys = 0, nmax = 0, kl = 0, ku = 0;
     int n[2] = {0, 0};
     GammaDev gam[2];
     double *d_G = nullptr, *d_Lm = nullptr, *d_U = nullptr, *d_dinv = nullptr;
@@ -124,8 +139,8 @@ struct ss_problem {
     GammaDev *d_gam = nullptr;
     double *d_rhs = nullptr, *d_x = nullptr, *d_res = nullptr, *d_cnorm = nullptr;
     int *d_iters = nullptr, *d_state = nullptr;
-    // flexible GMRES workspace
-    int fg_restart = 0;
+    // Krylov workspace (both GMRES variants)
+    int ws_restart = 0;
     double *d_V = nullptr, *d_Z = nullptr, *d_H = nullptr, *d_gv = nullptr, *d_cs = nullptr, *d_sn = nullptr;
     int *d_cyc = nullptr;
     __nv_bfloat16 *d_mlp_in = nullptr;
@@ -165,107 +180,105 @@ struct SolveArgs {
     const double *spec;  // grid spectral: B-vectors in
     double *spec_out;    // coefficients a out
     const GammaDev *gam;
-    const double *G, *Lm, *U, *dinv;
+    const double *G, *Lm, *U, *dinv;  // G: [m][nmax][WG]; Lm: [m][nmax][KL]; U: [m][nmax][WU] (U[.][0] = 1/pivot)
     const int *piv;
     double *rhs, *x, *res, *cnorm;
     int *iters, *state;  // state: 0 active, 1 converged (or solved directly), 2 stopped inside a cycle
+    double *V, *Z, *H, *gv, *cs, *sn;  // Krylov workspace per system
+    int *cyc;
+    __nv_bfloat16 *mlp_in;
+    const float *mlp_out;
     int64_t nspec;
-    int nslots, nvars, nmax, kl, ku, wG, wU, b, restart, max_iter, warm, masked;
+    int nsys, nslots, nvars, nmax, b, restart, max_iter, warm, masked, K, mcut, j;
     double tol;
 };
 
 __device__ __forceinline__ const GammaDev &gam_of(const SolveArgs &A, int m) { return A.gam[m == 0 ? 0 : 1]; }
 
-// c = Γ_m b (src/CubicBSpline.jl:427-458), zero-padded to nmax; ‖c‖ per system
-__global__ void rhs_kernel(SolveArgs A) {
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= A.nslots * A.nvars) return;
-    const int v = sys / A.nslots, q = sys % A.nslots, m = slot_wavenumber(q);
-    const GammaDev &g = gam_of(A, m);
-    const double *b = A.spec + (size_t)v * A.nspec + (size_t)q * A.b;
-    double *r = A.rhs + (size_t)sys * A.nmax;
-    const double b0 = b[0], b1 = b[1], bM1 = b[g.Md - 1], bM2 = b[g.Md - 2];
-    double nrm = 0.0;
-    for (int i = 0; i < g.Min; i++) r[i] = b[i + g.rankL];
-    if (g.lk == BC_A1) { r[0] += g.aL * b0; r[1] += g.bL * b0; }
-    else if (g.lk == BC_A2) r[0] += g.aL * b0 + g.bL * b1;
-    if (g.rk == BC_A1) { r[g.Min - 1] += g.aR * bM1; r[g.Min - 2] += g.bR * bM1; }
-    else if (g.rk == BC_A2) r[g.Min - 1] += g.aR * bM1 + g.bR * bM2;
-    for (int i = 0; i < g.Min; i++) nrm += r[i] * r[i];
-    for (int i = g.Min; i < A.nmax; i++) r[i] = 0.0;
-    A.cnorm[sys] = sqrt(nrm);
-}
-
-// a = Γ_mᵀ x into the spectral array (src/CubicBSpline.jl:461-500)
-__global__ void unfold_kernel(SolveArgs A) {
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= A.nslots * A.nvars) return;
-    const int v = sys / A.nslots, q = sys % A.nslots, m = slot_wavenumber(q);
-    const GammaDev &g = gam_of(A, m);
-    const double *x = A.x + (size_t)sys * A.nmax;
-    double *a = A.spec_out + (size_t)v * A.nspec + (size_t)q * A.b;
-    const int Md = g.Md, n = g.Min, rL = g.rankL;
-    for (int j = 0; j < rL; j++) a[j] = 0.0;
-    for (int j = Md - g.rankR; j < Md; j++) a[j] = 0.0;
-    for (int i = 0; i < n; i++) a[i + rL] = x[i];
-    if (g.lk == BC_A1) a[0] = g.aL * x[0] + g.bL * x[1];
-    else if (g.lk == BC_A2) { a[0] = g.aL * x[0]; a[1] = g.bL * x[0]; }
-    if (g.rk == BC_A1) a[Md - 1] = g.aR * x[n - 1] + g.bR * x[n - 2];
-    else if (g.rk == BC_A2) { a[Md - 2] = g.bR * x[n - 1]; a[Md - 1] = g.aR * x[n - 1]; }
-}
-
-// direct solve: banded LU with partial pivoting (dgbtrs order), one thread per system
-__global__ void direct_kernel(SolveArgs A) {
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= A.nslots * A.nvars) return;
-    if (A.masked && A.state[sys] == 1) return;
-    const int q = sys % A.nslots, m = slot_wavenumber(q);
-    const int n = gam_of(A, m).Min;
-    const double *Lm = A.Lm + (size_t)m * A.nmax * A.kl;
-    const double *U = A.U + (size_t)m * A.nmax * A.wU;
-    const int *piv = A.piv + (size_t)m * A.nmax;
-    double *x = A.x + (size_t)sys * A.nmax;
-    const double *r = A.rhs + (size_t)sys * A.nmax;
-    for (int i = 0; i < n; i++) x[i] = r[i];
-    for (int k = 0; k < n; k++) {
-        const int p = piv[k];
-        if (p != k) { double t = x[k]; x[k] = x[p]; x[p] = t; }
-        const double xk = x[k];
-        for (int t = 0; t < A.kl && k + 1 + t < n; t++) x[k + 1 + t] -= Lm[(size_t)k * A.kl + t] * xk;
-    }
-    for (int i = n - 1; i >= 0; i--) {
-        double s = x[i];
-        for (int t = 1; t < A.wU && i + t < n; t++) s -= U[(size_t)i * A.wU + t] * x[i + t];
-        x[i] = s / U[(size_t)i * A.wU];
-    }
-    A.state[sys] = 1;
-}
-
-// block-wide sum (blockDim a multiple of 32, ≤ 1024)
-__device__ double block_sum(double v, double *red) {
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) red[w] = v;
-    __syncthreads();
-    double s = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += red[i];
-    return s;
+    return v;
 }
 
-// w = G_m z (radial_op_matvec; band rows: G[i][i + t − kl] at i·wG + t)
-__device__ __forceinline__ void band_matvec(const double *G, int wG, int kl, int n, const double *z, double *w) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double acc = 0.0;
-        for (int t = 0; t < wG; t++) {
-            const int j = i + t - kl;
-            if (j >= 0 && j < n) acc += G[(size_t)i * wG + t] * z[j];
-        }
-        w[i] = acc;
+// per-warp shared scratch: one staged vector and the Gram–Schmidt coefficients
+struct WarpSmem {
+    double z[kSysPerBlock][kMaxN + 8];
+    double h[kSysPerBlock][kMaxRestart + 1];
+};
+
+#define WARP_SYSTEM()                                                  \
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;         \
+    const int sys = blockIdx.x * kSysPerBlock + wid;                   \
+    if (sys >= A.nsys) return;                                         \
+    const int q = sys % A.nslots, m = slot_wavenumber(q);              \
+    const int n = gam_of(A, m).Min;
+
+__device__ __forceinline__ void load_vec(double (&v)[kPer], const double *src, int n, int lane) {
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;
+        v[e] = i < n ? src[i] : 0.0;
     }
 }
+__device__ __forceinline__ void store_vec(double *dst, const double (&v)[kPer], int n, int lane) {
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;
+        if (i < n) dst[i] = v[e];
+    }
+}
+__device__ __forceinline__ double dot_vec(const double (&a)[kPer], const double (&b)[kPer]) {
+    double s = 0.0;
+#pragma unroll
+    for (int e = 0; e < kPer; e++) s += a[e] * b[e];
+    return warp_sum(s);
+}
 
-// Givens update of column j of H and of g (thread 0)
+// w = G_m z (radial_op_matvec): z staged in the warp's shared row, 7 diagonals per row
+__device__ __forceinline__ void band_matvec_w(const double *G, const double (&z)[kPer], double (&w)[kPer], double *zs,
+                                              int n, int lane) {
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;
+        if (i < n) zs[i + KL] = z[e];
+    }
+    if (lane < KL) zs[lane] = 0.0;
+    if (lane < KU) zs[n + KL + lane] = 0.0;
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;
+        double acc = 0.0;
+        if (i < n) {
+            const double *g = G + (size_t)i * WG;
+#pragma unroll
+            for (int t = 0; t < WG; t++) acc += g[t] * zs[i + t];
+        }
+        w[e] = acc;
+    }
+    __syncwarp();
+}
+
+// Orthogonalise w against V[0..jc) by modified Gram–Schmidt (the fewest FP64
+// operations per step; FP64 runs at 1/64 of the FP32 rate on this part); the
+// next row's load is issued before the current row's reduction.
+__device__ __forceinline__ void mgs_w(const double *V, int ld, int jc, double (&w)[kPer], int n, int lane, double *hs) {
+    double vk[kPer], vn[kPer];
+    load_vec(vk, V, n, lane);
+    for (int k = 0; k < jc; k++) {
+        if (k + 1 < jc) load_vec(vn, V + (size_t)(k + 1) * ld, n, lane);
+        const double h = dot_vec(w, vk);
+#pragma unroll
+        for (int e = 0; e < kPer; e++) w[e] -= h * vk[e];
+        if (lane == 0) hs[k] = h;
+#pragma unroll
+        for (int e = 0; e < kPer; e++) vk[e] = vn[e];
+    }
+    __syncwarp();
+}
+
+// Givens update of column j of H and of g (lane 0)
 __device__ __forceinline__ void givens_column(double *H, int R, int j, double *cs, double *sn, double *gv) {
     for (int k = 0; k < j; k++) {
         const double a = H[(size_t)k * R + j], bb = H[(size_t)(k + 1) * R + j];
@@ -282,16 +295,156 @@ __device__ __forceinline__ void givens_column(double *H, int R, int j, double *c
     gv[j] = cs[j] * gv[j];
 }
 
+// y = H⁻¹ g over `steps` columns (lane 0), into ys
+__device__ __forceinline__ void hessenberg_solve(const double *H, int R, const double *gv, int steps, double *ys) {
+    for (int k = steps - 1; k >= 0; k--) {
+        double s = gv[k];
+        for (int l = k + 1; l < steps; l++) s -= H[(size_t)k * R + l] * ys[l];
+        ys[k] = s / H[(size_t)k * R + k];
+    }
+}
+
+// c = Γ_m b (src/CubicBSpline.jl:427-458), zero-padded to nmax; ‖c‖ per system
+__global__ void __launch_bounds__(128) rhs_kernel(SolveArgs A) {
+    WARP_SYSTEM();
+    const GammaDev &g = gam_of(A, m);
+    const int v = sys / A.nslots;
+    const double *b = A.spec + (size_t)v * A.nspec + (size_t)q * A.b;
+    double *r = A.rhs + (size_t)sys * A.nmax;
+    const double b0 = b[0], b1 = b[1], bM1 = b[g.Md - 1], bM2 = b[g.Md - 2];
+    double c[kPer];
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;
+        double val = i < n ? b[i + g.rankL] : 0.0;
+        if (i == 0) { if (g.lk == BC_A1) val += g.aL * b0; else if (g.lk == BC_A2) val += g.aL * b0 + g.bL * b1; }
+        if (i == 1 && g.lk == BC_A1) val += g.bL * b0;
+        if (i == n - 1) { if (g.rk == BC_A1) val += g.aR * bM1; else if (g.rk == BC_A2) val += g.aR * bM1 + g.bR * bM2; }
+        if (i == n - 2 && g.rk == BC_A1) val += g.bR * bM1;
+        c[e] = val;
+        if (i < A.nmax) r[i] = val;
+    }
+    const double nrm = sqrt(dot_vec(c, c));
+    if (lane == 0) A.cnorm[sys] = nrm;
+}
+
+// a = Γ_mᵀ x into the spectral array (src/CubicBSpline.jl:461-500)
+__global__ void __launch_bounds__(128) unfold_kernel(SolveArgs A) {
+    WARP_SYSTEM();
+    const GammaDev &g = gam_of(A, m);
+    const int v = sys / A.nslots;
+    const double *x = A.x + (size_t)sys * A.nmax;
+    double *a = A.spec_out + (size_t)v * A.nspec + (size_t)q * A.b;
+    const int Md = g.Md, rL = g.rankL;
+    const double x0 = x[0], x1 = x[1], xn1 = x[n - 1], xn2 = x[n - 2];
+    for (int jx = lane; jx < Md; jx += 32) {
+        double val = (jx >= rL && jx < rL + n) ? x[jx - rL] : 0.0;
+        if (jx == 0) { if (g.lk == BC_A1) val = g.aL * x0 + g.bL * x1; else if (g.lk == BC_A2) val = g.aL * x0; }
+        if (jx == 1 && g.lk == BC_A2) val = g.bL * x0;
+        if (jx == Md - 1) { if (g.rk == BC_A1) val = g.aR * xn1 + g.bR * xn2; else if (g.rk == BC_A2) val = g.aR * xn1; }
+        if (jx == Md - 2 && g.rk == BC_A2) val = g.bR * xn1;
+        a[jx] = val;
+    }
+}
+
+// direct solve: banded LU with partial pivoting (dgbtrs order).  The warp
+// stages the right-hand side into shared memory; lane 0 runs both sweeps with
+// the moving window of the band in registers.
+__global__ void __launch_bounds__(128) direct_kernel(SolveArgs A) {
+    __shared__ double xs[kSysPerBlock][kMaxN + 8];
+    WARP_SYSTEM();
+    if (A.masked && A.state[sys] == 1) return;
+    double *xw = xs[wid];
+    const double *r = A.rhs + (size_t)sys * A.nmax;
+    for (int i = lane; i < n; i += 32) xw[i] = r[i];
+    __syncwarp();
+    if (lane == 0) {
+        const double *Lm = A.Lm + (size_t)m * A.nmax * KL;
+        const double *U = A.U + (size_t)m * A.nmax * WU;
+        const int *piv = A.piv + (size_t)m * A.nmax;
+        // forward: window w[0..KL] = x[k..k+KL]
+        double w0 = xw[0], w1 = n > 1 ? xw[1] : 0.0, w2 = n > 2 ? xw[2] : 0.0, w3 = n > 3 ? xw[3] : 0.0;
+        for (int k = 0; k < n; k++) {
+            const int p = piv[k] - k;  // 0..KL
+            if (p == 1) { const double t = w0; w0 = w1; w1 = t; }
+            else if (p == 2) { const double t = w0; w0 = w2; w2 = t; }
+            else if (p == 3) { const double t = w0; w0 = w3; w3 = t; }
+            const double *l = Lm + (size_t)k * KL;
+            w1 -= l[0] * w0;
+            w2 -= l[1] * w0;
+            w3 -= l[2] * w0;
+            xw[k] = w0;
+            w0 = w1; w1 = w2; w2 = w3;
+            w3 = (k + 4 < n) ? xw[k + 4] : 0.0;
+        }
+        // backward: window y[1..6] = x[i+1..i+6]
+        double y1 = 0.0, y2 = 0.0, y3 = 0.0, y4 = 0.0, y5 = 0.0, y6 = 0.0;
+        for (int i = n - 1; i >= 0; i--) {
+            const double *u = U + (size_t)i * WU;
+            const double s = xw[i] - (u[1] * y1 + u[2] * y2) - (u[3] * y3 + u[4] * y4) - (u[5] * y5 + u[6] * y6);
+            const double xi = s * u[0];
+            xw[i] = xi;
+            y6 = y5; y5 = y4; y4 = y3; y3 = y2; y2 = y1; y1 = xi;
+        }
+    }
+    __syncwarp();
+    double *x = A.x + (size_t)sys * A.nmax;
+    for (int i = lane; i < n; i += 32) x[i] = xw[i];
+    if (lane == 0) A.state[sys] = 1;
+}
+
+// true relative residual ‖c − G x‖ / ‖c‖
+__global__ void __launch_bounds__(128) residual_kernel(SolveArgs A) {
+    __shared__ double zs[kSysPerBlock][kMaxN + 8];
+    WARP_SYSTEM();
+    double x[kPer], w[kPer], c[kPer];
+    load_vec(x, A.x + (size_t)sys * A.nmax, n, lane);
+    load_vec(c, A.rhs + (size_t)sys * A.nmax, n, lane);
+    band_matvec_w(A.G + (size_t)m * A.nmax * WG, x, w, zs[wid], n, lane);
+#pragma unroll
+    for (int e = 0; e < kPer; e++) w[e] = c[e] - w[e];
+    const double rr = sqrt(dot_vec(w, w)) / (A.cnorm[sys] > 0.0 ? A.cnorm[sys] : 1.0);
+    if (lane == 0) A.res[sys] = rr;
+}
+
+// block-wide sum (blockDim a multiple of 32, ≤ 1024)
+__device__ double block_sum(double v, double *red) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += red[i];
+    return s;
+}
+
+// w = G_m z with z and w in shared memory (block version)
+__device__ __forceinline__ void band_matvec_b(const double *G, int n, const double *z, double *w) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double acc = 0.0;
+#pragma unroll
+        for (int t = 0; t < WG; t++) {
+            const int j = i + t - KL;
+            if (j >= 0 && j < n) acc += G[(size_t)i * WG + t] * z[j];
+        }
+        w[i] = acc;
+    }
+}
+
 // restarted GMRES with right Jacobi preconditioning (the reference's :diag,
-// src/solver_problem.jl:172-179): one CTA per system, Krylov basis in shared memory
-__global__ void gmres_kernel(SolveArgs A) {
+// src/solver_problem.jl:172-179).  One CTA per system with the Krylov basis in
+// shared memory: FP64 throughput is 1/64 of FP32 on this part, so the slow
+// low-wavenumber systems finish sooner when 128 threads share each iteration
+// (modified Gram–Schmidt, the fewest FP64 operations per step).
+__global__ void __launch_bounds__(128) gmres_kernel(SolveArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red[32];
     const int sys = blockIdx.x;
     if (A.masked && A.state[sys] == 1) return;
     const int q = sys % A.nslots, m = slot_wavenumber(q);
     const int n = gam_of(A, m).Min, R = A.restart;
-    const double *G = A.G + (size_t)m * A.nmax * A.wG;
+    const double *G = A.G + (size_t)m * A.nmax * WG;
     const double *dv = A.dinv + (size_t)m * A.nmax;
     double *V = reinterpret_cast<double *>(smem_raw);   // (R+1) × n
     double *w = V + (size_t)(R + 1) * n;                 // n
@@ -307,7 +460,7 @@ __global__ void gmres_kernel(SolveArgs A) {
     int it = 0;
     double rel = 1.0;
     while (it < A.max_iter) {
-        band_matvec(G, A.wG, A.kl, n, x, w);
+        band_matvec_b(G, n, x, w);
         __syncthreads();
         double part = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) { w[i] = c[i] - w[i]; part += w[i] * w[i]; }
@@ -321,7 +474,7 @@ __global__ void gmres_kernel(SolveArgs A) {
         for (; j < R && it < A.max_iter; j++, it++) {
             for (int i = threadIdx.x; i < n; i += blockDim.x) z[i] = dv[i] * V[(size_t)j * n + i];
             __syncthreads();
-            band_matvec(G, A.wG, A.kl, n, z, w);
+            band_matvec_b(G, n, z, w);
             __syncthreads();
             for (int k = 0; k <= j; k++) {  // modified Gram–Schmidt
                 double pk = 0.0;
@@ -341,14 +494,9 @@ __global__ void gmres_kernel(SolveArgs A) {
             }
             __syncthreads();
             rel = fabs(gv[j + 1]) / cn;
-            if (rel <= A.tol) { j++; it++; break; }
+            if (rel <= A.tol || hn == 0.0) { j++; it++; break; }
         }
-        if (threadIdx.x == 0)  // y = H⁻¹ g
-            for (int k = j - 1; k >= 0; k--) {
-                double s = gv[k];
-                for (int l = k + 1; l < j; l++) s -= H[(size_t)k * R + l] * yv[l];
-                yv[k] = s / H[(size_t)k * R + k];
-            }
+        if (threadIdx.x == 0) hessenberg_solve(H, R, gv, j, yv);
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += blockDim.x) {  // x += D⁻¹ V y
             double acc = 0.0;
@@ -358,7 +506,7 @@ __global__ void gmres_kernel(SolveArgs A) {
         __syncthreads();
         if (rel <= A.tol) break;
     }
-    band_matvec(G, A.wG, A.kl, n, x, w);  // true residual
+    band_matvec_b(G, n, x, w);  // true residual
     __syncthreads();
     double part = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) { const double d = c[i] - w[i]; part += d * d; }
@@ -370,158 +518,136 @@ __global__ void gmres_kernel(SolveArgs A) {
     }
 }
 
-// true relative residual ‖c − G x‖ / ‖c‖ (one CTA per system)
-__global__ void residual_kernel(SolveArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double red[32];
-    const int sys = blockIdx.x;
-    const int q = sys % A.nslots, m = slot_wavenumber(q);
-    const int n = gam_of(A, m).Min;
-    double *w = reinterpret_cast<double *>(smem_raw);
-    band_matvec(A.G + (size_t)m * A.nmax * A.wG, A.wG, A.kl, n, A.x + (size_t)sys * A.nmax, w);
-    __syncthreads();
-    const double *c = A.rhs + (size_t)sys * A.nmax;
-    double part = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) { const double d = c[i] - w[i]; part += d * d; }
-    const double rr = sqrt(block_sum(part, red)) / (A.cnorm[sys] > 0.0 ? A.cnorm[sys] : 1.0);
-    if (threadIdx.x == 0) A.res[sys] = rr;
+static size_t gmres_smem(int R, int n) {
+    return ((size_t)(R + 1) * n + 2 * (size_t)n + (size_t)(R + 1) * R + 4 * (size_t)R + 4) * 8;
 }
 
 // ---------------------------------------------------------------- flexible GMRES
 // All systems advance in lockstep so the MLP runs as one batched tensor-core
 // pass per Arnoldi step.  MLP input row of a system: v (first n entries),
 // zeros, then the features m/K and log(1+m)/log(1+K) in the last two columns.
-struct FgArgs {
-    SolveArgs S;
-    double *V, *Z, *H, *gv, *cs, *sn;
-    int *cyc;                // Arnoldi steps taken in the current cycle
-    __nv_bfloat16 *mlp_in;   // [mpad][256]
-    const float *mlp_out;    // [mpad][256]
-    int j, K, mcut;
-};
-
-__device__ __forceinline__ void write_mlp_row(__nv_bfloat16 *row, const double *v, double scale, int n, int m, int K) {
-    for (int i = threadIdx.x; i < kMlpWidth; i += blockDim.x) {
+__device__ __forceinline__ void write_mlp_row_w(__nv_bfloat16 *row, const double (&v)[kPer], double scale, int n, int m,
+                                                int K, int lane) {
+    const float f0 = (float)m / (float)(K > 0 ? K : 1);
+    const float f1 = (float)(log1p((double)m) / log1p((double)(K > 0 ? K : 1)));
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;  // covers 0..255
         float val = 0.f;
-        if (i < n) val = (float)(v[i] * scale);
-        else if (i == kMlpWidth - 2) val = (float)m / (float)(K > 0 ? K : 1);
-        else if (i == kMlpWidth - 1) val = (float)(log1p((double)m) / log1p((double)(K > 0 ? K : 1)));
+        if (i < n) val = (float)(v[e] * scale);
+        else if (i == kMlpWidth - 2) val = f0;
+        else if (i == kMlpWidth - 1) val = f1;
         row[i] = __float2bfloat16(val);
     }
 }
 
 // start of a cycle: r = c − G x; converged systems leave; else v0 = r / β
-__global__ void fg_begin_kernel(FgArgs F) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double red[32];
-    const SolveArgs &A = F.S;
-    const int sys = blockIdx.x;
-    const int q = sys % A.nslots, m = slot_wavenumber(q);
-    const int n = gam_of(A, m).Min, R = A.restart;
-    __nv_bfloat16 *row = F.mlp_in + (size_t)sys * kMlpWidth;
-    if (A.state[sys] == 1) { write_mlp_row(row, nullptr, 0.0, 0, m, F.K); return; }
-    double *w = reinterpret_cast<double *>(smem_raw);
-    const double *c = A.rhs + (size_t)sys * A.nmax;
-    double *x = A.x + (size_t)sys * A.nmax;
-    double *V = F.V + (size_t)sys * (R + 1) * A.nmax;
-    band_matvec(A.G + (size_t)m * A.nmax * A.wG, A.wG, A.kl, n, x, w);
-    __syncthreads();
-    double part = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) { w[i] = c[i] - w[i]; part += w[i] * w[i]; }
-    const double beta = sqrt(block_sum(part, red));
-    const double cn = A.cnorm[sys] > 0.0 ? A.cnorm[sys] : 1.0;
-    if (beta / cn <= A.tol || beta == 0.0) {
-        if (threadIdx.x == 0) { A.state[sys] = 1; A.res[sys] = beta / cn; }
-        write_mlp_row(row, nullptr, 0.0, 0, m, F.K);
+__global__ void __launch_bounds__(128) fg_begin_kernel(SolveArgs A) {
+    __shared__ double zs[kSysPerBlock][kMaxN + 8];
+    WARP_SYSTEM();
+    const int R = A.restart;
+    __nv_bfloat16 *row = A.mlp_in + (size_t)sys * kMlpWidth;
+    double x[kPer], c[kPer], w[kPer];
+    if (A.state[sys] == 1) {
+#pragma unroll
+        for (int e = 0; e < kPer; e++) w[e] = 0.0;
+        write_mlp_row_w(row, w, 0.0, 0, m, A.K, lane);
         return;
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) V[i] = w[i] / beta;
-    if (threadIdx.x == 0) {
-        double *gv = F.gv + (size_t)sys * (R + 1);
+    load_vec(x, A.x + (size_t)sys * A.nmax, n, lane);
+    load_vec(c, A.rhs + (size_t)sys * A.nmax, n, lane);
+    band_matvec_w(A.G + (size_t)m * A.nmax * WG, x, w, zs[wid], n, lane);
+#pragma unroll
+    for (int e = 0; e < kPer; e++) w[e] = c[e] - w[e];
+    const double beta = sqrt(dot_vec(w, w));
+    const double cn = A.cnorm[sys] > 0.0 ? A.cnorm[sys] : 1.0;
+    if (beta / cn <= A.tol || beta == 0.0) {
+        if (lane == 0) { A.state[sys] = 1; A.res[sys] = beta / cn; }
+#pragma unroll
+        for (int e = 0; e < kPer; e++) w[e] = 0.0;
+        write_mlp_row_w(row, w, 0.0, 0, m, A.K, lane);
+        return;
+    }
+#pragma unroll
+    for (int e = 0; e < kPer; e++) w[e] /= beta;
+    store_vec(A.V + (size_t)sys * (R + 1) * A.nmax, w, n, lane);
+    if (lane == 0) {
+        double *gv = A.gv + (size_t)sys * (R + 1);
         gv[0] = beta;
         for (int i = 1; i <= R; i++) gv[i] = 0.0;
         A.state[sys] = 0;
-        F.cyc[sys] = 0;
+        A.cyc[sys] = 0;
     }
-    write_mlp_row(row, w, 1.0 / beta, n, m, F.K);
+    write_mlp_row_w(row, w, 1.0, n, m, A.K, lane);
 }
 
 // Arnoldi step j: z_j = D⁻¹(v_j + N(v_j)), w = G z_j, orthogonalise, Givens, next MLP input
-__global__ void fg_step_kernel(FgArgs F) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double red[32];
-    const SolveArgs &A = F.S;
-    const int sys = blockIdx.x;
+__global__ void __launch_bounds__(128) fg_step_kernel(SolveArgs A) {
+    __shared__ WarpSmem S;
+    WARP_SYSTEM();
     if (A.state[sys] != 0) return;
-    const int q = sys % A.nslots, m = slot_wavenumber(q);
-    const int n = gam_of(A, m).Min, R = A.restart, j = F.j;
-    const double *dv = A.dinv + (size_t)m * A.nmax;
-    double *V = F.V + (size_t)sys * (R + 1) * A.nmax;
-    double *Z = F.Z + (size_t)sys * R * A.nmax;
-    double *H = F.H + (size_t)sys * (R + 1) * R;
-    double *gv = F.gv + (size_t)sys * (R + 1), *cs = F.cs + (size_t)sys * R, *sn = F.sn + (size_t)sys * R;
-    double *w = reinterpret_cast<double *>(smem_raw);
-    double *z = Z + (size_t)j * A.nmax;
-    const double *vj = V + (size_t)j * A.nmax;
-    const float *o = F.mlp_out + (size_t)sys * kMlpWidth;
-    const bool learned = m <= F.mcut;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) z[i] = dv[i] * (vj[i] + (learned ? (double)o[i] : 0.0));
-    __syncthreads();
-    band_matvec(A.G + (size_t)m * A.nmax * A.wG, A.wG, A.kl, n, z, w);
-    __syncthreads();
-    for (int k = 0; k <= j; k++) {
-        double pk = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) pk += w[i] * V[(size_t)k * A.nmax + i];
-        const double hk = block_sum(pk, red);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] -= hk * V[(size_t)k * A.nmax + i];
-        if (threadIdx.x == 0) H[(size_t)k * R + j] = hk;
-        __syncthreads();
+    const int R = A.restart, j = A.j, ld = A.nmax;
+    double *V = A.V + (size_t)sys * (R + 1) * ld;
+    double *H = A.H + (size_t)sys * (R + 1) * R;
+    double *gv = A.gv + (size_t)sys * (R + 1), *cs = A.cs + (size_t)sys * R, *sn = A.sn + (size_t)sys * R;
+    double dv[kPer], v[kPer], z[kPer], w[kPer];
+    load_vec(dv, A.dinv + (size_t)m * A.nmax, n, lane);
+    load_vec(v, V + (size_t)j * ld, n, lane);
+    const float *o = A.mlp_out + (size_t)sys * kMlpWidth;
+    const bool learned = m <= A.mcut;
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;
+        z[e] = i < n ? dv[e] * (v[e] + (learned ? (double)o[i] : 0.0)) : 0.0;
     }
-    double pn = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) pn += w[i] * w[i];
-    const double hn = sqrt(block_sum(pn, red));
-    double *vn = V + (size_t)(j + 1) * A.nmax;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) vn[i] = hn > 0.0 ? w[i] / hn : 0.0;
-    if (threadIdx.x == 0) {
+    store_vec(A.Z + (size_t)sys * R * ld + (size_t)j * ld, z, n, lane);
+    band_matvec_w(A.G + (size_t)m * A.nmax * WG, z, w, S.z[wid], n, lane);
+    mgs_w(V, ld, j + 1, w, n, lane, S.h[wid]);
+    const double hn = sqrt(dot_vec(w, w));
+#pragma unroll
+    for (int e = 0; e < kPer; e++) w[e] = hn > 0.0 ? w[e] / hn : 0.0;
+    store_vec(V + (size_t)(j + 1) * ld, w, n, lane);
+    double g1 = 0.0;
+    if (lane == 0) {
+        for (int k = 0; k <= j; k++) H[(size_t)k * R + j] = S.h[wid][k];
         H[(size_t)(j + 1) * R + j] = hn;
         givens_column(H, R, j, cs, sn, gv);
         A.iters[sys] += 1;
-        F.cyc[sys] = j + 1;
+        A.cyc[sys] = j + 1;
+        g1 = gv[j + 1];
     }
-    __syncthreads();
+    g1 = __shfl_sync(0xffffffffu, g1, 0);
     const double cn = A.cnorm[sys] > 0.0 ? A.cnorm[sys] : 1.0;
-    if (fabs(gv[j + 1]) / cn <= A.tol || hn == 0.0) {
-        if (threadIdx.x == 0) A.state[sys] = 2;  // converged estimate: stop this cycle
+    if (fabs(g1) / cn <= A.tol || hn == 0.0) {
+        if (lane == 0) A.state[sys] = 2;  // converged estimate: stop this cycle
         return;
     }
-    write_mlp_row(F.mlp_in + (size_t)sys * kMlpWidth, vn, 1.0, n, m, F.K);
+    write_mlp_row_w(A.mlp_in + (size_t)sys * kMlpWidth, w, 1.0, n, m, A.K, lane);
 }
 
 // end of a cycle: x += Z y over the steps this system took
-__global__ void fg_end_kernel(FgArgs F) {
-    const SolveArgs &A = F.S;
-    const int sys = blockIdx.x;
+__global__ void __launch_bounds__(128) fg_end_kernel(SolveArgs A) {
+    __shared__ double ys[kSysPerBlock][kMaxRestart + 1];
+    WARP_SYSTEM();
     if (A.state[sys] == 1) return;
-    const int q = sys % A.nslots, m = slot_wavenumber(q);
-    const int n = gam_of(A, m).Min, R = A.restart, steps = F.cyc[sys];
-    const double *Z = F.Z + (size_t)sys * R * A.nmax;
-    const double *H = F.H + (size_t)sys * (R + 1) * R;
-    const double *gv = F.gv + (size_t)sys * (R + 1);
-    __shared__ double yv[128];
-    if (threadIdx.x == 0)
-        for (int k = steps - 1; k >= 0; k--) {
-            double s = gv[k];
-            for (int l = k + 1; l < steps; l++) s -= H[(size_t)k * R + l] * yv[l];
-            yv[k] = s / H[(size_t)k * R + k];
+    const int R = A.restart, steps = A.cyc[sys], ld = A.nmax;
+    const double *Z = A.Z + (size_t)sys * R * ld;
+    if (lane == 0) hessenberg_solve(A.H + (size_t)sys * (R + 1) * R, R, A.gv + (size_t)sys * (R + 1), steps, ys[wid]);
+    __syncwarp();
+    double x[kPer];
+    double *xg = A.x + (size_t)sys * ld;
+    load_vec(x, xg, n, lane);
+    for (int k = 0; k < steps; k++) {
+        const double yk = ys[wid][k];
+        const double *zk = Z + (size_t)k * ld;
+#pragma unroll
+        for (int e = 0; e < kPer; e++) {
+            const int i = lane + 32 * e;
+            if (i < n) x[e] += yk * zk[i];
         }
-    __syncthreads();
-    double *x = A.x + (size_t)sys * A.nmax;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double acc = 0.0;
-        for (int k = 0; k < steps; k++) acc += Z[(size_t)k * A.nmax + i] * yv[k];
-        x[i] += acc;
     }
-    if (threadIdx.x == 0) A.state[sys] = 0;
+    store_vec(xg, x, n, lane);
+    if (lane == 0) A.state[sys] = 0;
 }
 
 // ---------------------------------------------------------------- training fields
@@ -541,27 +667,68 @@ __global__ void blob_field_kernel(double *phys, int64_t np, int nvars, const dou
     for (int v = 0; v < nvars; v++) phys[(size_t)v * np + i] = f;
 }
 
+// counter-based normal deviates (splitmix64 mixing + Box–Muller) for random right-hand sides
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double normal_dev(uint64_t seed, uint64_t idx) {
+    const uint64_t a = mix64(seed ^ mix64(2 * idx)), b = mix64(seed ^ mix64(2 * idx + 1));
+    const double u1 = ((a >> 11) + 1.0) * (1.0 / 9007199254740993.0);  // (0, 1]
+    const double u2 = (b >> 11) * (1.0 / 9007199254740992.0);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// c = white noise smoothed `smooth` times by a (1, 2, 1)/4 filter, per system
+__global__ void __launch_bounds__(128) rhs_random_kernel(SolveArgs A, uint64_t seed, int smooth) {
+    __shared__ double ws[kSysPerBlock][kMaxN + 2];
+    WARP_SYSTEM();
+    double *w = ws[wid] + 1;
+    for (int i = lane; i < n; i += 32) w[i] = normal_dev(seed, (uint64_t)sys * A.nmax + i);
+    if (lane == 0) { w[-1] = 0.0; w[n] = 0.0; }
+    __syncwarp();
+    double c[kPer];
+    for (int s = 0; s < smooth; s++) {
+#pragma unroll
+        for (int e = 0; e < kPer; e++) {
+            const int i = lane + 32 * e;
+            c[e] = i < n ? 0.25 * (w[i - 1] + 2.0 * w[i] + w[i + 1]) : 0.0;
+        }
+        __syncwarp();
+        store_vec(w, c, n, lane);
+        __syncwarp();
+    }
+    load_vec(c, w, n, lane);
+    double *r = A.rhs + (size_t)sys * A.nmax;
+    for (int i = lane; i < A.nmax; i += 32) r[i] = i < n ? w[i] : 0.0;
+    const double nrm = sqrt(dot_vec(c, c));
+    if (lane == 0) A.cnorm[sys] = nrm;
+}
+
 // training rows from the direct solution: input v = c/‖c‖, target D x/‖c‖ − v
-__global__ void training_rows_kernel(SolveArgs A, int K, int mcut, int64_t row0, __nv_bfloat16 *X,
-                                     __nv_bfloat16 *T, int32_t *nrow) {
-    const int sys = blockIdx.x;
-    const int q = sys % A.nslots, m = slot_wavenumber(q);
-    if (m > mcut) return;
+__global__ void __launch_bounds__(128) training_rows_kernel(SolveArgs A, int64_t row0, __nv_bfloat16 *X,
+                                                            __nv_bfloat16 *T, int32_t *nrow) {
+    WARP_SYSTEM();
+    if (m > A.mcut) return;
     // rows are packed per variable: the slots of wavenumbers ≤ mcut in slot order
-    const int per_var = 1 + 2 * min(mcut, K);
+    const int per_var = 1 + 2 * min(A.mcut, A.K);
     const int64_t row = row0 + (int64_t)(sys / A.nslots) * per_var + q;
-    const int n = gam_of(A, m).Min;
-    const double *c = A.rhs + (size_t)sys * A.nmax, *x = A.x + (size_t)sys * A.nmax;
-    const double *dv = A.dinv + (size_t)m * A.nmax;
+    double c[kPer], x[kPer], dv[kPer];
+    load_vec(c, A.rhs + (size_t)sys * A.nmax, n, lane);
+    load_vec(x, A.x + (size_t)sys * A.nmax, n, lane);
+    load_vec(dv, A.dinv + (size_t)m * A.nmax, n, lane);
     const double cn = A.cnorm[sys];
     const double s = cn > 0.0 ? 1.0 / cn : 0.0;
-    write_mlp_row(X + row * kMlpWidth, c, s, n, m, K);
-    for (int i = threadIdx.x; i < kMlpWidth; i += blockDim.x) {
-        float t = 0.f;
-        if (i < n) t = (float)((x[i] / dv[i] - c[i]) * s);
+    write_mlp_row_w(X + row * kMlpWidth, c, s, n, m, A.K, lane);
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+        const int i = lane + 32 * e;
+        const float t = i < n ? (float)((x[e] / dv[e] - c[e]) * s) : 0.f;
         T[row * kMlpWidth + i] = __float2bfloat16(t);
     }
-    if (threadIdx.x == 0) nrow[row] = n;
+    if (lane == 0) nrow[row] = n;
 }
 
 // ---------------------------------------------------------------- C ABI
@@ -573,8 +740,6 @@ extern "C" int32_t ss_problem_create(ss_grid *g, const double *k2, ss_problem **
         return SS_BAD_ARG;
     }
     cudaSetDevice(g->device);
-    ss_problem *p = new ss_problem();
-    p->g = g;
     const ss_grid_params &gp = g->p;
     const int iDim = (int)g->d.iDim;
     std::vector<double> kk(k2, k2 + iDim);
@@ -583,7 +748,13 @@ extern "C" int32_t ss_problem_create(ss_grid *g, const double *k2, ss_problem **
     SplineHost tpl[2];
     int32_t st = build_spline(gp.iMin, gp.iMax, gp.num_cells, gp.mubar, gp.quadrature, g->l_q[0], r1t1, r1t0, tpl[0]);
     if (!st) st = build_spline(gp.iMin, gp.iMax, gp.num_cells, gp.mubar, gp.quadrature, g->l_q[0], r1t0, r1t0, tpl[1]);
-    if (st) { delete p; return st; }
+    if (st) return st;
+    if (std::max(tpl[0].Min, tpl[1].Min) > kMaxN) {
+        set_error("radial systems of %d unknowns exceed %d", std::max(tpl[0].Min, tpl[1].Min), kMaxN);
+        return SS_BAD_SHAPE;
+    }
+    ss_problem *p = new ss_problem();
+    p->g = g;
     for (int t = 0; t < 2; t++) {
         const SplineHost &s = tpl[t];
         GammaDev &gd = p->gam[t];
@@ -606,40 +777,45 @@ extern "C" int32_t ss_problem_create(ss_grid *g, const double *k2, ss_problem **
             for (int j = std::max(0, i - 8); j < std::min(n, i + 9); j++)
                 if (Gs[m][(size_t)i * n + j] != 0.0) { kl = std::max(kl, i - j); ku = std::max(ku, j - i); }
     }
-    p->kl = std::max(kl, 1); p->ku = ku; p->wG = p->kl + ku + 1; p->wU = p->kl + ku + 1;
-    kl = p->kl;
+    if (kl > KL || ku > KU) {
+        delete p;
+        set_error("radial operator bandwidth (%d, %d) exceeds (3, 3)", kl, ku);
+        return SS_BAD_SHAPE;
+    }
+    p->kl = KL; p->ku = KU;
     const int nm = p->nmax, Kp = p->K + 1;
-    std::vector<double> hG((size_t)Kp * nm * p->wG, 0.0), hL((size_t)Kp * nm * kl, 0.0),
-        hU((size_t)Kp * nm * p->wU, 0.0), hD((size_t)Kp * nm, 1.0);
+    std::vector<double> hG((size_t)Kp * nm * WG, 0.0), hL((size_t)Kp * nm * KL, 0.0), hU((size_t)Kp * nm * WU, 0.0),
+        hD((size_t)Kp * nm, 1.0);
     std::vector<int> hP((size_t)Kp * nm, 0);
     for (int m = 0; m <= p->K; m++) {
         const int n = p->n[m == 0 ? 0 : 1];
         std::vector<double> &A = Gs[m];
         for (int i = 0; i < n; i++) {
-            for (int t = 0; t < p->wG; t++) {
-                const int j = i + t - kl;
-                if (j >= 0 && j < n) hG[((size_t)m * nm + i) * p->wG + t] = A[(size_t)i * n + j];
+            for (int t = 0; t < WG; t++) {
+                const int j = i + t - KL;
+                if (j >= 0 && j < n) hG[((size_t)m * nm + i) * WG + t] = A[(size_t)i * n + j];
             }
             const double d = A[(size_t)i * n + i];
             hD[(size_t)m * nm + i] = std::fabs(d) > 0.0 ? 1.0 / d : 1.0;
         }
-        // banded LU with partial pivoting (dgbtf2 order); U gains kl superdiagonals
+        // banded LU with partial pivoting (dgbtf2 order); U gains KL superdiagonals
         for (int k = 0; k < n; k++) {
             int piv = k;
             double mx = std::fabs(A[(size_t)k * n + k]);
-            for (int i = k + 1; i <= std::min(n - 1, k + kl); i++)
+            for (int i = k + 1; i <= std::min(n - 1, k + KL); i++)
                 if (std::fabs(A[(size_t)i * n + k]) > mx) { mx = std::fabs(A[(size_t)i * n + k]); piv = i; }
             if (mx == 0.0) { delete p; set_error("singular radial operator at wavenumber %d", m); return SS_NOT_SPD; }
             hP[(size_t)m * nm + k] = piv;
-            const int jend = std::min(n - 1, k + kl + ku);
+            const int jend = std::min(n - 1, k + KL + KU);
             if (piv != k)
                 for (int j = k; j <= jend; j++) std::swap(A[(size_t)k * n + j], A[(size_t)piv * n + j]);
-            for (int i = k + 1; i <= std::min(n - 1, k + kl); i++) {
+            for (int i = k + 1; i <= std::min(n - 1, k + KL); i++) {
                 const double l = A[(size_t)i * n + k] / A[(size_t)k * n + k];
-                hL[((size_t)m * nm + k) * kl + (i - k - 1)] = l;
+                hL[((size_t)m * nm + k) * KL + (i - k - 1)] = l;
                 for (int j = k + 1; j <= jend; j++) A[(size_t)i * n + j] -= l * A[(size_t)k * n + j];
             }
-            for (int t = 0; t < p->wU && k + t < n; t++) hU[((size_t)m * nm + k) * p->wU + t] = A[(size_t)k * n + k + t];
+            hU[((size_t)m * nm + k) * WU] = 1.0 / A[(size_t)k * n + k];  // the pivot, inverted
+            for (int t = 1; t < WU && k + t < n; t++) hU[((size_t)m * nm + k) * WU + t] = A[(size_t)k * n + k + t];
         }
         std::vector<double>().swap(A);
     }
@@ -680,7 +856,7 @@ extern "C" int32_t ss_problem_dims(const ss_problem *p, int32_t *nsys, int32_t *
     if (nsys) *nsys = p->nsys;
     if (nmax) *nmax = p->nmax;
     if (K) *K = p->K;
-    if (bandwidth) *bandwidth = p->wG;
+    if (bandwidth) *bandwidth = WG;
     return SS_OK;
 }
 
@@ -701,10 +877,9 @@ extern "C" int32_t ss_problem_operator_band(const ss_problem *p, int32_t m, doub
     if (!p || m < 0 || m > p->K) { set_error("wavenumber out of range"); return SS_BAD_ARG; }
     cudaSetDevice(p->g->device);
     if (n) *n = p->n[m == 0 ? 0 : 1];
-    if (kl) *kl = p->kl;
+    if (kl) *kl = KL;
     if (band)
-        CUDA_TRY(cudaMemcpy(band, p->d_G + (size_t)m * p->nmax * p->wG, (size_t)p->nmax * p->wG * 8,
-                            cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(band, p->d_G + (size_t)m * p->nmax * WG, (size_t)p->nmax * WG * 8, cudaMemcpyDeviceToHost));
     return SS_OK;
 }
 
@@ -714,37 +889,38 @@ static SolveArgs solve_args(ss_problem *p, int restart, int max_iter, double tol
     A.spec = (const double *)g->spec; A.spec_out = (double *)g->spec; A.gam = p->d_gam;
     A.G = p->d_G; A.Lm = p->d_Lm; A.U = p->d_U; A.dinv = p->d_dinv; A.piv = p->d_piv;
     A.rhs = p->d_rhs; A.x = p->d_x; A.res = p->d_res; A.cnorm = p->d_cnorm; A.iters = p->d_iters; A.state = p->d_state;
-    A.nspec = g->d.n_spectral; A.nslots = 1 + 2 * p->K; A.nvars = (int)g->d.nvars; A.nmax = p->nmax;
-    A.kl = p->kl; A.ku = p->ku; A.wG = p->wG; A.wU = p->wU; A.b = (int)g->d.b_iDim;
+    A.V = p->d_V; A.Z = p->d_Z; A.H = p->d_H; A.gv = p->d_gv; A.cs = p->d_cs; A.sn = p->d_sn; A.cyc = p->d_cyc;
+    A.mlp_in = p->d_mlp_in; A.mlp_out = p->d_mlp_out;
+    A.nspec = g->d.n_spectral; A.nsys = p->nsys; A.nslots = 1 + 2 * p->K; A.nvars = (int)g->d.nvars;
+    A.nmax = p->nmax; A.b = (int)g->d.b_iDim; A.K = p->K; A.mcut = p->mcut;
     A.restart = restart; A.max_iter = max_iter; A.tol = tol;
     return A;
 }
 
-static int32_t ensure_fg(ss_problem *p, int R) {
-    if (p->fg_restart >= R && p->d_V) return SS_OK;
+static int32_t ensure_workspace(ss_problem *p, int R) {
+    if (p->ws_restart >= R && p->d_V) return SS_OK;
     const size_t ns = p->nsys, nm = p->nmax;
     int32_t st;
     if ((st = palloc(p, (void **)&p->d_V, ns * (R + 1) * nm * 8)) || (st = palloc(p, (void **)&p->d_Z, ns * R * nm * 8)) ||
         (st = palloc(p, (void **)&p->d_H, ns * (R + 1) * R * 8)) || (st = palloc(p, (void **)&p->d_gv, ns * (R + 1) * 8)) ||
-        (st = palloc(p, (void **)&p->d_cs, ns * R * 8)) || (st = palloc(p, (void **)&p->d_sn, ns * R * 8)) ||
-        (st = palloc(p, (void **)&p->d_cyc, ns * 4)))
+        (st = palloc(p, (void **)&p->d_cs, ns * R * 8)) || (st = palloc(p, (void **)&p->d_sn, ns * R * 8)))
         return st;
-    p->mpad = (int)((ns + kMlpTileM - 1) / kMlpTileM * kMlpTileM);
-    if (!p->d_mlp_in &&
-        ((st = palloc(p, (void **)&p->d_mlp_in, (size_t)p->mpad * kMlpWidth * 2)) ||
-         (st = palloc(p, (void **)&p->d_mlp_out, (size_t)p->mpad * kMlpWidth * 4))))
-        return st;
-    p->fg_restart = R;
+    if (!p->d_cyc) {
+        p->mpad = (int)((ns + kMlpTileM - 1) / kMlpTileM * kMlpTileM);
+        if ((st = palloc(p, (void **)&p->d_cyc, ns * 4)) ||
+            (st = palloc(p, (void **)&p->d_mlp_in, (size_t)p->mpad * kMlpWidth * 2)) ||
+            (st = palloc(p, (void **)&p->d_mlp_out, (size_t)p->mpad * kMlpWidth * 4)))
+            return st;
+    }
+    p->ws_restart = R;
     return SS_OK;
 }
 
-static size_t gmres_smem(int R, int n) {
-    return ((size_t)(R + 1) * n + 2 * (size_t)n + (size_t)(R + 1) * R + 4 * (size_t)R + 4) * 8;
-}
+static inline unsigned warp_blocks(int nsys) { return (unsigned)((nsys + kSysPerBlock - 1) / kSysPerBlock); }
 
-static int32_t run_gmres(ss_problem *p, SolveArgs A, cudaStream_t st) {
+static int32_t run_gmres(ss_problem *p, const SolveArgs &A, cudaStream_t st) {
     const size_t smem = gmres_smem(A.restart, p->nmax);
-    if (smem > 200 * 1024) { set_error("restart too long for shared memory"); return SS_BAD_ARG; }
+    if (smem > 200 * 1024) { set_error("restart %d too long for shared memory", A.restart); return SS_BAD_ARG; }
     if (smem > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(gmres_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     gmres_kernel<<<p->nsys, 128, smem, st>>>(A);
     CUDA_TRY(cudaGetLastError());
@@ -754,16 +930,16 @@ static int32_t run_gmres(ss_problem *p, SolveArgs A, cudaStream_t st) {
 // the chosen backend on the right-hand sides already in d_rhs (no transforms)
 static int32_t solve_systems(ss_problem *p, int method, SolveArgs A, cudaStream_t st, int *fallback) {
     const int ns = p->nsys;
+    const unsigned nb = warp_blocks(ns);
     int32_t r;
     *fallback = 0;
     CUDA_TRY(cudaMemsetAsync(p->d_iters, 0, (size_t)ns * 4, st));
     CUDA_TRY(cudaMemsetAsync(p->d_state, 0, (size_t)ns * 4, st));
-    const size_t wsm = (size_t)p->nmax * 8;
     if (method == SS_SOLVER_DIRECT) {
         A.masked = 0;
-        direct_kernel<<<(ns + 63) / 64, 64, 0, st>>>(A);
+        direct_kernel<<<nb, 128, 0, st>>>(A);
         CUDA_TRY(cudaGetLastError());
-        residual_kernel<<<ns, 128, wsm, st>>>(A);
+        residual_kernel<<<nb, 128, 0, st>>>(A);
         CUDA_TRY(cudaGetLastError());
         return SS_OK;
     }
@@ -772,28 +948,24 @@ static int32_t solve_systems(ss_problem *p, int method, SolveArgs A, cudaStream_
         return run_gmres(p, A, st);
     }
     // flexible GMRES with the learned preconditioner, cycles in lockstep
-    if ((r = ensure_fg(p, A.restart))) return r;
     if ((r = mlp_reserve(p->mlp, p->mpad))) return r;
     CUDA_TRY(cudaMemsetAsync(p->d_x, 0, (size_t)ns * p->nmax * 8, st));
-    FgArgs F{};
-    F.S = A; F.V = p->d_V; F.Z = p->d_Z; F.H = p->d_H; F.gv = p->d_gv; F.cs = p->d_cs; F.sn = p->d_sn;
-    F.cyc = p->d_cyc; F.mlp_in = p->d_mlp_in; F.mlp_out = p->d_mlp_out; F.K = p->K; F.mcut = p->mcut;
-    fg_begin_kernel<<<ns, 128, wsm, st>>>(F);
+    fg_begin_kernel<<<nb, 128, 0, st>>>(A);
     CUDA_TRY(cudaGetLastError());
     int done_iters = 0;
     std::vector<int> hstate(ns);
     while (done_iters < A.max_iter) {
         const int steps = std::min(A.restart, A.max_iter - done_iters);
         for (int j = 0; j < steps; j++) {
-            F.j = j;
+            A.j = j;
             if ((r = mlp_forward(p->mlp, p->d_mlp_in, p->d_mlp_out, p->mpad, st))) return r;
-            fg_step_kernel<<<ns, 128, wsm, st>>>(F);
+            fg_step_kernel<<<nb, 128, 0, st>>>(A);
             CUDA_TRY(cudaGetLastError());
         }
-        fg_end_kernel<<<ns, 128, 0, st>>>(F);
+        fg_end_kernel<<<nb, 128, 0, st>>>(A);
         CUDA_TRY(cudaGetLastError());
         done_iters += steps;
-        fg_begin_kernel<<<ns, 128, wsm, st>>>(F);  // true residual: converged systems leave, others restart
+        fg_begin_kernel<<<nb, 128, 0, st>>>(A);  // true residual: converged systems leave, others restart
         CUDA_TRY(cudaGetLastError());
         CUDA_TRY(cudaMemcpyAsync(hstate.data(), p->d_state, (size_t)ns * 4, cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
@@ -810,10 +982,10 @@ static int32_t solve_systems(ss_problem *p, int method, SolveArgs A, cudaStream_
         *fallback = left;
         A.warm = 1; A.masked = 1;
         if ((r = run_gmres(p, A, st))) return r;
-        direct_kernel<<<(ns + 63) / 64, 64, 0, st>>>(A);
+        direct_kernel<<<nb, 128, 0, st>>>(A);
         CUDA_TRY(cudaGetLastError());
     }
-    residual_kernel<<<ns, 128, wsm, st>>>(A);
+    residual_kernel<<<nb, 128, 0, st>>>(A);
     CUDA_TRY(cudaGetLastError());
     return SS_OK;
 }
@@ -824,21 +996,22 @@ extern "C" int32_t ss_solve(ss_problem *p, int32_t method, double tol, int32_t m
     if (method < SS_SOLVER_DIRECT || method > SS_SOLVER_FGMRES_MLP) { set_error("unknown solver"); return SS_BAD_ARG; }
     if (!(tol > 0.0)) { set_error("tolerance must be positive"); return SS_BAD_ARG; }
     if (restart < 1) restart = 30;
-    if (restart > 100) { set_error("restart must be <= 100"); return SS_BAD_ARG; }
+    if (restart > kMaxRestart) { set_error("restart must be <= %d", kMaxRestart); return SS_BAD_ARG; }
     if (max_iter < 1) max_iter = 2000;
     if (method == SS_SOLVER_FGMRES_MLP && !p->mlp) { set_error("no MLP preconditioner attached"); return SS_BAD_ARG; }
     ss_grid *g = p->g;
     cudaSetDevice(g->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
-    int32_t r = grid_forward(g, st);  // f (physical slot 1) → spectral B-vectors
-    if (r) return r;
+    int32_t r;
+    if (method != SS_SOLVER_DIRECT && (r = ensure_workspace(p, restart))) return r;
+    if ((r = grid_forward(g, st))) return r;  // f (physical slot 1) → spectral B-vectors
     SolveArgs A = solve_args(p, restart, max_iter, tol);
     CUDA_TRY(cudaEventRecord(p->e0, st));
-    rhs_kernel<<<(p->nsys + 127) / 128, 128, 0, st>>>(A);
+    rhs_kernel<<<warp_blocks(p->nsys), 128, 0, st>>>(A);
     CUDA_TRY(cudaGetLastError());
     int fallback = 0;
     if ((r = solve_systems(p, method, A, st, &fallback))) return r;
-    unfold_kernel<<<(p->nsys + 127) / 128, 128, 0, st>>>(A);
+    unfold_kernel<<<warp_blocks(p->nsys), 128, 0, st>>>(A);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(p->e1, st));
     if ((r = grid_inverse_coeffs(g, st))) return r;  // a → u and its derivatives in the physical slots
@@ -882,6 +1055,12 @@ extern "C" int32_t ss_problem_export(const ss_problem *p, double *rhs, double *x
     return SS_OK;
 }
 
+static int32_t check_training_args(ss_problem *p, ss_mlp *mlp) {
+    if (p->nmax > kMlpWidth - 2) { set_error("radial systems exceed the network width"); return SS_BAD_SHAPE; }
+    if (mlp->device != p->g->device) { set_error("network and grid on different devices"); return SS_BAD_ARG; }
+    return SS_OK;
+}
+
 // Training pairs from the direct solve: for each field (blobs[offsets[f] ..
 // offsets[f+1]) as (xc, yc, w, A) quadruples) the field is evaluated on the
 // device at the gridpoints `pts` (n_physical × 2: r then λ), transformed,
@@ -890,15 +1069,14 @@ extern "C" int32_t ss_problem_export(const ss_problem *p, double *rhs, double *x
 extern "C" int32_t ss_problem_collect_training(ss_problem *p, ss_mlp *mlp, const double *pts, const double *blobs,
                                                const int32_t *offsets, int32_t nfields, int32_t max_wavenumber) {
     if (!p || !mlp || !blobs || !offsets || nfields < 0) { set_error("bad argument"); return SS_BAD_ARG; }
-    if (p->nmax > kMlpWidth - 2) { set_error("radial systems exceed the network width"); return SS_BAD_SHAPE; }
-    if (mlp->device != p->g->device) { set_error("network and grid on different devices"); return SS_BAD_ARG; }
+    int32_t r;
+    if ((r = check_training_args(p, mlp))) return r;
     for (int f = 0; f < nfields; f++)
         if (offsets[f + 1] < offsets[f] || offsets[f] < 0) { set_error("blob offsets decrease"); return SS_BAD_ARG; }
     ss_grid *g = p->g;
     cudaSetDevice(g->device);
     cudaStream_t st = g->stream;
     const int64_t np = g->d.n_physical;
-    int32_t r;
     if (pts) {
         if (!p->d_pts && (r = palloc(p, (void **)&p->d_pts, (size_t)np * 16))) return r;
         CUDA_TRY(cudaMemcpy(p->d_pts, pts, (size_t)np * 16, cudaMemcpyHostToDevice));
@@ -915,17 +1093,49 @@ extern "C" int32_t ss_problem_collect_training(ss_problem *p, ss_mlp *mlp, const
     if ((r = mlp_dataset_reserve(mlp, mlp->ds_rows + (int64_t)nfields * per_field))) return r;
     SolveArgs A = solve_args(p, 1, 1, 1.0);
     A.masked = 0;
+    A.mcut = mcut;
+    const unsigned nb = warp_blocks(p->nsys);
     for (int f = 0; f < nfields; f++) {
-        const int nb = offsets[f + 1] - offsets[f];
+        const int cnt = offsets[f + 1] - offsets[f];
         blob_field_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>((double *)g->phys, np, (int)g->d.nvars, p->d_pts,
-                                                                         p->d_blobs + 4 * (size_t)offsets[f], nb);
+                                                                         p->d_blobs + 4 * (size_t)offsets[f], cnt);
         CUDA_TRY(cudaGetLastError());
         if ((r = grid_forward(g, st))) return r;
-        rhs_kernel<<<(p->nsys + 127) / 128, 128, 0, st>>>(A);
-        direct_kernel<<<(p->nsys + 63) / 64, 64, 0, st>>>(A);
-        training_rows_kernel<<<p->nsys, 128, 0, st>>>(A, p->K, mcut, mlp->ds_rows, mlp->ds_X, mlp->ds_T, mlp->ds_n);
+        rhs_kernel<<<nb, 128, 0, st>>>(A);
+        direct_kernel<<<nb, 128, 0, st>>>(A);
+        training_rows_kernel<<<nb, 128, 0, st>>>(A, mlp->ds_rows, mlp->ds_X, mlp->ds_T, mlp->ds_n);
         CUDA_TRY(cudaGetLastError());
         mlp->ds_rows += per_field;
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return SS_OK;
+}
+
+// Training pairs on random right-hand sides: `nsets` sets of one white-noise
+// vector per radial system (smoothed `smooth` times by (1, 2, 1)/4), each
+// solved directly; they widen the inputs beyond forcing-shaped vectors toward
+// the Arnoldi vectors the flexible solve hands the network.
+extern "C" int32_t ss_problem_collect_random(ss_problem *p, ss_mlp *mlp, int32_t nsets, uint64_t seed, int32_t smooth,
+                                             int32_t max_wavenumber) {
+    if (!p || !mlp || nsets < 0 || smooth < 0) { set_error("bad argument"); return SS_BAD_ARG; }
+    int32_t r;
+    if ((r = check_training_args(p, mlp))) return r;
+    ss_grid *g = p->g;
+    cudaSetDevice(g->device);
+    cudaStream_t st = g->stream;
+    const int mcut = max_wavenumber < 0 ? p->K : std::min(max_wavenumber, p->K);
+    const int per_set = (int)g->d.nvars * (1 + 2 * mcut);
+    if ((r = mlp_dataset_reserve(mlp, mlp->ds_rows + (int64_t)nsets * per_set))) return r;
+    SolveArgs A = solve_args(p, 1, 1, 1.0);
+    A.masked = 0;
+    A.mcut = mcut;
+    const unsigned nb = warp_blocks(p->nsys);
+    for (int s = 0; s < nsets; s++) {
+        rhs_random_kernel<<<nb, 128, 0, st>>>(A, seed * 0x100000001B3ull + (uint64_t)s, smooth);
+        direct_kernel<<<nb, 128, 0, st>>>(A);
+        training_rows_kernel<<<nb, 128, 0, st>>>(A, mlp->ds_rows, mlp->ds_X, mlp->ds_T, mlp->ds_n);
+        CUDA_TRY(cudaGetLastError());
+        mlp->ds_rows += per_set;
     }
     CUDA_TRY(cudaStreamSynchronize(st));
     return SS_OK;

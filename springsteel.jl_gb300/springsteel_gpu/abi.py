@@ -156,6 +156,7 @@ EXPORTED = [
     "ss_tile_sum_spectral", "ss_tile_copy_physical", "ss_grid_zero_spectral",
     "ss_problem_create", "ss_problem_destroy", "ss_problem_dims", "ss_problem_operator_band",
     "ss_problem_set_mlp", "ss_solve", "ss_problem_export", "ss_problem_collect_training",
+    "ss_problem_collect_random",
     "ss_mlp_create", "ss_mlp_destroy", "ss_mlp_set_params", "ss_mlp_get_params", "ss_mlp_forward",
     "ss_mlp_gradients", "ss_mlp_dataset_rows", "ss_mlp_dataset_clear", "ss_mlp_train",
 ]
@@ -226,6 +227,7 @@ def bind(lib):
         "ss_solve": ([vp, i32, C.c_double, i32, i32, C.POINTER(ss_solve_stats), vp], i32),
         "ss_problem_export": ([vp, vp, vp, vp, vp], i32),
         "ss_problem_collect_training": ([vp, vp, vp, vp, vp, i32, i32], i32),
+        "ss_problem_collect_random": ([vp, vp, i32, C.c_uint64, i32, i32], i32),
         "ss_mlp_create": ([i32, C.c_uint64, C.POINTER(vp)], i32),
         "ss_mlp_destroy": ([vp], i32),
         "ss_mlp_set_params": ([vp, vp, vp], i32),

@@ -173,6 +173,12 @@ class SpringsteelProblem:
         _check(load_library().ss_problem_collect_training(self.handle, mlp.handle, _ptr(pts), _ptr(blobs), _ptr(offs),
                                                           len(blob_lists), int(max_wavenumber)))
 
+    def collect_random(self, mlp, nsets, seed=0, smooth=0, max_wavenumber=-1):
+        """Append direct solutions of seeded random right-hand sides (one per radial system
+        per set, smoothed ``smooth`` times) to the network's training set."""
+        _check(load_library().ss_problem_collect_random(self.handle, mlp.handle, int(nsets), int(seed), int(smooth),
+                                                        int(max_wavenumber)))
+
 
 def solve(problem, method=None, tol=None, maxiter=None, restart=None, stream=None):
     """solve!(problem): f in physical slot 1 → u (all derivative slots); returns the solve statistics."""
