@@ -244,6 +244,8 @@ static int32_t build_grid(ss_grid *g) {
         int dev = g->device;
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || g->sms <= 0)
+            g->sms = 152;
         int i = 0;
         while (i < iDim) {
             RingBucket bkt{};
@@ -253,8 +255,8 @@ static int32_t build_grid(ss_grid *g) {
             while (j < iDim && bufof(order[j]) * 2 > top) j++;
             bkt.count = j - i;
             bkt.max_buf = top;
-            int km = 0;
-            for (int q = i; q < j; q++) km = std::max(km, rings[order[q]].kmax);
+            int km = 0;  // the inverse kernel keeps ri + 1 ≥ kmax + 1 spectrum entries per item
+            for (int q = i; q < j; q++) km = std::max(km, std::max(rings[order[q]].kmax, rings[order[q]].ri));
             bkt.max_kmax = km;
             bkt.smem_fwd_f64 = size_t(2) * top * 16;
             bkt.smem_inv_f64 = (size_t(2) * top + km + 1) * 16;
@@ -287,6 +289,53 @@ static int32_t build_grid(ss_grid *g) {
             if ((st = upload_bytes(g, &cd.inv_o_t, real_layout(ch.inv_o, g->tl)))) return st;
             if ((st = upload_bytes(g, &cd.gu_t, real_layout(ch.gu, g->tl)))) return st;
             if ((st = upload_bytes(g, &cd.gv_t, real_layout(ch.gv, g->tl)))) return st;
+            {
+                const int N = ch.N, half = ch.half, ne = (N + 1) / 2, no = std::max(N / 2, 1);
+                const int JP = cheb_pad4(half), KEP = cheb_pad4((ch.bk + 1) / 2), KOP = cheb_pad4(ch.bk / 2);
+                std::vector<double> et((size_t)ne * JP, 0.0), ot((size_t)no * JP, 0.0);
+                std::vector<double> fe((size_t)half * KEP, 0.0), fo((size_t)half * KOP, 0.0);
+                for (int j = 0; j < half; j++) {
+                    for (int k = 0; k < ne; k++) et[(size_t)k * JP + j] = ch.inv_e[(size_t)j * ne + k];
+                    if (N / 2 > 0)
+                        for (int k = 0; k < no; k++) ot[(size_t)k * JP + j] = ch.inv_o[(size_t)j * no + k];
+                    for (int i = 0; 2 * i < ch.bk; i++) fe[(size_t)j * KEP + i] = ch.fwd[(size_t)(2 * i) * half + j];
+                    for (int i = 0; 2 * i + 1 < ch.bk; i++) fo[(size_t)j * KOP + i] = ch.fwd[(size_t)(2 * i + 1) * half + j];
+                }
+                if ((st = upload_bytes(g, &cd.inv_et_t, real_layout(et, g->tl)))) return st;
+                if ((st = upload_bytes(g, &cd.inv_ot_t, real_layout(ot, g->tl)))) return st;
+                if ((st = upload_bytes(g, &cd.fwd_et_t, real_layout(fe, g->tl)))) return st;
+                if ((st = upload_bytes(g, &cd.fwd_ot_t, real_layout(fo, g->tl)))) return st;
+                // composed inverse matrices: X_0 = G (CA), X_d = D X_{d-1} / dscale (CIxcoefficients)
+                const int B = ch.bk;
+                std::vector<double> X((size_t)N * B, 0.0), Xn((size_t)N * B, 0.0);
+                for (int k = 0; k < N; k++)
+                    for (int i = 0; i < B; i++) {
+                        double val = (k == i) ? 1.0 : 0.0;
+                        for (int p = 0; p < ch.nrank; p++) val += ch.gv[(size_t)p * N + k] * ch.gu[(size_t)p * B + i];
+                        X[(size_t)k * B + i] = val;
+                    }
+                std::vector<double> mt((size_t)6 * B * JP, 0.0);
+                for (int dd = 0; dd < 3; dd++) {
+                    if (dd > 0) {
+                        for (int k = 0; k < N; k++)
+                            for (int i = 0; i < B; i++) {
+                                double acc = 0.0;  // (D X)[k][i] = Σ_{m > k, m − k odd} 2m X[m][i]
+                                for (int m = k + 1; m < N; m += 2) acc += 2.0 * m * X[(size_t)m * B + i];
+                                Xn[(size_t)k * B + i] = acc / ch.dscale;
+                            }
+                        X.swap(Xn);
+                    }
+                    for (int j = 0; j < half; j++)
+                        for (int i = 0; i < B; i++) {
+                            double se = 0.0, so = 0.0;
+                            for (int k = 0; k < N; k += 2) se += ch.inv_e[(size_t)j * ne + k / 2] * X[(size_t)k * B + i];
+                            for (int k = 1; k < N; k += 2) so += ch.inv_o[(size_t)j * no + k / 2] * X[(size_t)k * B + i];
+                            mt[((size_t)(dd * 2 + 0) * B + i) * JP + j] = se;
+                            mt[((size_t)(dd * 2 + 1) * B + i) * JP + j] = so;
+                        }
+                }
+                if ((st = upload_bytes(g, &cd.inv_m_t, real_layout(mt, g->tl)))) return st;
+            }
         }
         if ((st = upload_vec(g, &g->d_cheb, cdev))) return st;
     }
@@ -323,7 +372,7 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
         const int N = (int)d.kDim, half = (N + 1) / 2;
         size_t smem = (size_t(64) * (N | 1) + size_t(bk) * half) * sizeof(T);
         StageScope sc(g, SS_STAGE_CHEB_FWD, st);
-        CUDA_TRY((launch_cheb_forward<P, T>(Cl, smem, st)));
+        CUDA_TRY((launch_cheb_forward<P, T>(Cl, smem, st, N)));
         g->launches[SS_STAGE_CHEB_FWD]++;
     }
     RingLaunch L{};
@@ -340,6 +389,7 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
         for (const RingBucket &bkt : g->buckets) {
             L.ring_list = g->d_ring_list + bkt.offset;
             size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
+            L.ib = ring_batch(smem, g->nitems, bkt.count, 4 * g->sms, g->ring_threads_fwd, bkt.max_buf);
             CUDA_TRY((launch_ring_forward<P, T>(L, bkt.count, g->nitems, smem, g->ring_threads_fwd, st)));
             g->launches[SS_STAGE_RING_FWD]++;
         }
@@ -392,6 +442,7 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st, int coeffs = 0) {
         for (const RingBucket &bkt : g->buckets) {
             L.ring_list = g->d_ring_list + bkt.offset;
             size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
+            L.ib = ring_batch(sm, g->nitems, bkt.count, 4 * g->sms, g->ring_threads_inv, bkt.max_buf);
             CUDA_TRY((launch_ring_inverse<P, T>(L, bkt.count, g->nitems, sm, g->ring_threads_inv, st)));
             g->launches[SS_STAGE_RING_INV]++;
         }
@@ -403,7 +454,7 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st, int coeffs = 0) {
         const int N = (int)d.kDim, half = (N + 1) / 2, ne = (N + 1) / 2, no = std::max(N / 2, 1);
         size_t sm = (size_t(128) * (N | 1) + size_t(half) * ne + size_t(half) * no + size_t(64) * (bk | 1)) * sizeof(T);
         StageScope sc(g, SS_STAGE_CHEB_INV, st);
-        CUDA_TRY((launch_cheb_inverse<P, T>(Cl, sm, st)));
+        CUDA_TRY((launch_cheb_inverse<P, T>(Cl, sm, st, N)));
         g->launches[SS_STAGE_CHEB_INV]++;
     }
     return SS_OK;

@@ -8,6 +8,10 @@
 // by Bluestein's chirp-z convolution of smooth length M >= 2N-1 whose two FFTs
 // are again Stockham passes.  Twiddles come from FP64-accurate tables built on
 // the host (ss_setup.cpp), stored in the compute type's layout.
+//
+// Every routine transforms a batch of `nb` independent sequences of the same
+// plan, `bs` complex entries apart in shared memory: one barrier per pass
+// serves the whole batch, and every thread loops over (sequence, index) pairs.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -72,17 +76,32 @@ __device__ __forceinline__ void dft_small(cpx<T> *v) {
     }
 }
 
-// One Stockham pass: Ns = product of the radices already applied.
+// j / d for 0 ≤ j < 2^22 and d ≥ 1 via a float reciprocal and one correction
+// (the quotient estimate is off by at most one), instead of an integer division
+__device__ __forceinline__ int div_small(int j, int d, float inv_d) {
+    int q = __float2int_rz((float)j * inv_d);
+    if (q * d > j) q--;
+    else if ((q + 1) * d <= j) q++;
+    return q;
+}
+
+// One Stockham pass over the batch: Ns = product of the radices already applied.
 template <int R, int SIGN, typename T>
 __device__ __forceinline__ void stockham_pass(const cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N,
-                                              int Ns, const void *__restrict__ tw) {
+                                              int Ns, const void *__restrict__ tw, int nb, int bs) {
     const int NR = N / R;
     const int tstride = N / (Ns * R);
-    for (int j = threadIdx.x; j < NR; j += blockDim.x) {
-        const int k = j % Ns;
+    const int total = nb * NR;
+    const float inv_ns = 1.0f / (float)Ns;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int bi = nb == 1 ? 0 : t / NR, j = t - bi * NR;  // no division for a single sequence
+        const cpx<T> *s = src + (size_t)bi * bs;
+        cpx<T> *d = dst + (size_t)bi * bs;
+        const int jq = div_small(j, Ns, inv_ns);
+        const int k = j - jq * Ns;
         cpx<T> v[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = src[j + r * NR];
+        for (int r = 0; r < R; r++) v[r] = s[j + r * NR];
         if (k > 0) {
             const int step = tstride * k;
 #pragma unroll
@@ -93,9 +112,9 @@ __device__ __forceinline__ void stockham_pass(const cpx<T> *__restrict__ src, cp
             }
         }
         dft_small<R, SIGN>(v);
-        const int idxD = (j / Ns) * Ns * R + k;
+        const int idxD = jq * Ns * R + k;
 #pragma unroll
-        for (int r = 0; r < R; r++) dst[idxD + r * Ns] = v[r];
+        for (int r = 0; r < R; r++) d[idxD + r * Ns] = v[r];
     }
 }
 
@@ -106,18 +125,18 @@ __device__ __forceinline__ const void *tab_at(const void *pool, int64_t off) {
 
 // Stockham DFT over ping-pong buffers; returns the buffer holding the result.
 template <int SIGN, typename T>
-__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw) {
+__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int nb, int bs) {
     int Ns = 1;
     for (int s = 0; s < nrad; s++) {
         const int R = rad[s];
         switch (R) {
-        case 4: stockham_pass<4, SIGN>(a, b, N, Ns, tw); break;
-        case 2: stockham_pass<2, SIGN>(a, b, N, Ns, tw); break;
-        case 3: stockham_pass<3, SIGN>(a, b, N, Ns, tw); break;
-        case 5: stockham_pass<5, SIGN>(a, b, N, Ns, tw); break;
-        case 7: stockham_pass<7, SIGN>(a, b, N, Ns, tw); break;
-        case 11: stockham_pass<11, SIGN>(a, b, N, Ns, tw); break;
-        case 13: stockham_pass<13, SIGN>(a, b, N, Ns, tw); break;
+        case 4: stockham_pass<4, SIGN>(a, b, N, Ns, tw, nb, bs); break;
+        case 2: stockham_pass<2, SIGN>(a, b, N, Ns, tw, nb, bs); break;
+        case 3: stockham_pass<3, SIGN>(a, b, N, Ns, tw, nb, bs); break;
+        case 5: stockham_pass<5, SIGN>(a, b, N, Ns, tw, nb, bs); break;
+        case 7: stockham_pass<7, SIGN>(a, b, N, Ns, tw, nb, bs); break;
+        case 11: stockham_pass<11, SIGN>(a, b, N, Ns, tw, nb, bs); break;
+        case 13: stockham_pass<13, SIGN>(a, b, N, Ns, tw, nb, bs); break;
         default: break;
         }
         __syncthreads();
@@ -129,35 +148,44 @@ __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nra
     return a;
 }
 
-// Length-N DFT of the N values in `a` (sign SIGN).  Both buffers hold
-// fft_buffer_len(plan) entries.  Returns the buffer with the N results.
+// Length-N DFTs of the nb sequences in `a` (sign SIGN), sequence i at a + i·bs.
+// Both buffers hold nb × fft_buffer_len(plan) entries (bs ≥ that length).
+// Returns the buffer with the results, laid out like the input.
 template <int SIGN, typename T>
-__device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool) {
-    if (!p.blu) return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw));
+__device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool, int nb = 1, int bs = 0) {
+    if (!p.blu) return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw), nb, bs);
     const int N = p.N, M = p.M;
     const void *chirp = tab_at<T>(pool, p.chirp);
     const void *filt = tab_at<T>(pool, p.filt);
     // X_k = c_k Σ_j (x_j c_j) conj(c_{k-j}) with c_k = exp(-πi k²/N); the
     // inverse DFT is conj(forward(conj x)).
-    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    for (int t = threadIdx.x; t < nb * M; t += blockDim.x) {
+        const int bi = nb == 1 ? 0 : t / M, k = t - bi * M;
+        cpx<T> *ab = a + (size_t)bi * bs;
         cpx<T> v = c_zero<T>();
         if (k < N) {
-            v = a[k];
+            v = ab[k];
             if (SIGN > 0) v.y = -v.y;
             v = c_mul(v, ld_cplx<T>(chirp, k));
         }
-        a[k] = v;
+        ab[k] = v;
     }
     __syncthreads();
-    cpx<T> *r = stockham<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw));
-    for (int k = threadIdx.x; k < M; k += blockDim.x) r[k] = c_mul(r[k], ld_cplx<T>(filt, k));
+    cpx<T> *r = stockham<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
+    for (int t = threadIdx.x; t < nb * M; t += blockDim.x) {
+        const int bi = nb == 1 ? 0 : t / M, k = t - bi * M;
+        cpx<T> *rb = r + (size_t)bi * bs;
+        rb[k] = c_mul(rb[k], ld_cplx<T>(filt, k));
+    }
     __syncthreads();
     cpx<T> *other = (r == a) ? b : a;
-    cpx<T> *q = stockham<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw));
-    for (int k = threadIdx.x; k < N; k += blockDim.x) {
-        cpx<T> v = c_mul(q[k], ld_cplx<T>(chirp, k));
+    cpx<T> *q = stockham<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
+    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
+        const int bi = nb == 1 ? 0 : t / N, k = t - bi * N;
+        cpx<T> *qb = q + (size_t)bi * bs;
+        cpx<T> v = c_mul(qb[k], ld_cplx<T>(chirp, k));
         if (SIGN > 0) v.y = -v.y;
-        q[k] = v;
+        qb[k] = v;
     }
     __syncthreads();
     return q;

@@ -45,6 +45,7 @@ struct ss_grid {
     double *d_ahat = nullptr, *d_fw = nullptr, *d_cw = nullptr;
     int filtered = 0;
     int ring_threads_fwd = 256, ring_threads_inv = 256;  // CTA size of the ring kernels (autotuned by batches)
+    int sms = 152;                                        // SMs of the grid's device
     std::vector<RingBucket> buckets;
     std::vector<void *> allocs;
     std::vector<SplineHost> spl_host;

@@ -87,7 +87,20 @@ struct ChebDev {
     const void *inv_o_t;  // half_out × no: inverse DCT-I, odd-k columns
     const void *gu_t;     // nrank × bk   (Γ = Σ u vᵀ restricted to the first bk rows)
     const void *gv_t;     // nrank × N
+    // the same tables transposed and zero-padded to multiples of 4 for the
+    // register-tiled kernels (coalesced loads, 16-byte aligned rows)
+    const void *inv_et_t;  // ne × JP,   JP  = 4⌈half/4⌉:  inv_e[j][k] at [k][j]
+    const void *inv_ot_t;  // no × JP
+    const void *fwd_et_t;  // half × KEP, KEP = 4⌈⌈bk/2⌉/4⌉: fwd[2i][j] at [j][i]
+    const void *fwd_ot_t;  // half × KOP, KOP = 4⌈⌊bk/2⌋/4⌉: fwd[2i+1][j] at [j][i]
+    // CA, the CIx recurrence D (÷ dscale) and the folded DCT-I composed:
+    // u = M_d b for derivative order d = 0, 1, 2; even/odd halves
+    // Me_d[j][i] = Σ_{k even} IE[j][k/2] (D^d G)[k][i], Mo_d likewise over odd k,
+    // u[j] = (Me b)[j] + (Mo b)[j], u[N-1-j] = (Me b)[j] − (Mo b)[j]; stored
+    // transposed as [d][e/o][i < bk][JP]
+    const void *inv_m_t;
 };
+SS_HD inline int cheb_pad4(int n) { return n > 0 ? (n + 3) / 4 * 4 : 4; }
 
 enum { BC_R0 = 0, BC_A1 = 1, BC_A2 = 2, BC_PER = 3, BC_R3 = 4 };
 

@@ -59,37 +59,57 @@ void fft_init_constants() {
     if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
+// Resident 256-thread CTAs the ring kernels are compiled for: binary32 butterflies
+// fit 64 registers (4 CTAs per SM); binary64 and double-float need more.
+template <typename T>
+constexpr int kRingMinBlocks = std::is_same<T, float>::value ? 4 : 2;
+
 // ====================================================================
-// ring_forward: one CTA per (ring, item); item = v*bk + zb
+// ring_forward: one CTA per (ring, batch of up to L.ib items); item = v*bk + zb
+// (RLZ) or v (RL).  The items of a batch share the ring's plan and twiddles;
+// their sequences sit `buf` complex entries apart in each ping-pong buffer.
 // ====================================================================
 template <typename P, typename T>
-__global__ void __launch_bounds__(256) ring_forward_kernel(RingLaunch L) {
+__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(RingLaunch L) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int kmx[kRingBatchMax];
     const int ring = L.ring_list[blockIdx.x];
-    const int item = blockIdx.y;
-    const int vv = L.rlz ? item / L.bk : item;
-    const RingDesc rd = L.rings[(size_t)vv * L.ring_var_stride + ring];
+    const int item0 = blockIdx.y * L.ib;
+    const int nb = min(L.ib, L.nitems - item0);
+    const RingDesc rd = L.rings[(size_t)(L.rlz ? 0 : item0) * L.ring_var_stride + ring];
     const FftPlan &pl = L.plans[rd.plan];
     const int buf = fft_buffer_len(pl);
     cpx<T> *A = reinterpret_cast<cpx<T> *>(smem_raw);
-    cpx<T> *B = A + buf;
+    cpx<T> *B = A + (size_t)L.ib * buf;
+    __shared__ int64_t ioff[kRingBatchMax];  // element offset of each item's ring in the input
     const int Lr = rd.L, N = Lr / 2;
-
-    if (L.rlz) {
-        const int v = item / L.bk, zb = item % L.bk;
-        const T *in = (const T *)L.in + (size_t)v * L.bk * L.jDim + (size_t)L.bk * rd.jofs + (size_t)zb * Lr;
-        for (int n = threadIdx.x; n < N; n += blockDim.x) A[n] = {in[2 * n], in[2 * n + 1]};
-    } else {
-        const P *in = (const P *)L.in + (size_t)item * L.in_item_stride + rd.jofs;
-        for (int n = threadIdx.x; n < N; n += blockDim.x)
-            A[n] = {to_compute<T>(in[2 * n]), to_compute<T>(in[2 * n + 1])};
+    if (threadIdx.x < nb) {
+        const int item = item0 + threadIdx.x;
+        kmx[threadIdx.x] = L.rings[(size_t)(L.rlz ? 0 : item) * L.ring_var_stride + ring].kmax;
+        ioff[threadIdx.x] = L.rlz ? (int64_t)(item / L.bk) * L.bk * L.jDim + (int64_t)L.bk * rd.jofs +
+                                        (int64_t)(item % L.bk) * Lr
+                                  : (int64_t)item * L.in_item_stride + rd.jofs;
     }
     __syncthreads();
-    cpx<T> *Z = dft<-1, T>(A, B, pl, L.pool);
+    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
+        const int b = nb == 1 ? 0 : t / N, n = t - b * N;
+        if (L.rlz) {
+            const T *in = (const T *)L.in + ioff[b];
+            A[(size_t)b * buf + n] = {in[2 * n], in[2 * n + 1]};
+        } else {
+            const P *in = (const P *)L.in + ioff[b];
+            A[(size_t)b * buf + n] = {to_compute<T>(in[2 * n]), to_compute<T>(in[2 * n + 1])};
+        }
+    }
+    __syncthreads();
+    cpx<T> *Zb = dft<-1, T>(A, B, pl, L.pool, nb, buf);
 
-    T *out = (T *)L.out + (size_t)item * L.frows + rd.fofs;
     const T invL = T(1.0f) / T((float)Lr);
-    for (int k = threadIdx.x; k <= rd.ri; k += blockDim.x) {
+    const int nk = rd.ri + 1;
+    for (int t = threadIdx.x; t < nb * nk; t += blockDim.x) {
+        const int b = nb == 1 ? 0 : t / nk, k = t - b * nk;
+        const cpx<T> *Z = Zb + (size_t)b * buf;
+        T *out = (T *)L.out + (size_t)(item0 + b) * L.frows + rd.fofs;
         cpx<T> zk = Z[k];
         cpx<T> zn = c_conj(Z[(N - k) % N]);
         if (k == 0) {
@@ -97,7 +117,7 @@ __global__ void __launch_bounds__(256) ring_forward_kernel(RingLaunch L) {
             continue;
         }
         T bre = T(0.0f), bim = T(0.0f);
-        if (k <= rd.kmax) {
+        if (k <= kmx[b]) {
             cpx<T> e = {scale_f(zk.x + zn.x, 0.5f), scale_f(zk.y + zn.y, 0.5f)};
             cpx<T> d = {scale_f(zk.x - zn.x, 0.5f), scale_f(zk.y - zn.y, 0.5f)};
             cpx<T> o = {d.y, -d.x};  // d / i
@@ -118,40 +138,57 @@ __global__ void __launch_bounds__(256) ring_forward_kernel(RingLaunch L) {
 // and run HC2R for the variants: d=0 → f, ∂λ, ∂λλ; d=1 → ∂r; d=2 → ∂rr.
 // ====================================================================
 template <typename P, typename T>
-__global__ void __launch_bounds__(256) ring_inverse_kernel(RingLaunch L) {
+__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(RingLaunch L) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int kmx[kRingBatchMax];
     const int ring = L.ring_list[blockIdx.x];
-    const int item = blockIdx.y;
-    const int v = L.rlz ? item / L.bk : item;
-    const int zb = L.rlz ? item % L.bk : 0;
-    const RingDesc rd = L.rings[(size_t)v * L.ring_var_stride + ring];
+    const int item0 = blockIdx.y * L.ib;
+    const int nb = min(L.ib, L.nitems - item0);
+    const RingDesc rd = L.rings[(size_t)(L.rlz ? 0 : item0) * L.ring_var_stride + ring];
     const FftPlan &pl = L.plans[rd.plan];
     const int buf = fft_buffer_len(pl);
+    const int nk = rd.ri + 1;  // Xs stride: kmax ≤ ri
     cpx<T> *A = reinterpret_cast<cpx<T> *>(smem_raw);
-    cpx<T> *B = A + buf;
-    cpx<T> *Xs = B + buf;  // rotated spectrum X_k, k = 0..kmax
-    const int Lr = rd.L, N = Lr / 2, kmax = rd.kmax;
+    cpx<T> *B = A + (size_t)L.ib * buf;
+    cpx<T> *Xs = B + (size_t)L.ib * buf;  // rotated spectra X_k, k = 0..kmax, per item
+    __shared__ int64_t ooff[kRingBatchMax];  // element offset of each item's ring in one output plane
+    const int Lr = rd.L, N = Lr / 2;
+    if (threadIdx.x < nb) {
+        const int item = item0 + threadIdx.x;
+        kmx[threadIdx.x] = L.rings[(size_t)(L.rlz ? 0 : item) * L.ring_var_stride + ring].kmax;
+        // RLZ: H[variant][v][r][zb][l]; RL: physical[slot][v][point]
+        ooff[threadIdx.x] = L.rlz ? (int64_t)(item / L.bk) * L.bk * L.jDim + (int64_t)L.bk * rd.jofs +
+                                        (int64_t)(item % L.bk) * Lr
+                                  : (int64_t)item * L.np + rd.jofs;
+    }
+    __syncthreads();
 
     for (int d = 0; d < 3; d++) {
-        const T *g = (const T *)L.in + ((size_t)d * L.nitems + item) * L.frows + rd.fofs;
         // FAtransform!: a_re = c br - s bi, a_im = s br + c bi (phase_filter.jl:154-190)
-        for (int k = threadIdx.x; k <= kmax; k += blockDim.x) {
+        for (int t = threadIdx.x; t < nb * nk; t += blockDim.x) {
+            const int b = nb == 1 ? 0 : t / nk, k = t - b * nk;
+            if (k > kmx[b]) continue;
+            const T *g = (const T *)L.in + ((size_t)d * L.nitems + item0 + b) * L.frows + rd.fofs;
+            cpx<T> *X = Xs + (size_t)b * nk;
             if (k == 0) {
-                Xs[0] = {g[0], T(0.0f)};
+                X[0] = {g[0], T(0.0f)};
             } else {
                 T br = g[2 * k - 1], bi = g[2 * k];
                 cpx<T> cs = ld_cplx<T>(L.phase, rd.phase + (k - 1));
-                Xs[k] = {cs.x * br - cs.y * bi, cs.y * br + cs.x * bi};
+                X[k] = {cs.x * br - cs.y * bi, cs.y * br + cs.x * bi};
             }
         }
         __syncthreads();
         const int nvar = (d == 0) ? 3 : 1;
         for (int dl = 0; dl < nvar; dl++) {
             // packed spectrum Zp_k = E_k + i O_k, k < N (HC2R of length L via a length-N inverse DFT)
-            for (int k = threadIdx.x; k < N; k += blockDim.x) {
+            for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
+                const int b = nb == 1 ? 0 : t / N, k = t - b * N;
+                const int kmax = kmx[b];
+                const cpx<T> *X = Xs + (size_t)b * nk;
                 cpx<T> xa = c_zero<T>(), xb = c_zero<T>();
-                if (k <= kmax) xa = Xs[k];
-                if (N - k <= kmax && k > 0) xb = c_conj(Xs[N - k]);
+                if (k <= kmax) xa = X[k];
+                if (N - k <= kmax && k > 0) xb = c_conj(X[N - k]);
                 if (dl > 0) {
                     // FIxcoefficients: X_k → i κ X_k (twice for ∂λλ); κ = k for index k,
                     // κ = k - N for index k + N (its signed wavenumber k + N - L)
@@ -166,27 +203,24 @@ __global__ void __launch_bounds__(256) ring_inverse_kernel(RingLaunch L) {
                 }
                 cpx<T> e = c_add(xa, xb);
                 cpx<T> o = c_mul(c_sub(xa, xb), c_conj(ld_cplx<T>(L.pool, rd.utw + k)));
-                A[k] = {e.x - o.y, e.y + o.x};
+                A[(size_t)b * buf + k] = {e.x - o.y, e.y + o.x};
             }
             __syncthreads();
-            cpx<T> *z = dft<1, T>(A, B, pl, L.pool);
+            cpx<T> *zb0 = dft<1, T>(A, B, pl, L.pool, nb, buf);
             int slot;  // 1-based physical slot
             if (d == 0) slot = (dl == 0) ? 1 : (dl == 1 ? 4 : 5);
             else slot = (d == 1) ? 2 : 3;
-            if (L.rlz) {
-                // H[variant][v][r][zb][l], variant: 0 f, 1 ∂λ, 2 ∂λλ, 3 ∂r, 4 ∂rr
-                const int var = (d == 0) ? dl : (d == 1 ? 3 : 4);
-                T *dst = (T *)L.out + ((size_t)var * L.nvars + v) * L.bk * L.jDim + (size_t)L.bk * rd.jofs +
-                         (size_t)zb * Lr;
-                for (int n = threadIdx.x; n < N; n += blockDim.x) {
-                    cpx<T> w = z[n];
+            const int var = (d == 0) ? dl : (d == 1 ? 3 : 4);  // H variant: 0 f, 1 ∂λ, 2 ∂λλ, 3 ∂r, 4 ∂rr
+            const int64_t plane = L.rlz ? (int64_t)var * L.nvars * L.bk * L.jDim : (int64_t)(slot - 1) * L.nvars * L.np;
+            for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
+                const int b = nb == 1 ? 0 : t / N, n = t - b * N;
+                const cpx<T> w = zb0[(size_t)b * buf + n];
+                if (L.rlz) {
+                    T *dst = (T *)L.out + plane + ooff[b];
                     dst[2 * n] = w.x;
                     dst[2 * n + 1] = w.y;
-                }
-            } else {
-                P *dst = (P *)L.out + ((size_t)(slot - 1) * L.nvars + v) * L.np + rd.jofs;
-                for (int n = threadIdx.x; n < N; n += blockDim.x) {
-                    cpx<T> w = z[n];
+                } else {
+                    P *dst = (P *)L.out + plane + ooff[b];
                     dst[2 * n] = to_storage<P>(w.x);
                     dst[2 * n + 1] = to_storage<P>(w.y);
                 }
@@ -360,131 +394,222 @@ __device__ __forceinline__ int ring_of_column(const RingDesc *rings, int iDim, i
     return lo;
 }
 
-template <typename P, typename T>
-__global__ void __launch_bounds__(256) cheb_forward_kernel(ChebLaunch C) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int v = blockIdx.y;
-    const ChebDev &cb = C.cheb[v];
-    const int N = cb.N, bk = cb.bk, half = cb.half;
-    const int ldx = N | 1;                      // odd column stride: no bank conflicts
-    T *xs = reinterpret_cast<T *>(smem_raw);  // 64 × ldx
-    T *fw = xs + 64 * ldx;                      // bk × half
-    const int64_t c0 = (int64_t)blockIdx.x * 64;
-    const int ncol = (int)((C.jDim - c0) < 64 ? (C.jDim - c0) : 64);
-    const P *in = (const P *)C.in + (size_t)v * C.np + c0 * N;
-    for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) xs[(e / N) * ldx + (e % N)] = to_compute<T>(in[e]);
-    for (int e = threadIdx.x; e < bk * half; e += blockDim.x) fw[e] = ld_real<T>(cb.fwd_t, e);
-    __syncthreads();
-    const int col = threadIdx.x & 63, kg = threadIdx.x >> 6;  // 4 groups of modes
-    if (col < ncol) {
-        const int64_t q = c0 + col;
-        const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
-        const int l = (int)(q - rd.jofs);
-        T *out = (T *)C.out + (size_t)v * C.bk * C.jDim + (size_t)C.bk * rd.jofs + l;
-        const T *x = xs + col * ldx;
-        for (int k = kg; k < bk; k += 4) {
-            const T *row = fw + k * half;
-            T acc = T(0.0f);
-            const bool odd = k & 1;
-            for (int j = 0; j < half; j++) {
-                const int jj = N - 1 - j;
-                T e = (jj == j) ? x[j] : (odd ? x[j] - x[jj] : x[j] + x[jj]);
-                acc = acc + row[j] * e;
-            }
-            out[(size_t)k * rd.L] = acc;
+// K consecutive shared-memory values (16-byte aligned rows: vector loads for float/double)
+template <typename T, int K>
+__device__ __forceinline__ void load_row(const T *p, T (&v)[K]) {
+    if constexpr (std::is_same<T, float>::value && K % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < K / 4; q++) {
+            const float4 x = reinterpret_cast<const float4 *>(p)[q];
+            v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
         }
+    } else if constexpr (std::is_same<T, double>::value && K % 2 == 0) {
+#pragma unroll
+        for (int q = 0; q < K / 2; q++) {
+            const double2 x = reinterpret_cast<const double2 *>(p)[q];
+            v[2 * q] = x.x; v[2 * q + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < K; c++) v[c] = p[c];
     }
 }
 
 // ====================================================================
-// cheb_inverse: CAtransform! (a = bfill + Γᵀ bfill, Γ = Σ u vᵀ) then
-// CItransform! (DCT-I); variant 0 also CIx/CIxx (recurrence, src/Chebyshev.jl:636-646).
-// CTA = 64 consecutive columns of one variable; grid.z = ring variant.
+// cheb_forward, register-tiled: the CTA's 64 columns are staged (cp.async),
+// folded into xe[j][c] = x_j + x_{N-1-j} and xo[j][c] = x_j − x_{N-1-j}
+// (j < half; the middle point once), then out[k][c] = Σ_j FW[k][j] x{e,o}[j][c]
+// as two small GEMMs (even and odd k) with 4 × 4 register tiles; the same
+// per-output summation order (j ascending) as cheb_forward.  Results are staged
+// k-major and stored per ring row (C[r][zb][l]) with consecutive columns
+// contiguous.
 // ====================================================================
 template <typename P, typename T>
-__global__ void __launch_bounds__(256) cheb_inverse_kernel(ChebLaunch C) {
+__global__ void __launch_bounds__(128) cheb_forward_tiled_kernel(ChebLaunch C) {
+    constexpr int COLS = 64, TK = 4, TC = 4, CT = COLS / TC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int64_t col_base[64];  // H offset of column (ring start + l) for z_b = 0
-    __shared__ int col_L[64];
+    __shared__ int64_t col_base[COLS];
+    __shared__ int col_L[COLS];
+    const int v = blockIdx.y;
+    const ChebDev &cb = C.cheb[v];
+    const int N = cb.N, bk = cb.bk, half = cb.half;
+    const int ke = (bk + 1) / 2, ko = bk / 2;
+    const int KEP = (ke + TK - 1) / TK * TK, KOP = (ko > 0 ? (ko + TK - 1) / TK : 1) * TK;
+    const int ldx = N | 1;
+    T *xe = reinterpret_cast<T *>(smem_raw);      // half × COLS
+    T *xo = xe + (size_t)half * COLS;              // half × COLS
+    T *fe = xo + (size_t)half * COLS;              // half × KEP: FW[2i][j] at fe[j][i]
+    T *fo = fe + (size_t)half * KEP;               // half × KOP: FW[2i+1][j] at fo[j][i]
+    T *xs = fo + (size_t)half * KOP;               // COLS × ldx staged columns; later bk × COLS outputs
+    T *os = xs;
+    // tables once per CTA (host-transposed: coalesced)
+    for (int e = threadIdx.x; e < half * KEP; e += blockDim.x) fe[e] = ld_real<T>(cb.fwd_et_t, e);
+    for (int e = threadIdx.x; e < half * KOP; e += blockDim.x) fo[e] = ld_real<T>(cb.fwd_ot_t, e);
+    const int64_t nblk = (C.jDim + COLS - 1) / COLS;
+    for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int64_t c0 = blk * COLS;
+    const int ncol = (int)((C.jDim - c0) < COLS ? (C.jDim - c0) : COLS);
+    const P *in = (const P *)C.in + (size_t)v * C.np + c0 * N;
+    if constexpr (std::is_same<P, T>::value) {
+        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) cp_async<sizeof(T)>(xs + (e / N) * ldx + (e % N), in + e);
+    } else {
+        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) xs[(e / N) * ldx + (e % N)] = to_compute<T>(in[e]);
+    }
+    for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
+        if (c < ncol) {
+            const int64_t q = c0 + c;
+            const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
+            col_base[c] = (int64_t)C.bk * rd.jofs + (q - rd.jofs);
+            col_L[c] = rd.L;
+        }
+    }
+    if constexpr (std::is_same<P, T>::value) cp_async_wait_all();
+    __syncthreads();
+    for (int e = threadIdx.x; e < half * COLS; e += blockDim.x) {
+        const int j = e / COLS, c = e % COLS;
+        T a = T(0.0f), b = T(0.0f);
+        if (c < ncol) {
+            const T *x = xs + c * ldx;
+            const int jj = N - 1 - j;
+            if (jj == j) { a = x[j]; b = x[j]; }
+            else { a = x[j] + x[jj]; b = x[j] - x[jj]; }
+        }
+        xe[e] = a;
+        xo[e] = b;
+    }
+    __syncthreads();
+    const int KT = KEP / TK + KOP / TK;
+    for (int t = threadIdx.x; t < KT * CT; t += blockDim.x) {
+        const int ct = t % CT, kt = t / CT;
+        const bool odd = kt >= KEP / TK;
+        const int i0 = (odd ? kt - KEP / TK : kt) * TK, cc = ct * TC;
+        const T *ft = odd ? fo : fe;
+        const T *xt = odd ? xo : xe;
+        const int KP = odd ? KOP : KEP;
+        T acc[TK][TC];
+#pragma unroll
+        for (int i = 0; i < TK; i++)
+#pragma unroll
+            for (int c = 0; c < TC; c++) acc[i][c] = T(0.0f);
+        for (int j = 0; j < half; j++) {
+            T w[TK], x[TC];
+            load_row<T, TK>(ft + (size_t)j * KP + i0, w);
+            load_row<T, TC>(xt + (size_t)j * COLS + cc, x);
+#pragma unroll
+            for (int i = 0; i < TK; i++)
+#pragma unroll
+                for (int c = 0; c < TC; c++) acc[i][c] = acc[i][c] + w[i] * x[c];
+        }
+        // os aliases xs, which only the fold pass (before the last barrier) read
+#pragma unroll
+        for (int i = 0; i < TK; i++) {
+            const int k = 2 * (i0 + i) + (odd ? 1 : 0);
+            if (k < bk)
+#pragma unroll
+                for (int c = 0; c < TC; c++) os[(size_t)k * COLS + cc + c] = acc[i][c];
+        }
+    }
+    __syncthreads();
+    T *out = (T *)C.out + (size_t)v * C.bk * C.jDim;
+    for (int e = threadIdx.x; e < bk * ncol; e += blockDim.x) {
+        const int k = e / ncol, c = e % ncol;
+        out[col_base[c] + (int64_t)k * col_L[c]] = os[(size_t)k * COLS + c];
+    }
+    __syncthreads();  // os and col_base are rewritten by the next block
+    }  // column blocks
+}
+
+template <typename T>
+size_t cheb_forward_tiled_smem(int N, int bk) {
+    const int half = (N + 1) / 2, ke = (bk + 1) / 2, ko = bk / 2;
+    const int KEP = (ke + 3) / 4 * 4, KOP = (ko > 0 ? (ko + 3) / 4 : 1) * 4;
+    const size_t stage = std::max((size_t)64 * (N | 1), (size_t)bk * 64);
+    return ((size_t)2 * half * 64 + (size_t)half * (KEP + KOP) + stage) * sizeof(T);
+}
+
+// ====================================================================
+// cheb_inverse as one GEMM per output: CA (Γ fold), the CIx recurrence and
+// the folded DCT-I are linear, so each output column is u = M_d b with
+// M_d = IDCT·(D/dscale)^d·G composed on the host in FP64 (ChebDev::inv_m_t).
+// A CTA gathers the bk ring outputs of its 64 columns (cp.async, k-major) and
+// runs, per output, Ue = Me·B and Uo = Mo·B with 4 × 4 register tiles (matrix
+// rows read through L1, broadcast within a warp; B from shared memory), then
+// u[j] = Ue + Uo, u[N-1-j] = Ue − Uo, staged for a coalesced store.  No serial
+// per-column phase remains.  grid = (column blocks, variables, 5 ring variants);
+// variant 0 (f) also writes ∂z and ∂zz.
+// ====================================================================
+template <typename P, typename T>
+__global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
+    constexpr int COLS = 64, TJ = 4, TC = 4, CT = COLS / TC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int64_t col_base[COLS];
+    __shared__ int col_L[COLS];
     const int v = blockIdx.y, var = blockIdx.z;
     const ChebDev &cb = C.cheb[v];
     const int N = cb.N, bk = cb.bk, half = cb.half;
-    const int ne = (N + 1) / 2, no = N / 2;
-    const int ldn = N | 1, ldb = bk | 1;        // odd strides: no bank conflicts
-    T *as = reinterpret_cast<T *>(smem_raw);  // 64 × ldn coefficients
-    T *us = as + 64 * ldn;                      // 64 × ldn outputs
-    T *ie = us + 64 * ldn;                      // half × ne
-    T *io = ie + half * ne;                     // half × no
-    T *bs = io + half * (no > 0 ? no : 1);      // 64 × ldb inputs
-    const int64_t c0 = (int64_t)blockIdx.x * 64;
-    const int ncol = (int)((C.jDim - c0) < 64 ? (C.jDim - c0) : 64);
-    for (int e = threadIdx.x; e < half * ne; e += blockDim.x) ie[e] = ld_real<T>(cb.inv_e_t, e);
-    for (int e = threadIdx.x; e < half * no; e += blockDim.x) io[e] = ld_real<T>(cb.inv_o_t, e);
-    if (threadIdx.x < ncol) {
-        const int64_t q = c0 + threadIdx.x;
-        const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
-        col_base[threadIdx.x] = (int64_t)C.bk * rd.jofs + (q - rd.jofs);
-        col_L[threadIdx.x] = rd.L;
+    const int JT = (half + TJ - 1) / TJ, JP = JT * TJ;
+    const int ldn = N | 1;
+    T *bs = reinterpret_cast<T *>(smem_raw);  // bk × COLS inputs, k-major
+    T *us = bs + (size_t)bk * COLS;            // COLS × ldn outputs
+    const int64_t c0 = (int64_t)blockIdx.x * COLS;
+    const int ncol = (int)((C.jDim - c0) < COLS ? (C.jDim - c0) : COLS);
+    for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
+        if (c < ncol) {
+            const int64_t q = c0 + c;
+            const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
+            col_base[c] = (int64_t)C.bk * rd.jofs + (q - rd.jofs);
+            col_L[c] = rd.L;
+        }
     }
     __syncthreads();
-    // gather the bk ring outputs of each column
     const T *H = (const T *)C.in + ((size_t)var * C.nvars + v) * C.bk * C.jDim;
-    for (int e = threadIdx.x; e < ncol * bk; e += blockDim.x) {
-        const int zb = e / ncol, col = e % ncol;
-        bs[col * ldb + zb] = H[col_base[col] + (int64_t)zb * col_L[col]];
+    for (int e = threadIdx.x; e < bk * COLS; e += blockDim.x) {
+        const int zb = e / COLS, col = e % COLS;
+        if (col < ncol) cp_async<sizeof(T)>(bs + e, H + col_base[col] + (int64_t)zb * col_L[col]);
+        else bs[e] = T(0.0f);
     }
-    __syncthreads();
-    const int col = threadIdx.x & 63, jg = threadIdx.x >> 6;
-    // CA: a_j = b_j (j < bk) + Σ_p (u_p·b) v_p[j]
-    if (col < ncol) {
-        const T *bb = bs + col * ldb;
-        T sp[2] = {T(0.0f), T(0.0f)};
-        for (int p = 0; p < cb.nrank; p++) {
-            T acc = T(0.0f);
-            for (int i = 0; i < bk; i++) acc = acc + ld_real<T>(cb.gu_t, (int64_t)p * bk + i) * bb[i];
-            sp[p] = acc;
-        }
-        for (int j = jg; j < N; j += 4) {
-            T aj = (j < bk) ? bb[j] : T(0.0f);
-            for (int p = 0; p < cb.nrank; p++) aj = aj + ld_real<T>(cb.gv_t, (int64_t)p * N + j) * sp[p];
-            as[col * ldn + j] = aj;
-        }
-    }
+    cp_async_wait_all();
     __syncthreads();
     const int nd = (var == 0) ? 3 : 1;
-    const T dsc = to_compute<T>(cb.dscale);
     for (int dd = 0; dd < nd; dd++) {
-        if (dd > 0) {
-            // CIxcoefficients in place: ax[N-1] = 0, ax[i] = 2(i+1) a[i+1] + ax[i+2], then ax /= dscale
-            if (jg == 0 && col < ncol) {
-                T *a = as + col * ldn;
-                T a_next = a[N - 1];
-                a[N - 1] = T(0.0f);
-                T ax1 = T(0.0f), ax2 = T(0.0f);  // ax[i+1], ax[i+2]
-                for (int i = N - 2; i >= 0; i--) {
-                    T axi = scale_f(a_next, (float)(2 * (i + 1))) + ax2;
-                    a_next = a[i];
-                    a[i] = axi;
-                    ax2 = ax1;
-                    ax1 = axi;
+        const int64_t me = (int64_t)(dd * 2) * bk * JP, mo = me + (int64_t)bk * JP;
+        for (int t = threadIdx.x; t < JT * CT; t += blockDim.x) {
+            const int ct = t % CT, jt = t / CT;
+            const int j0 = jt * TJ, cc = ct * TC;
+            T E[TJ][TC], O[TJ][TC];
+#pragma unroll
+            for (int i = 0; i < TJ; i++)
+#pragma unroll
+                for (int c = 0; c < TC; c++) { E[i][c] = T(0.0f); O[i][c] = T(0.0f); }
+            for (int k = 0; k < bk; k++) {
+                T we[TJ], wo[TJ], b[TC];
+#pragma unroll
+                for (int i = 0; i < TJ; i++) {
+                    we[i] = ld_real<T>(cb.inv_m_t, me + (int64_t)k * JP + j0 + i);
+                    wo[i] = ld_real<T>(cb.inv_m_t, mo + (int64_t)k * JP + j0 + i);
                 }
-                for (int j = 0; j < N; j++) a[j] = a[j] / dsc;
+                load_row<T, TC>(bs + (size_t)k * COLS + cc, b);
+#pragma unroll
+                for (int i = 0; i < TJ; i++)
+#pragma unroll
+                    for (int c = 0; c < TC; c++) {
+                        E[i][c] = E[i][c] + we[i] * b[c];
+                        O[i][c] = O[i][c] + wo[i] * b[c];
+                    }
             }
-            __syncthreads();
-        }
-        if (col < ncol) {
-            const T *a = as + col * ldn;
-            T *u = us + col * ldn;
-            for (int j = jg; j < half; j += 4) {
-                T E = T(0.0f), O = T(0.0f);
-                for (int k = 0; k < ne; k++) E = E + ie[j * ne + k] * a[2 * k];
-                for (int k = 0; k < no; k++) O = O + io[j * no + k] * a[2 * k + 1];
-                u[j] = E + O;
-                if (N - 1 - j != j) u[N - 1 - j] = E - O;
+#pragma unroll
+            for (int i = 0; i < TJ; i++) {
+                const int j = j0 + i;
+                if (j < half)
+#pragma unroll
+                    for (int c = 0; c < TC; c++) {
+                        T *u = us + (size_t)(cc + c) * ldn;
+                        u[j] = E[i][c] + O[i][c];
+                        if (N - 1 - j != j) u[N - 1 - j] = E[i][c] - O[i][c];
+                    }
             }
         }
         __syncthreads();
-        // coalesced write of the tile: physical slot of (variant, derivative)
         int slot;
         if (var == 0) slot = (dd == 0) ? 1 : (dd == 1 ? 6 : 7);
         else slot = (var == 1) ? 4 : (var == 2 ? 5 : (var == 3 ? 2 : 3));
@@ -494,25 +619,57 @@ __global__ void __launch_bounds__(256) cheb_inverse_kernel(ChebLaunch C) {
     }
 }
 
+template <typename T>
+size_t cheb_inverse_m_smem(int N, int bk) {
+    return ((size_t)bk * 64 + (size_t)64 * (N | 1)) * sizeof(T);
+}
+
 // ====================================================================
 // launchers
 // ====================================================================
+// SMs of the current device (cached) and a CTA count that keeps them busy
+static int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cached[dev] = n > 0 ? n : 152;
+    }
+    return cached[dev];
+}
+static int resident_ctas(size_t smem, int threads) {
+    int per = std::min(2048 / threads, 32);
+    if (smem > 0) per = std::min<int>(per, (int)((227 * 1024) / (smem + 2048)));
+    return sm_count() * std::max(per, 1);
+}
+
 template <typename K>
 static void set_smem(K kernel, size_t smem) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
+// `per_item`: shared-memory bytes of one item of the bucket's largest ring; a
+// CTA takes L.ib items (1 when unset)
 template <typename P, typename T>
-cudaError_t launch_ring_forward(const RingLaunch &L, int nrings, int nitems, size_t smem, int threads,
+cudaError_t launch_ring_forward(const RingLaunch &L0, int nrings, int nitems, size_t per_item, int threads,
                                 cudaStream_t st) {
+    RingLaunch L = L0;
+    L.ib = std::max(1, std::min(L.ib, kRingBatchMax));
+    const size_t smem = per_item * L.ib;
     set_smem(ring_forward_kernel<P, T>, smem);
-    ring_forward_kernel<P, T><<<dim3(nrings, nitems), threads, smem, st>>>(L);
+    ring_forward_kernel<P, T><<<dim3(nrings, (nitems + L.ib - 1) / L.ib), threads, smem, st>>>(L);
     return cudaGetLastError();
 }
 template <typename P, typename T>
-cudaError_t launch_ring_inverse(const RingLaunch &L, int nrings, int nitems, size_t smem, int threads,
+cudaError_t launch_ring_inverse(const RingLaunch &L0, int nrings, int nitems, size_t per_item, int threads,
                                 cudaStream_t st) {
+    RingLaunch L = L0;
+    L.ib = std::max(1, std::min(L.ib, kRingBatchMax));
+    const size_t smem = per_item * L.ib;
     set_smem(ring_inverse_kernel<P, T>, smem);
-    ring_inverse_kernel<P, T><<<dim3(nrings, nitems), threads, smem, st>>>(L);
+    ring_inverse_kernel<P, T><<<dim3(nrings, (nitems + L.ib - 1) / L.ib), threads, smem, st>>>(L);
     return cudaGetLastError();
 }
 template <typename P, typename T>
@@ -528,18 +685,27 @@ cudaError_t launch_sa_si(const SaLaunch &A, int nitems, size_t smem, cudaStream_
     sa_si_kernel<P, T><<<grid, 128, smem, st>>>(A);
     return cudaGetLastError();
 }
+// the register-tiled kernel; `smem` (the one-MAC-per-load kernel's size) is unused
 template <typename P, typename T>
-cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st) {
-    set_smem(cheb_forward_kernel<P, T>, smem);
-    dim3 grid((unsigned)((C.jDim + 63) / 64), C.nvars);
-    cheb_forward_kernel<P, T><<<grid, 256, smem, st>>>(C);
+cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st, int N) {
+    (void)smem;
+    const size_t sm = cheb_forward_tiled_smem<T>(N, C.bk);
+    set_smem(cheb_forward_tiled_kernel<P, T>, sm);
+    const int64_t nblk = (C.jDim + 63) / 64;
+    const int64_t want = std::max<int64_t>(1, (int64_t)resident_ctas(sm, 128) / std::max(C.nvars, 1));
+    dim3 grid((unsigned)std::min(nblk, want), C.nvars);
+    cheb_forward_tiled_kernel<P, T><<<grid, 128, sm, st>>>(C);
     return cudaGetLastError();
 }
+// the register-tiled kernel; `smem` (the 64-column kernel's size) is unused.
+// N and bk are the grid's (every variable shares them).
 template <typename P, typename T>
-cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t st) {
-    set_smem(cheb_inverse_kernel<P, T>, smem);
+cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t st, int N) {
+    (void)smem;
+    const size_t sm = cheb_inverse_m_smem<T>(N, C.bk);
+    set_smem(cheb_inverse_m_kernel<P, T>, sm);
     dim3 grid((unsigned)((C.jDim + 63) / 64), C.nvars, 5);
-    cheb_inverse_kernel<P, T><<<grid, 256, smem, st>>>(C);
+    cheb_inverse_m_kernel<P, T><<<grid, 128, sm, st>>>(C);
     return cudaGetLastError();
 }
 
@@ -655,8 +821,8 @@ template cudaError_t launch_tile_sum<float>(const TileLaunch &, cudaStream_t);
     template cudaError_t launch_ring_inverse<P, T>(const RingLaunch &, int, int, size_t, int, cudaStream_t); \
     template cudaError_t launch_sb_project<P, T>(const SbLaunch &, int, cudaStream_t);                      \
     template cudaError_t launch_sa_si<P, T>(const SaLaunch &, int, size_t, cudaStream_t);                   \
-    template cudaError_t launch_cheb_forward<P, T>(const ChebLaunch &, size_t, cudaStream_t);               \
-    template cudaError_t launch_cheb_inverse<P, T>(const ChebLaunch &, size_t, cudaStream_t);
+    template cudaError_t launch_cheb_forward<P, T>(const ChebLaunch &, size_t, cudaStream_t, int);               \
+    template cudaError_t launch_cheb_inverse<P, T>(const ChebLaunch &, size_t, cudaStream_t, int);
 SS_INSTANTIATE(double, double)
 SS_INSTANTIATE(double, df64)
 SS_INSTANTIATE(float, float)

@@ -23,7 +23,26 @@ struct RingLaunch {
     int64_t jDim;
     int64_t np;
     int nitems, nvars, bk, rlz;
+    int ib;                    // items per CTA (≤ kRingBatchMax): one batched DFT per pass
 };
+constexpr int kRingBatchMax = 16;
+constexpr size_t kRingBatchBytes = 64 * 1024;  // shared-memory budget of one ring batch
+// items per CTA for a launch of `nrings` rings of buffer length ≤ `buf` complex
+// entries, needing `per_item` shared-memory bytes each: enough sequences to
+// give each of the CTA's `threads` about one butterfly per pass (batching
+// only pays off for rings shorter than the CTA), within the shared-memory
+// budget, while the launch keeps at least `min_ctas` CTAs (each bucket of
+// rings is its own launch)
+inline int ring_batch(size_t per_item, int nitems, int nrings, int min_ctas, int threads, int buf) {
+    size_t ib = kRingBatchBytes / (per_item > 0 ? per_item : 1);
+    const size_t by_work = (size_t)(2 * threads) / (size_t)(buf > 0 ? buf : 1);
+    if (ib > by_work) ib = by_work;
+    if (ib < 1) ib = 1;
+    if (ib > (size_t)kRingBatchMax) ib = kRingBatchMax;
+    if (ib > (size_t)nitems) ib = nitems > 0 ? nitems : 1;
+    while (ib > 1 && (long long)nrings * ((nitems + (long long)ib - 1) / (long long)ib) < min_ctas) ib--;
+    return (int)ib;
+}
 
 struct SbLaunch {
     const void *F;
@@ -95,8 +114,8 @@ cudaError_t launch_sb_project(const SbLaunch &S, int nitems, cudaStream_t st);
 template <typename P, typename T>
 cudaError_t launch_sa_si(const SaLaunch &A, int nitems, size_t smem, cudaStream_t st);
 template <typename P, typename T>
-cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st);
+cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st, int N);
 template <typename P, typename T>
-cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t st);
+cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t st, int N);
 
 }  // namespace ss

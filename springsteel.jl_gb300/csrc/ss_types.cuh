@@ -127,6 +127,18 @@ __device__ __forceinline__ cpx<T> c_conj(cpx<T> a) { return {a.x, -a.y}; }
 template <typename T>
 __device__ __forceinline__ cpx<T> c_zero() { return {T(0.0f), T(0.0f)}; }
 
+// Asynchronous global → shared copies (cp.async): a gather issues every copy of
+// a tile before waiting once, instead of one load in flight per thread.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem_dst, const void *gsrc) {
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(gsrc), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
 // cos/sin(2π j/R) for the odd-prime butterflies, in each layout
 __constant__ double c_rcos_d[14][14];
 __constant__ double c_rsin_d[14][14];

@@ -203,6 +203,27 @@ def test_fp32_refined_error_vs_fp64_oracle():
     assert np.all(errs < 1e-4), errs
 
 
+@pytest.mark.parametrize("precision", ["f64", "f64_fast"])
+def test_rlz_kz64_parity(precision):
+    # the configuration-4 column length (64 levels) in FP64 arithmetic
+    gp = fields.config4_params(precision=precision, num_cells=12, kDim=64, nvars=2)
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.rlz_blob_fields(pts, 2, zmax=20000.0)
+    _, _, sg, so, pg, po = _run_both(gp, u)
+    _assert_parity(sg, so, pg, po, gp, tol=TOL64 if precision == "f64" else TOL_FAST)
+
+
+def test_fp32_kz64_error_vs_fp64_oracle():
+    gp = fields.config4_params(precision="f32", num_cells=24, kDim=64, nvars=2)
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.rlz_blob_fields(pts, 2, zmax=20000.0)
+    _, o, sg, so, pg, po = _run_both(gp, u)
+    errs = slot_errors(pg, po, gp)
+    print("FP32 kz=64 slot errors", errs)
+    # binary32 bulk: f and the first derivatives ~1e-5, second derivatives ~1e-4
+    assert np.all(errs < 5e-4), errs
+
+
 def test_bad_shapes_rejected():
     with pytest.raises(S.SpringsteelError):
         S.createGrid(S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=1.0, num_cells=0))
