@@ -4,9 +4,10 @@
 // L = 4+4ri points (src/Fourier.jl:192-193, 388-395, 463-468).  Ring lengths
 // have arbitrary prime factors, so a length-N complex DFT (N = L/2 after real
 // packing) is evaluated either by mixed-radix Stockham autosort passes
-// (radices 4,2,3,5,7,11,13 in registers) or, when N has a prime factor > 13,
-// by Bluestein's chirp-z convolution of smooth length M >= 2N-1 whose two FFTs
-// are again Stockham passes.  Twiddles come from FP64-accurate tables built on
+// (radices 4,2,3,5,7,11,13 in registers, odd primes up to kMaxPrimeRadix as
+// output-pair passes) or, when N has a larger prime factor, by Bluestein's
+// chirp-z convolution of smooth length M >= 2N-1 whose two FFTs are again
+// Stockham passes.  Twiddles come from FP64-accurate tables built on
 // the host (ss_setup.cpp), stored in the compute type's layout.
 //
 // Every routine transforms a batch of `nb` independent sequences of the same
@@ -123,6 +124,73 @@ __device__ __forceinline__ const void *tab_at(const void *pool, int64_t off) {
     return (const void *)((const typename Tab<T>::cplx_t *)pool + off);
 }
 
+// Radix-R pass for an odd prime R > 13 (up to kMaxPrimeRadix).  The inputs
+// are first multiplied in place by their twiddles (skipped when Ns = 1); then
+// each work item computes one conjugate output pair (s, R−s) of one butterfly
+// from the pairs a_q = v_q + v_{R−q}, b_q = v_q − v_{R−q}:
+//   re = v_0 + Σ_q a_q cos(2πqs/R),  im = Σ_q b_q sin(2πqs/R),
+//   X_s = re ∓ i·im, X_{R−s} = re ± i·im  (upper signs forward), X_0 = Σ v_q.
+// cos/sin(2πe/R) are the N-point twiddles at e·N/R.  (R−1)/2 complex
+// multiply-adds per output instead of a length ≥ 2N−1 chirp-z convolution.
+template <int SIGN, typename T>
+__device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N, int Ns, int R,
+                           const void *__restrict__ tw, int nb, int bs) {
+    const int NR = N / R, H = (R - 1) / 2;
+    const int tstride = N / (Ns * R), rstep = N / R;
+    const float inv_ns = 1.0f / (float)Ns, inv_nr = 1.0f / (float)NR, inv_h1 = 1.0f / (float)(H + 1);
+    if (Ns > 1) {
+        for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
+            const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
+            const int q = div_small(e, NR, inv_nr), j = e - q * NR;
+            const int k = j - div_small(j, Ns, inv_ns) * Ns;
+            if (q > 0 && k > 0) {
+                cpx<T> w = ld_cplx<T>(tw, (int64_t)q * k * tstride);
+                if (SIGN > 0) w.y = -w.y;
+                cpx<T> *p = src + (size_t)bi * bs + e;
+                *p = c_mul(*p, w);
+            }
+        }
+        __syncthreads();
+    }
+    const int per = NR * (H + 1);
+    for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
+        const int bi = nb == 1 ? 0 : t / per, rest = t - bi * per;
+        const int j = div_small(rest, H + 1, inv_h1), s = rest - j * (H + 1);
+        const cpx<T> *sv = src + (size_t)bi * bs + j;
+        cpx<T> *d = dst + (size_t)bi * bs;
+        const int jq = div_small(j, Ns, inv_ns), k = j - jq * Ns;
+        const int idxD = jq * Ns * R + k;
+        const cpx<T> x0 = sv[0];
+        if (s == 0) {
+            cpx<T> acc = x0;
+            for (int q = 1; q < R; q++) acc = c_add(acc, sv[q * NR]);
+            d[idxD] = acc;
+            continue;
+        }
+        cpx<T> re = x0, im = c_zero<T>();
+        int e = 0;
+        for (int q = 1; q <= H; q++) {
+            e += s;
+            if (e >= R) e -= R;
+            const cpx<T> w = ld_cplx<T>(tw, (int64_t)e * rstep);  // (cos, −sin)(2πe/R)
+            const cpx<T> vq = sv[q * NR], vr = sv[(R - q) * NR];
+            const cpx<T> a = c_add(vq, vr), b = c_sub(vq, vr);
+            re.x = re.x + a.x * w.x;
+            re.y = re.y + a.y * w.x;
+            im.x = im.x - b.x * w.y;
+            im.y = im.y - b.y * w.y;
+        }
+        const cpx<T> iim = {-im.y, im.x};
+        if (SIGN < 0) {
+            d[idxD + s * Ns] = c_sub(re, iim);
+            d[idxD + (R - s) * Ns] = c_add(re, iim);
+        } else {
+            d[idxD + s * Ns] = c_add(re, iim);
+            d[idxD + (R - s) * Ns] = c_sub(re, iim);
+        }
+    }
+}
+
 // Stockham DFT over ping-pong buffers; returns the buffer holding the result.
 template <int SIGN, typename T>
 __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int nb, int bs) {
@@ -137,7 +205,7 @@ __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nra
         case 7: stockham_pass<7, SIGN>(a, b, N, Ns, tw, nb, bs); break;
         case 11: stockham_pass<11, SIGN>(a, b, N, Ns, tw, nb, bs); break;
         case 13: stockham_pass<13, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        default: break;
+        default: prime_pass<SIGN, T>(a, b, N, Ns, R, tw, nb, bs); break;
         }
         __syncthreads();
         cpx<T> *t = a;

@@ -33,6 +33,8 @@ struct Status {
 // shared memory, or (N with a prime factor > 13) by Bluestein's chirp-z
 // convolution of smooth length M >= 2N-1.
 constexpr int kMaxRadices = 24;
+// largest odd prime handled by a direct radix pass; larger factors go through Bluestein
+constexpr int kMaxPrimeRadix = 127;
 struct FftPlan {
     int N;
     int nrad;

@@ -364,15 +364,38 @@ int64_t TwiddlePool::push(const std::vector<double> &ci) {
     return off;
 }
 
+// Radix sequence of an n-point DFT: odd primes 17..kMaxPrimeRadix first (as the
+// first pass they need no input twiddles), then 4s and 2, 3, 5, 7, 11, 13.
+// smooth_only (Bluestein lengths) admits 2, 3, 5, 7 only.  False when a prime
+// factor is not covered (the caller then uses Bluestein).
 static bool factor_radices(int n, int *rad, int &nrad, bool smooth_only) {
     nrad = 0;
-    while (n % 4 == 0 && n > 1) { rad[nrad++] = 4; n /= 4; }
+    if (!smooth_only)
+        for (int f = 17; f <= kMaxPrimeRadix && n > 1; f += 2) {
+            bool prime = true;
+            for (int d = 3; d * d <= f; d += 2)
+                if (f % d == 0) { prime = false; break; }
+            if (!prime) continue;
+            while (n % f == 0) {
+                if (nrad >= kMaxRadices) return false;
+                rad[nrad++] = f;
+                n /= f;
+            }
+        }
+    while (n % 4 == 0 && n > 1) {
+        if (nrad >= kMaxRadices) return false;
+        rad[nrad++] = 4;
+        n /= 4;
+    }
     const int primes[] = {2, 3, 5, 7, 11, 13};
     for (int f : primes) {
         if (smooth_only && f > 7) break;
-        while (n % f == 0) { rad[nrad++] = f; n /= f; }
+        while (n % f == 0) {
+            if (nrad >= kMaxRadices) return false;
+            rad[nrad++] = f;
+            n /= f;
+        }
     }
-    if (nrad > kMaxRadices) return false;
     return n == 1;
 }
 
