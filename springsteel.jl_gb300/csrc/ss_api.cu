@@ -305,35 +305,50 @@ static int32_t build_grid(ss_grid *g) {
                 if ((st = upload_bytes(g, &cd.inv_ot_t, real_layout(ot, g->tl)))) return st;
                 if ((st = upload_bytes(g, &cd.fwd_et_t, real_layout(fe, g->tl)))) return st;
                 if ((st = upload_bytes(g, &cd.fwd_ot_t, real_layout(fo, g->tl)))) return st;
-                // composed inverse matrices: X_0 = G (CA), X_d = D X_{d-1} / dscale (CIxcoefficients)
-                const int B = ch.bk;
-                std::vector<double> X((size_t)N * B, 0.0), Xn((size_t)N * B, 0.0);
-                for (int k = 0; k < N; k++)
-                    for (int i = 0; i < B; i++) {
-                        double val = (k == i) ? 1.0 : 0.0;
-                        for (int p = 0; p < ch.nrank; p++) val += ch.gv[(size_t)p * N + k] * ch.gu[(size_t)p * B + i];
-                        X[(size_t)k * B + i] = val;
-                    }
-                std::vector<double> mt((size_t)6 * B * JP, 0.0);
+                // Composed inverse matrices.  G = Ĩ + V Uᵀ (CA: Ĩ keeps the bk modes, V = gvᵀ,
+                // U = guᵀ), D the CIxcoefficients map (÷ dscale).  Columns: X_d = D^d [Ĩ | V].
+                // D flips coefficient parity, so the output half of parity pe (even/odd k)
+                // reads only the inputs i of parity (pe + d) mod 2 through D^d Ĩ, plus the
+                // rank-nrank term through s = Uᵀ b.  Rows of table (d, pe): the K_q inputs of
+                // that parity (i = 2i' + q), then the nrank rows of s; zero-padded to Kcap.
+                const int B = ch.bk, nr = ch.nrank, Kcols = B + nr;
+                const int Ke = (B + 1) / 2 + nr, Ko = B / 2 + nr, Kcap = std::max(Ke, Ko);
+                std::vector<double> X((size_t)N * Kcols, 0.0), Xn((size_t)N * Kcols, 0.0);
+                for (int k = 0; k < N; k++) {
+                    if (k < B) X[(size_t)k * Kcols + k] = 1.0;
+                    for (int p = 0; p < nr; p++) X[(size_t)k * Kcols + B + p] = ch.gv[(size_t)p * N + k];
+                }
+                std::vector<double> mt((size_t)6 * Kcap * JP, 0.0);
                 for (int dd = 0; dd < 3; dd++) {
                     if (dd > 0) {
                         for (int k = 0; k < N; k++)
-                            for (int i = 0; i < B; i++) {
-                                double acc = 0.0;  // (D X)[k][i] = Σ_{m > k, m − k odd} 2m X[m][i]
-                                for (int m = k + 1; m < N; m += 2) acc += 2.0 * m * X[(size_t)m * B + i];
-                                Xn[(size_t)k * B + i] = acc / ch.dscale;
+                            for (int c = 0; c < Kcols; c++) {
+                                double acc = 0.0;  // (D X)[k][c] = Σ_{m > k, m − k odd} 2m X[m][c]
+                                for (int m = k + 1; m < N; m += 2) acc += 2.0 * m * X[(size_t)m * Kcols + c];
+                                Xn[(size_t)k * Kcols + c] = acc / ch.dscale;
                             }
                         X.swap(Xn);
                     }
-                    for (int j = 0; j < half; j++)
-                        for (int i = 0; i < B; i++) {
-                            double se = 0.0, so = 0.0;
-                            for (int k = 0; k < N; k += 2) se += ch.inv_e[(size_t)j * ne + k / 2] * X[(size_t)k * B + i];
-                            for (int k = 1; k < N; k += 2) so += ch.inv_o[(size_t)j * no + k / 2] * X[(size_t)k * B + i];
-                            mt[((size_t)(dd * 2 + 0) * B + i) * JP + j] = se;
-                            mt[((size_t)(dd * 2 + 1) * B + i) * JP + j] = so;
+                    for (int pe = 0; pe < 2; pe++) {
+                        const int q = (pe + dd) & 1;  // input parity feeding this half
+                        const int nq = q ? B / 2 : (B + 1) / 2;
+                        const std::vector<double> &IT = pe ? ch.inv_o : ch.inv_e;
+                        const int nk = pe ? no : ne;
+                        double *tab = mt.data() + (size_t)(dd * 2 + pe) * Kcap * JP;
+                        for (int j = 0; j < half; j++) {
+                            for (int r = 0; r < nq + nr; r++) {
+                                const int c = r < nq ? 2 * r + q : B + (r - nq);
+                                double acc = 0.0;
+                                for (int kk = 0; kk < nk; kk++) {
+                                    const int k = 2 * kk + pe;
+                                    if (k < N) acc += IT[(size_t)j * nk + kk] * X[(size_t)k * Kcols + c];
+                                }
+                                tab[(size_t)r * JP + j] = acc;
+                            }
                         }
+                    }
                 }
+                cd.kcap = Kcap;
                 if ((st = upload_bytes(g, &cd.inv_m_t, real_layout(mt, g->tl)))) return st;
             }
         }

@@ -96,11 +96,12 @@ struct ChebDev {
     const void *fwd_et_t;  // half × KEP, KEP = 4⌈⌈bk/2⌉/4⌉: fwd[2i][j] at [j][i]
     const void *fwd_ot_t;  // half × KOP, KOP = 4⌈⌊bk/2⌋/4⌉: fwd[2i+1][j] at [j][i]
     // CA, the CIx recurrence D (÷ dscale) and the folded DCT-I composed:
-    // u = M_d b for derivative order d = 0, 1, 2; even/odd halves
-    // Me_d[j][i] = Σ_{k even} IE[j][k/2] (D^d G)[k][i], Mo_d likewise over odd k,
-    // u[j] = (Me b)[j] + (Mo b)[j], u[N-1-j] = (Me b)[j] − (Mo b)[j]; stored
-    // transposed as [d][e/o][i < bk][JP]
+    // u = M_d b for derivative order d = 0, 1, 2, split into output halves
+    // (u[j] = (Me b)[j] + (Mo b)[j], u[N-1-j] = (Me b)[j] − (Mo b)[j]).  Half pe
+    // reads only the inputs of parity (pe + d) mod 2 plus s = Uᵀ b (the rank
+    // term of Γ); stored as [d][pe][kcap rows: those inputs, then s][JP]
     const void *inv_m_t;
+    int kcap, _kpad;
 };
 SS_HD inline int cheb_pad4(int n) { return n > 0 ? (n + 3) / 4 * 4 : 4; }
 

@@ -549,8 +549,10 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
     const int N = cb.N, bk = cb.bk, half = cb.half;
     const int JT = (half + TJ - 1) / TJ, JP = JT * TJ;
     const int ldn = N | 1;
-    T *bs = reinterpret_cast<T *>(smem_raw);  // bk × COLS inputs, k-major
-    T *us = bs + (size_t)bk * COLS;            // COLS × ldn outputs
+    const int nr = cb.nrank, Ke = (bk + 1) / 2 + nr, Ko = bk / 2 + nr;
+    T *xe = reinterpret_cast<T *>(smem_raw);  // Ke × COLS: even inputs b_{2i'}, then s = Uᵀ b
+    T *xo = xe + (size_t)Ke * COLS;            // Ko × COLS: odd inputs b_{2i'+1}, then s
+    T *us = xo + (size_t)Ko * COLS;            // COLS × ldn outputs
     const int64_t c0 = (int64_t)blockIdx.x * COLS;
     const int ncol = (int)((C.jDim - c0) < COLS ? (C.jDim - c0) : COLS);
     for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
@@ -565,14 +567,28 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
     const T *H = (const T *)C.in + ((size_t)var * C.nvars + v) * C.bk * C.jDim;
     for (int e = threadIdx.x; e < bk * COLS; e += blockDim.x) {
         const int zb = e / COLS, col = e % COLS;
-        if (col < ncol) cp_async<sizeof(T)>(bs + e, H + col_base[col] + (int64_t)zb * col_L[col]);
-        else bs[e] = T(0.0f);
+        T *dst = ((zb & 1) ? xo : xe) + (size_t)(zb >> 1) * COLS + col;
+        if (col < ncol) cp_async<sizeof(T)>(dst, H + col_base[col] + (int64_t)zb * col_L[col]);
+        else *dst = T(0.0f);
     }
     cp_async_wait_all();
     __syncthreads();
+    // s_p = Σ_i gu[p][i] b_i (the rank term of the Γ fold), appended to both input sets
+    for (int c = threadIdx.x; c < COLS; c += blockDim.x)
+        for (int p = 0; p < nr; p++) {
+            T acc = T(0.0f);
+            for (int i = 0; i < bk; i++)
+                acc = acc + ld_real<T>(cb.gu_t, (int64_t)p * bk + i) * ((i & 1) ? xo : xe)[(size_t)(i >> 1) * COLS + c];
+            xe[(size_t)((bk + 1) / 2 + p) * COLS + c] = acc;
+            xo[(size_t)(bk / 2 + p) * COLS + c] = acc;
+        }
+    __syncthreads();
     const int nd = (var == 0) ? 3 : 1;
     for (int dd = 0; dd < nd; dd++) {
-        const int64_t me = (int64_t)(dd * 2) * bk * JP, mo = me + (int64_t)bk * JP;
+        // output half pe reads the inputs of parity (pe + dd) mod 2
+        const int64_t me = (int64_t)(dd * 2) * cb.kcap * JP, mo = me + (int64_t)cb.kcap * JP;
+        const T *ie = (dd & 1) ? xo : xe, *io = (dd & 1) ? xe : xo;
+        const int Kie = (dd & 1) ? Ko : Ke, Kio = (dd & 1) ? Ke : Ko;
         for (int t = threadIdx.x; t < JT * CT; t += blockDim.x) {
             const int ct = t % CT, jt = t / CT;
             const int j0 = jt * TJ, cc = ct * TC;
@@ -581,21 +597,25 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
             for (int i = 0; i < TJ; i++)
 #pragma unroll
                 for (int c = 0; c < TC; c++) { E[i][c] = T(0.0f); O[i][c] = T(0.0f); }
-            for (int k = 0; k < bk; k++) {
-                T we[TJ], wo[TJ], b[TC];
+            for (int k = 0; k < Kie; k++) {
+                T w[TJ], b[TC];
 #pragma unroll
-                for (int i = 0; i < TJ; i++) {
-                    we[i] = ld_real<T>(cb.inv_m_t, me + (int64_t)k * JP + j0 + i);
-                    wo[i] = ld_real<T>(cb.inv_m_t, mo + (int64_t)k * JP + j0 + i);
-                }
-                load_row<T, TC>(bs + (size_t)k * COLS + cc, b);
+                for (int i = 0; i < TJ; i++) w[i] = ld_real<T>(cb.inv_m_t, me + (int64_t)k * JP + j0 + i);
+                load_row<T, TC>(ie + (size_t)k * COLS + cc, b);
 #pragma unroll
                 for (int i = 0; i < TJ; i++)
 #pragma unroll
-                    for (int c = 0; c < TC; c++) {
-                        E[i][c] = E[i][c] + we[i] * b[c];
-                        O[i][c] = O[i][c] + wo[i] * b[c];
-                    }
+                    for (int c = 0; c < TC; c++) E[i][c] = E[i][c] + w[i] * b[c];
+            }
+            for (int k = 0; k < Kio; k++) {
+                T w[TJ], b[TC];
+#pragma unroll
+                for (int i = 0; i < TJ; i++) w[i] = ld_real<T>(cb.inv_m_t, mo + (int64_t)k * JP + j0 + i);
+                load_row<T, TC>(io + (size_t)k * COLS + cc, b);
+#pragma unroll
+                for (int i = 0; i < TJ; i++)
+#pragma unroll
+                    for (int c = 0; c < TC; c++) O[i][c] = O[i][c] + w[i] * b[c];
             }
 #pragma unroll
             for (int i = 0; i < TJ; i++) {
@@ -620,8 +640,8 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
 }
 
 template <typename T>
-size_t cheb_inverse_m_smem(int N, int bk) {
-    return ((size_t)bk * 64 + (size_t)64 * (N | 1)) * sizeof(T);
+size_t cheb_inverse_m_smem(int N, int bk) {  // rank of the Γ fold ≤ 2: two s rows per input set
+    return ((size_t)(bk + 4) * 64 + (size_t)64 * (N | 1)) * sizeof(T);
 }
 
 // ====================================================================
