@@ -191,6 +191,9 @@ static int32_t build_grid(ss_grid *g) {
     // ---- rings (src/factory.jl:608-624) and FFT plans
     TwiddlePool pool;
     PlanSet plans;
+    // binary32 butterflies are issue-bound and keep Bluestein above 127; the FP64
+    // pipe favours direct prime passes up to 199
+    plans.max_prime = (g->tl == TL_F32) ? 127 : kMaxPrimeRadix;
     std::vector<double> phase;
     const int nring_sets = g->rlz ? 1 : nv;
     std::vector<RingDesc> rings(size_t(nring_sets) * iDim);

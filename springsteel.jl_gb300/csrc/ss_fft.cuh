@@ -124,31 +124,40 @@ __device__ __forceinline__ const void *tab_at(const void *pool, int64_t off) {
     return (const void *)((const typename Tab<T>::cplx_t *)pool + off);
 }
 
-// Radix-R pass for an odd prime R > 13 (up to kMaxPrimeRadix).  The inputs
-// are first multiplied in place by their twiddles (skipped when Ns = 1); then
-// each work item computes one conjugate output pair (s, R−s) of one butterfly
-// from the pairs a_q = v_q + v_{R−q}, b_q = v_q − v_{R−q}:
+// Radix-R pass for an odd prime R > 13 (up to kMaxPrimeRadix).  A first
+// sweep twiddles each butterfly's inputs (skipped when Ns = 1) and replaces
+// them in place by the pairs a_q = v_q + v_{R−q} (at q) and b_q = v_q − v_{R−q}
+// (at R−q), q = 1..(R−1)/2; then each work item computes one conjugate output
+// pair (s, R−s) of one butterfly:
 //   re = v_0 + Σ_q a_q cos(2πqs/R),  im = Σ_q b_q sin(2πqs/R),
-//   X_s = re ∓ i·im, X_{R−s} = re ± i·im  (upper signs forward), X_0 = Σ v_q.
-// cos/sin(2πe/R) are the N-point twiddles at e·N/R.  (R−1)/2 complex
-// multiply-adds per output instead of a length ≥ 2N−1 chirp-z convolution.
+//   X_s = re ∓ i·im, X_{R−s} = re ± i·im  (upper signs forward), X_0 = v_0 + Σ a_q.
+// cos/sin(2πe/R) are the N-point twiddles at e·N/R.  Four FMAs per term and
+// output pair instead of a length ≥ 2N−1 chirp-z convolution.
 template <int SIGN, typename T>
 __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N, int Ns, int R,
                            const void *__restrict__ tw, int nb, int bs) {
     const int NR = N / R, H = (R - 1) / 2;
     const int tstride = N / (Ns * R), rstep = N / R;
-    const float inv_ns = 1.0f / (float)Ns, inv_nr = 1.0f / (float)NR, inv_h1 = 1.0f / (float)(H + 1);
-    if (Ns > 1) {
-        for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
-            const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
-            const int q = div_small(e, NR, inv_nr), j = e - q * NR;
-            const int k = j - div_small(j, Ns, inv_ns) * Ns;
-            if (q > 0 && k > 0) {
-                cpx<T> w = ld_cplx<T>(tw, (int64_t)q * k * tstride);
-                if (SIGN > 0) w.y = -w.y;
-                cpx<T> *p = src + (size_t)bi * bs + e;
-                *p = c_mul(*p, w);
+    const float inv_ns = 1.0f / (float)Ns, inv_h = 1.0f / (float)H, inv_h1 = 1.0f / (float)(H + 1);
+    {
+        const int per = NR * H;
+        for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
+            const int bi = nb == 1 ? 0 : t / per, rest = t - bi * per;
+            const int j = div_small(rest, H, inv_h), q = rest - j * H + 1;
+            cpx<T> *sv = src + (size_t)bi * bs + j;
+            cpx<T> vq = sv[q * NR], vr = sv[(R - q) * NR];
+            if (Ns > 1) {
+                const int k = j - div_small(j, Ns, inv_ns) * Ns;
+                if (k > 0) {
+                    cpx<T> w1 = ld_cplx<T>(tw, (int64_t)q * k * tstride);
+                    cpx<T> w2 = ld_cplx<T>(tw, (int64_t)(R - q) * k * tstride);
+                    if (SIGN > 0) { w1.y = -w1.y; w2.y = -w2.y; }
+                    vq = c_mul(vq, w1);
+                    vr = c_mul(vr, w2);
+                }
             }
+            sv[q * NR] = c_add(vq, vr);
+            sv[(R - q) * NR] = c_sub(vq, vr);
         }
         __syncthreads();
     }
@@ -163,7 +172,7 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
         const cpx<T> x0 = sv[0];
         if (s == 0) {
             cpx<T> acc = x0;
-            for (int q = 1; q < R; q++) acc = c_add(acc, sv[q * NR]);
+            for (int q = 1; q <= H; q++) acc = c_add(acc, sv[q * NR]);
             d[idxD] = acc;
             continue;
         }
@@ -173,8 +182,7 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
             e += s;
             if (e >= R) e -= R;
             const cpx<T> w = ld_cplx<T>(tw, (int64_t)e * rstep);  // (cos, −sin)(2πe/R)
-            const cpx<T> vq = sv[q * NR], vr = sv[(R - q) * NR];
-            const cpx<T> a = c_add(vq, vr), b = c_sub(vq, vr);
+            const cpx<T> a = sv[q * NR], b = sv[(R - q) * NR];
             re.x = re.x + a.x * w.x;
             re.y = re.y + a.y * w.x;
             im.x = im.x - b.x * w.y;

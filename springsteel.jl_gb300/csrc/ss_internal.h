@@ -33,8 +33,10 @@ struct Status {
 // shared memory, or (N with a prime factor > 13) by Bluestein's chirp-z
 // convolution of smooth length M >= 2N-1.
 constexpr int kMaxRadices = 24;
-// largest odd prime handled by a direct radix pass; larger factors go through Bluestein
-constexpr int kMaxPrimeRadix = 127;
+// largest odd prime handled by a direct radix pass (≈ (R−1) FMAs per element,
+// below Bluestein's two length-≥2N FFTs up to about here); larger factors go
+// through Bluestein
+constexpr int kMaxPrimeRadix = 199;
 struct FftPlan {
     int N;
     int nrad;
@@ -140,6 +142,7 @@ struct PlanSet {
     std::vector<int64_t> utw_of_L;  // by L
     std::vector<int64_t> mtw_of_M;  // by M
     int max_smem_cplx = 0;          // largest complex buffer (N or M)
+    int max_prime = kMaxPrimeRadix; // direct prime passes up to here, Bluestein above
     int plan_for(int N, TwiddlePool &pool);
     int64_t unpack_for(int L, TwiddlePool &pool);
 };

@@ -7,6 +7,7 @@
 // src/CubicBSpline.jl:1000-1030, and of SItransform's 4-tap window,
 // :1554-1567), the Chebyshev tables (src/Chebyshev.jl:329-378, 991-1177) and
 // the FFT plans/twiddles.  Nothing here runs per transform.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -368,10 +369,10 @@ int64_t TwiddlePool::push(const std::vector<double> &ci) {
 // first pass they need no input twiddles), then 4s and 2, 3, 5, 7, 11, 13.
 // smooth_only (Bluestein lengths) admits 2, 3, 5, 7 only.  False when a prime
 // factor is not covered (the caller then uses Bluestein).
-static bool factor_radices(int n, int *rad, int &nrad, bool smooth_only) {
+static bool factor_radices(int n, int *rad, int &nrad, bool smooth_only, int max_prime = kMaxPrimeRadix) {
     nrad = 0;
     if (!smooth_only)
-        for (int f = 17; f <= kMaxPrimeRadix && n > 1; f += 2) {
+        for (int f = 17; f <= std::min(max_prime, kMaxPrimeRadix) && n > 1; f += 2) {
             bool prime = true;
             for (int d = 3; d * d <= f; d += 2)
                 if (f % d == 0) { prime = false; break; }
@@ -446,7 +447,7 @@ int PlanSet::plan_for(int N, TwiddlePool &pool) {
     FftPlan p;
     std::memset(&p, 0, sizeof p);
     p.N = N;
-    if (factor_radices(N, p.rad, p.nrad, false)) {
+    if (factor_radices(N, p.rad, p.nrad, false, max_prime)) {
         p.blu = 0;
         p.tw = pool.push_table(N, -1, N);
     } else {
