@@ -191,9 +191,11 @@ static int32_t build_grid(ss_grid *g) {
     // ---- rings (src/factory.jl:608-624) and FFT plans
     TwiddlePool pool;
     PlanSet plans;
-    // binary32 butterflies are issue-bound and keep Bluestein above 127; the FP64
-    // pipe favours direct prime passes up to 199
+    // binary32 butterflies are issue-bound and keep Bluestein above 127 (measured
+    // faster than Rader there); the FP64 pipe favours direct prime passes up to
+    // 199 and Rader above
     plans.max_prime = (g->tl == TL_F32) ? 127 : kMaxPrimeRadix;
+    plans.rader = g->tl != TL_F32;
     std::vector<double> phase;
     const int nring_sets = g->rlz ? 1 : nv;
     std::vector<RingDesc> rings(size_t(nring_sets) * iDim);

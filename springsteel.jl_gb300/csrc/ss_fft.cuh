@@ -199,11 +199,23 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
     }
 }
 
-// Stockham DFT over ping-pong buffers; returns the buffer holding the result.
+__device__ __forceinline__ int mod_pow_i(int b, int e, int m) {
+    int r = 1;
+    while (e > 0) {
+        if (e & 1) r = r * b % m;
+        b = b * b % m;
+        e >>= 1;
+    }
+    return r;
+}
+
+// Stockham passes rad[s_begin..nrad) over ping-pong buffers, Ns0 = product of the
+// radices already applied; returns the buffer holding the result.
 template <int SIGN, typename T>
-__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int nb, int bs) {
-    int Ns = 1;
-    for (int s = 0; s < nrad; s++) {
+__device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int nb,
+                                  int bs, int s_begin = 0, int Ns0 = 1) {
+    int Ns = Ns0;
+    for (int s = s_begin; s < nrad; s++) {
         const int R = rad[s];
         switch (R) {
         case 4: stockham_pass<4, SIGN>(a, b, N, Ns, tw, nb, bs); break;
@@ -224,12 +236,84 @@ __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nra
     return a;
 }
 
+// Radix-p pass by Rader's algorithm (p prime, first pass: Ns = 1, no input
+// twiddles).  Per butterfly j (NR = N/p of them):
+//   u_a = x_{g^a} (a < p−1) into dst[j(p−1) + a], x_0 into dst's tail dst[N + j];
+//   c = u ⊛ h by two (p−1)-point DFTs (inner plan) and H = DFT(h)/(p−1);
+//   X_0 = x_0 + DFT(u)_0 (kept in src's tail), X_{g^{−b}} = x_0 + c_b.
+// The inverse transform runs as conj(forward(conj x)).  The tails beyond the N
+// data entries are never touched by the inner passes.  Returns the buffer
+// holding the pass's outputs (either a or b).
+template <int SIGN, typename T>
+__device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl, const void *pool, int nb, int bs) {
+    const int p = pl.rp, P1 = p - 1, NR = N / p, g = pl.rg;
+    const float inv_p = 1.0f / (float)p, inv_p1 = 1.0f / (float)P1;
+    const void *H = tab_at<T>(pool, pl.rH);
+    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {  // gather: (j, a), a = p−1 → x_0
+        const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
+        const int j = div_small(e, p, inv_p), a = e - j * p;
+        const int q = a < P1 ? mod_pow_i(g, a, p) : 0;
+        cpx<T> v = src[(size_t)bi * bs + j + q * NR];
+        if (SIGN > 0) v.y = -v.y;
+        dst[(size_t)bi * bs + (a < P1 ? j * P1 + a : N + j)] = v;
+    }
+    __syncthreads();
+    cpx<T> *r2 = dst;
+    for (int bi = 0; bi < nb; bi++) {  // inner cyclic convolutions of one item at a time
+        cpx<T> *d0 = dst + (size_t)bi * bs, *s0 = src + (size_t)bi * bs;
+        cpx<T> *r1 = stockham_plain<-1, T>(d0, s0, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), NR, P1);
+        for (int e = threadIdx.x; e < NR * P1; e += blockDim.x) {
+            const int j = div_small(e, P1, inv_p1), k = e - j * P1;
+            const cpx<T> U = r1[e];
+            if (k == 0) s0[N + j] = c_add(d0[N + j], U);  // X_0 into src's tail
+            r1[e] = c_mul(U, ld_cplx<T>(H, k));
+        }
+        __syncthreads();
+        cpx<T> *other = (r1 == d0) ? s0 : d0;
+        cpx<T> *rr = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), NR, P1);
+        r2 = (rr == d0) ? dst : src;  // same choice for every item
+    }
+    cpx<T> *out = (r2 == dst) ? src : dst;
+    const int ginv = mod_pow_i(g, p - 2, p);
+    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {  // scatter: (j, b), b = p−1 → X_0
+        const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
+        const int j = div_small(e, p, inv_p), b = e - j * p;
+        const cpx<T> *rb = r2 + (size_t)bi * bs;
+        cpx<T> X;
+        int s;
+        if (b == P1) {
+            X = src[(size_t)bi * bs + N + j];
+            s = 0;
+        } else {
+            X = c_add(dst[(size_t)bi * bs + N + j], rb[j * P1 + b]);
+            s = mod_pow_i(ginv, b, p);
+        }
+        if (SIGN > 0) X.y = -X.y;
+        out[(size_t)bi * bs + j * p + s] = X;  // Ns = 1: butterfly j's outputs at j·p + s
+    }
+    __syncthreads();
+    return out;
+}
+
+// A plan's Stockham DFT: the Rader pass first when the plan has one, then the
+// remaining radix passes; returns the buffer holding the result.
+template <int SIGN, typename T>
+__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int nb, int bs,
+                            const FftPlan *pl, const void *pool) {
+    if (pl && pl->rp) {
+        cpx<T> *o = rader_pass<SIGN, T>(a, b, N, *pl, pool, nb, bs);
+        if (o != a) { b = a; a = o; }
+        return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, nb, bs, 1, pl->rp);
+    }
+    return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, nb, bs);
+}
+
 // Length-N DFTs of the nb sequences in `a` (sign SIGN), sequence i at a + i·bs.
 // Both buffers hold nb × fft_buffer_len(plan) entries (bs ≥ that length).
 // Returns the buffer with the results, laid out like the input.
 template <int SIGN, typename T>
 __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool, int nb = 1, int bs = 0) {
-    if (!p.blu) return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw), nb, bs);
+    if (!p.blu) return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw), nb, bs, &p, pool);
     const int N = p.N, M = p.M;
     const void *chirp = tab_at<T>(pool, p.chirp);
     const void *filt = tab_at<T>(pool, p.filt);
@@ -247,7 +331,7 @@ __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool,
         ab[k] = v;
     }
     __syncthreads();
-    cpx<T> *r = stockham<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
+    cpx<T> *r = stockham_plain<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
     for (int t = threadIdx.x; t < nb * M; t += blockDim.x) {
         const int bi = nb == 1 ? 0 : t / M, k = t - bi * M;
         cpx<T> *rb = r + (size_t)bi * bs;
@@ -255,7 +339,7 @@ __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool,
     }
     __syncthreads();
     cpx<T> *other = (r == a) ? b : a;
-    cpx<T> *q = stockham<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
+    cpx<T> *q = stockham_plain<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
     for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
         const int bi = nb == 1 ? 0 : t / N, k = t - bi * N;
         cpx<T> *qb = q + (size_t)bi * bs;

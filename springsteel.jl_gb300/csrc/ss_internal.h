@@ -49,6 +49,14 @@ struct FftPlan {
     int64_t mtw;     // pool offset of W_M^t, t < M
     int64_t chirp;   // pool offset of exp(-πi k²/N), k < N
     int64_t filt;    // pool offset of FFT_M(conj chirp filter)/M
+    // Rader pass for one prime factor p > the direct-pass limit (first radix of
+    // rad[], stored as p): generator g, the (p−1)-point inner plan, and
+    // H = FFT_{p−1}(h)/(p−1) with h_d = W_p^{g^{−d}}
+    int rp, rg;
+    int rnrad;
+    int rrad[kMaxRadices];
+    int64_t rtw;     // pool offset of W_{p−1}^t, t < p−1
+    int64_t rH;      // pool offset of H, p−1 entries
 };
 
 // One Fourier ring (src/factory.jl:608-624): L = 4+4ri points, kmax, bDim = 2ri+1.
@@ -142,11 +150,14 @@ struct PlanSet {
     std::vector<int64_t> utw_of_L;  // by L
     std::vector<int64_t> mtw_of_M;  // by M
     int max_smem_cplx = 0;          // largest complex buffer (N or M)
-    int max_prime = kMaxPrimeRadix; // direct prime passes up to here, Bluestein above
+    int max_prime = kMaxPrimeRadix; // direct prime passes up to here, Rader or Bluestein above
+    bool rader = true;              // Rader passes for larger primes (else Bluestein)
     int plan_for(int N, TwiddlePool &pool);
     int64_t unpack_for(int L, TwiddlePool &pool);
 };
 // complex entries of one ping-pong buffer of a plan
-SS_HD inline int fft_buffer_len(const FftPlan &p) { return p.blu ? p.M : p.N; }
+// complex entries of one ping-pong buffer: M (Bluestein), N + N/p (Rader: a tail
+// of N/p entries beyond the N data entries holds the x_0 terms), else N
+SS_HD inline int fft_buffer_len(const FftPlan &p) { return p.blu ? p.M : (p.rp ? p.N + p.N / p.rp : p.N); }
 
 }  // namespace ss

@@ -441,6 +441,74 @@ static void host_stockham(std::vector<std::complex<double>> &x, const int *rad, 
 }
 
 
+static long mod_pow(long b, long e, long m) {
+    long r = 1;
+    b %= m;
+    while (e > 0) {
+        if (e & 1) r = r * b % m;
+        b = b * b % m;
+        e >>= 1;
+    }
+    return r;
+}
+
+// smallest primitive root of the prime p
+static int primitive_root(int p) {
+    std::vector<int> qs;
+    int m = p - 1;
+    for (int d = 2; d * d <= m; d++)
+        if (m % d == 0) {
+            qs.push_back(d);
+            while (m % d == 0) m /= d;
+        }
+    if (m > 1) qs.push_back(m);
+    for (int g = 2; g < p; g++) {
+        bool ok = true;
+        for (int q : qs)
+            if (mod_pow(g, (p - 1) / q, p) == 1) { ok = false; break; }
+        if (ok) return g;
+    }
+    return 1;
+}
+
+// Rader plan: N = p·m with one prime p above max_prime, m and p − 1 covered by
+// direct radices.  The p-point DFTs become cyclic convolutions of length p − 1
+// (Rader, 1968): X_{g^{−b}} = x_0 + Σ_a x_{g^a} W_p^{g^{a−b}}.
+static bool rader_plan(int N, int max_prime, FftPlan &p, TwiddlePool &pool) {
+    int n = N, P = 1;
+    for (int d = 2; d * d <= n; d++)
+        while (n % d == 0) { P = std::max(P, d); n /= d; }
+    if (n > 1) P = std::max(P, n);
+    if (P <= max_prime || P > 4096) return false;
+    int nr = 0;
+    if (!factor_radices(N / P, p.rad + 1, nr, false, max_prime)) return false;
+    if (!factor_radices(P - 1, p.rrad, p.rnrad, false, max_prime)) return false;
+    p.rad[0] = P;
+    p.nrad = 1 + nr;
+    p.rp = P;
+    p.rg = primitive_root(P);
+    const int P1 = P - 1;
+    p.rtw = pool.push_table(P1, -1, P1);
+    // h_d = W_P^{g^{−d}}, H = DFT_{P−1}(h) / (P − 1) (forward sign)
+    std::vector<std::complex<double>> h(P1), root(P1);
+    const long ginv = mod_pow(p.rg, P - 2, P);
+    long e = 1;
+    for (int d = 0; d < P1; d++) {
+        h[d] = unit_root(e, P, -1);
+        e = e * ginv % P;
+    }
+    for (int t = 0; t < P1; t++) root[t] = unit_root(t, P1, -1);
+    std::vector<double> H(2 * (size_t)P1);
+    for (int k = 0; k < P1; k++) {
+        std::complex<double> acc = 0.0;
+        for (int d = 0; d < P1; d++) acc += h[d] * root[(size_t)d * k % P1];
+        H[2 * k] = acc.real() / P1;
+        H[2 * k + 1] = acc.imag() / P1;
+    }
+    p.rH = pool.push(H);
+    return true;
+}
+
 int PlanSet::plan_for(int N, TwiddlePool &pool) {
     if ((int)plan_of_N.size() <= N) plan_of_N.resize(N + 1, -1);
     if (plan_of_N[N] >= 0) return plan_of_N[N];
@@ -450,7 +518,12 @@ int PlanSet::plan_for(int N, TwiddlePool &pool) {
     if (factor_radices(N, p.rad, p.nrad, false, max_prime)) {
         p.blu = 0;
         p.tw = pool.push_table(N, -1, N);
+    } else if (rader && rader_plan(N, max_prime, p, pool)) {
+        p.blu = 0;
+        p.tw = pool.push_table(N, -1, N);
     } else {
+        std::memset(&p, 0, sizeof p);
+        p.N = N;
         p.blu = 1;
         int M = 2 * N - 1;
         for (;; M++)
