@@ -46,10 +46,110 @@ WORKLOADS = {
     # small case for profiling captures (same kernels, a few hundred MB)
     "rlz100-f64": dict(num_cells=100, kDim=32, nvars=2, precision="f64"),
     "rlz200-f32": dict(num_cells=200, kDim=64, nvars=2, precision="f32"),
+    # 64 uneven RL grids (50-400 cells, 1-4 variables) as one batch under a CUDA graph
+    "batch-rl64": dict(ngrids=64, nc_min=50, nc_max=400, nv_min=1, nv_max=4, precision="f64", seed=3),
+    "batch-rl64-f32": dict(ngrids=64, nc_min=50, nc_max=400, nv_min=1, nv_max=4, precision="f32", seed=3),
     # learned-preconditioner elliptic solve on the 200-cell RL grid (separate JSON line)
     "elliptic-rl200": dict(num_cells=200, rmax=100.0, train_fields=20000, train_random=20000, eval_seeds=1000,
                            k2_seed=5, restart=30, tol=1e-10),
 }
+
+
+def run_batch(args):
+    """Config 3's batched workload: one step = spectralTransform! + gridTransform! of
+    every grid of the batch (all variables, all 5 slots), replayed as one CUDA graph
+    with autotuned ring-kernel CTA sizes.  Also reported: the same grids as
+    individual calls (no graph), and e2e with every grid's slot 1 uploaded and all
+    slots downloaded per step."""
+    import torch
+
+    import springsteel_gpu as S
+    from springsteel_gpu import abi, fields
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    rng = np.random.default_rng(w["seed"] + rank)
+    grids, ups = [], []
+    nbytes = 0
+    host_dt = np.float32 if w["precision"] == "f32" else np.float64
+    for i in range(w["ngrids"]):
+        nc = int(rng.integers(w["nc_min"], w["nc_max"] + 1))
+        nv = int(rng.integers(w["nv_min"], w["nv_max"] + 1))
+        gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=float(nc), num_cells=nc,
+                                         vars={"v%d" % k: k + 1 for k in range(nv)}, precision=w["precision"])
+        g = S.createGrid(gp)
+        pts = S.getGridpoints(g)
+        u = np.empty((pts.shape[0], nv), order="F", dtype=host_dt)
+        for v in range(nv):
+            u[:, v] = fields.blob_sum(pts, seed=1000 * i + v, nblobs=4)
+        g.set_physical(u, slot=1)
+        grids.append(g)
+        ups.append(u)
+        nbytes += g.dims["n_physical"] * nv * (1 + 5) * np.dtype(host_dt).itemsize
+    lib = S.load_library()
+    batch = S.Batch(grids, autotune=True)
+    for _ in range(max(args.warmup, 3)):
+        batch.run(what=3, use_graph=True)
+    batch.synchronize()
+
+    def timed(fn, steps):  # wall clock between device-wide synchronisations
+        torch.cuda.synchronize()
+        for g in grids:
+            g.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        batch.synchronize()
+        for g in grids:
+            g.synchronize()
+        return (time.perf_counter() - t0) / steps
+
+    with ClockSampler(local) as clk:
+        t_batch = timed(lambda: batch.run(what=3, use_graph=True), args.steps)
+
+        def singles():
+            for g in grids:
+                S.spectralTransform_b(g)
+                S.gridTransform_b(g)
+
+        t_single = timed(singles, max(1, args.steps // 2))
+
+        pinned = [torch.from_numpy(np.ascontiguousarray(u.T)).pin_memory() for u in ups]
+        outs = [torch.empty(g.dims["n_physical"] * g.dims["nvars"] * g.dims["nslots"],
+                            dtype=torch.float32 if host_dt == np.float32 else torch.float64).pin_memory()
+                for g in grids]
+        dt_code = abi.SS_DTYPE_F32 if host_dt == np.float32 else abi.SS_DTYPE_F64
+
+        def e2e():
+            for g, h in zip(grids, pinned):
+                S._check(lib.ss_upload_physical(g.handle, C.c_void_p(h.data_ptr()), dt_code, 1, None))
+            batch.run(what=3, use_graph=True)
+            batch.synchronize()
+            for g, h in zip(grids, outs):
+                S._check(lib.ss_download_physical(g.handle, C.c_void_p(h.data_ptr()), dt_code, 0, None))
+
+        t_e2e = timed(e2e, max(1, min(args.steps, 3)))
+    h2d = sum(p.numel() * p.element_size() for p in pinned)
+    d2h = sum(o.numel() * o.element_size() for o in outs)
+    peak, peak_kind = _peaks()
+    line = {
+        "metric": "batched RL transforms/s (64 uneven grids, graph)", "value": 1.0 / t_batch,
+        "unit": "batch round trips/s", "n_gpus": ws, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if host_dt == np.float32 else "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "grids": len(grids),
+                   "cells": [g.params.num_cells for g in grids], "vars": [g.dims["nvars"] for g in grids]},
+        "individual_calls_ms": t_single * 1e3, "graph_speedup": t_single / t_batch,
+        "path_gbs": nbytes / t_batch / 1e9, "path_frac": nbytes / t_batch / 1e9 / peak, "peak": peak,
+        "peak_source": peak_kind, "clocks": clk.summary(),
+        "e2e": {"value": 1.0 / t_e2e, "unit": "batch round trips/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+    }
+    batch.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
 
 
 def run_elliptic(args):
@@ -459,6 +559,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "elliptic-rl200":
         return run_elliptic(args)
+    if args.workload.startswith("batch-"):
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

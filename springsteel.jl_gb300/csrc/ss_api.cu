@@ -370,6 +370,16 @@ static int32_t build_grid(ss_grid *g) {
         if ((st = dev_alloc(g, &g->C, size_t(nv) * bk * jDim * es))) return st;
         if ((st = dev_alloc(g, &g->H, size_t(5) * nv * bk * jDim * es))) return st;
     }
+    if (g->tl == TL_F32) {
+        // the binary32 SAtransform! streams its vectors through two scratch
+        // arrays; F (free during gridTransform!) and phys (overwritten by it)
+        // serve when they are large enough
+        const size_t need = size_t(g->nitems) * d.b_iDim * g->nslots_z;
+        g->sa_x = size_t(g->nitems) * g->frows >= need ? g->F : nullptr;
+        g->sa_y = size_t(d.n_physical) * nv * d.nslots >= need ? g->phys : nullptr;
+        if (!g->sa_x && (st = dev_alloc(g, &g->sa_x, need * sizeof(float), false))) return st;
+        if (!g->sa_y && (st = dev_alloc(g, &g->sa_y, need * sizeof(float), false))) return st;
+    }
     {
         std::vector<double> ones_f(size_t(nv) * (K + 1), 1.0), ones_c(size_t(nv) * bk, 1.0);
         if ((st = upload_vec(g, &g->d_fw, ones_f))) return st;
@@ -445,7 +455,11 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st, int coeffs = 0) {
     if (g->tl != TL_F64) smem += size_t(32) * A.ld * ssz;  // FP32 residuals / df64 coefficients
     {
         StageScope sc(g, SS_STAGE_SA_SI, st);
-        CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
+        if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
+            CUDA_TRY((launch_sa_si_f32<P>(A, g->nitems, (float *)g->sa_x, (float *)g->sa_y, st)));
+        } else {
+            CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
+        }
         g->launches[SS_STAGE_SA_SI]++;
     }
 

@@ -32,6 +32,7 @@ struct ss_grid {
     int64_t frows = 0;
 
     void *phys = nullptr, *spec = nullptr, *C = nullptr, *F = nullptr, *G = nullptr, *H = nullptr;
+    void *sa_x = nullptr, *sa_y = nullptr;  // binary32 SAtransform! scratch (alias F / phys when large enough)
     void *stage = nullptr;
     size_t stage_bytes = 0;
 

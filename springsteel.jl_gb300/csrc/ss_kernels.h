@@ -113,6 +113,10 @@ template <typename P, typename T>
 cudaError_t launch_sb_project(const SbLaunch &S, int nitems, cudaStream_t st);
 template <typename P, typename T>
 cudaError_t launch_sa_si(const SaLaunch &A, int nitems, size_t smem, cudaStream_t st);
+// binary32 grids: slot-parallel solve over the scratch arrays X, Y, each
+// nitems × b × nslots_z floats (ss_sa_f32.cu)
+template <typename P>
+cudaError_t launch_sa_si_f32(const SaLaunch &A, int nitems, float *X, float *Y, cudaStream_t st);
 template <typename P, typename T>
 cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st, int N);
 template <typename P, typename T>
