@@ -192,10 +192,17 @@ static int32_t build_grid(ss_grid *g) {
     TwiddlePool pool;
     PlanSet plans;
     // binary32 butterflies are issue-bound and keep Bluestein above 127 (measured
-    // faster than Rader there); the FP64 pipe favours direct prime passes up to
-    // 199 and Rader above
-    plans.max_prime = (g->tl == TL_F32) ? 127 : kMaxPrimeRadix;
+    // faster than Rader there at limits 41-127); the FP64 pipe favours direct
+    // prime passes up to 67 and Rader above (measured on the 200-cell RLZ grid:
+    // ring_inverse 46.9 ms at 67, 47.1 at 101, 49.2 at 199, 48.0 at 41)
+    plans.max_prime = (g->tl == TL_F32) ? 127 : 67;
     plans.rader = g->tl != TL_F32;
+    // tuning override of the direct-pass limit (odd, 13 ≤ limit ≤ 199)
+    if (const char *e = std::getenv("SS_FFT_MAX_PRIME")) {
+        const int v = std::atoi(e);
+        if (v >= 13 && v <= kMaxPrimeRadix) plans.max_prime = v;
+    }
+    if (const char *e = std::getenv("SS_FFT_RADER")) plans.rader = std::atoi(e) != 0;
     std::vector<double> phase;
     const int nring_sets = g->rlz ? 1 : nv;
     std::vector<RingDesc> rings(size_t(nring_sets) * iDim);

@@ -471,8 +471,8 @@ static int primitive_root(int p) {
     return 1;
 }
 
-// Rader plan: N = p·m with one prime p above max_prime, m and p − 1 covered by
-// direct radices.  The p-point DFTs become cyclic convolutions of length p − 1
+// Rader plan: N = p·m with p the largest prime factor, above max_prime; m and
+// p − 1 covered by direct radices.  The p-point DFTs become cyclic convolutions of length p − 1
 // (Rader, 1968): X_{g^{−b}} = x_0 + Σ_a x_{g^a} W_p^{g^{a−b}}.
 static bool rader_plan(int N, int max_prime, FftPlan &p, TwiddlePool &pool) {
     int n = N, P = 1;
@@ -481,8 +481,9 @@ static bool rader_plan(int N, int max_prime, FftPlan &p, TwiddlePool &pool) {
     if (n > 1) P = std::max(P, n);
     if (P <= max_prime || P > 4096) return false;
     int nr = 0;
-    if (!factor_radices(N / P, p.rad + 1, nr, false, max_prime)) return false;
-    if (!factor_radices(P - 1, p.rrad, p.rnrad, false, max_prime)) return false;
+    // the cofactor and the inner length take direct passes up to the hard limit
+    if (!factor_radices(N / P, p.rad + 1, nr, false, kMaxPrimeRadix)) return false;
+    if (!factor_radices(P - 1, p.rrad, p.rnrad, false, kMaxPrimeRadix)) return false;
     p.rad[0] = P;
     p.nrad = 1 + nr;
     p.rp = P;
