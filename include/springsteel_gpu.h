@@ -167,6 +167,21 @@ int32_t ss_spectral_transform(ss_grid *grid, void *stream);
  * (RL: f, ∂r, ∂rr, ∂λ, ∂λλ; RLZ adds ∂z, ∂zz).  Asynchronous on `stream`. */
 int32_t ss_grid_transform(ss_grid *grid, void *stream);
 
+/* The same transforms with the physical array in host memory, as the
+ * reference's spectralTransform!(grid) / gridTransform!(grid) operate on
+ * grid.physical (src/transforms_cylindrical.jl:159-222, 259-428).  The grid's
+ * rings are split into radial chunks of about equal point counts; each
+ * chunk's columns move between host and device on a second stream while the
+ * next chunk computes (one strided copy per chunk).  `host_slot1` holds
+ * physical slot 1 (np × nvars), `host_all` receives every slot (nslots × nvars
+ * × np), both in `dtype`.  from_host returns once the host buffer may be
+ * reused (the transform itself stays queued on `stream`); to_host returns with
+ * the result in `host_all`.  Page-locked host buffers give full overlap; with
+ * a `dtype` other than the grid's the calls copy and transform in sequence. */
+int32_t ss_spectral_transform_from_host(ss_grid *grid, const void *host_slot1, int32_t dtype,
+                                        void *stream);
+int32_t ss_grid_transform_to_host(ss_grid *grid, void *host_all, int32_t dtype, void *stream);
+
 /* Spectral filter weights (applyFilter!, src/filtering.jl:262-428): the host
  * evaluates the reference's _filter_weight per wavenumber (kDim_wn+1 values)
  * and per Chebyshev mode (b_kDim values); NULL clears that filter. */

@@ -108,8 +108,11 @@ static int32_t upload_bytes(ss_grid *g, const void **dst, const std::vector<unsi
 static void free_grid(ss_grid *g) {
     if (!g) return;
     if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->copy_stream) cudaStreamSynchronize(g->copy_stream);
     for (cudaEvent_t e : g->ev_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : g->chunk_ev) cudaEventDestroy(e);
     for (void *p : g->allocs) cudaFree(p);
+    if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
@@ -284,6 +287,31 @@ static int32_t build_grid(ss_grid *g) {
         }
         (void)maxsm;
         if ((st = upload_vec(g, &g->d_ring_list, order))) return st;
+
+        // radial chunks of about equal point counts for the host-overlapped
+        // transforms; within a chunk the rings keep their bucket order
+        g->ring_jofs.resize(iDim + 1);
+        for (int r = 0; r < iDim; r++) g->ring_jofs[r] = rings[r].jofs;
+        g->ring_jofs[iDim] = rings[iDim - 1].jofs + rings[iDim - 1].L;
+        const int nch = std::min(kHostChunks, iDim);
+        g->chunk_r0.assign(1, 0);
+        for (int c = 1; c < nch; c++) {
+            const int64_t target = g->ring_jofs[iDim] * c / nch;
+            int r = g->chunk_r0.back() + 1;
+            while (r < iDim && g->ring_jofs[r] < target) r++;
+            if (r < iDim) g->chunk_r0.push_back(r);
+        }
+        g->chunk_r0.push_back(iDim);
+        std::vector<int> clist;
+        g->chunk_seg.assign(g->chunk_r0.size() - 1, {});
+        for (size_t c = 0; c + 1 < g->chunk_r0.size(); c++)
+            for (const RingBucket &bkt : g->buckets) {
+                const int off = (int)clist.size();
+                for (int q = bkt.offset; q < bkt.offset + bkt.count; q++)
+                    if (order[q] >= g->chunk_r0[c] && order[q] < g->chunk_r0[c + 1]) clist.push_back(order[q]);
+                g->chunk_seg[c].push_back({off, (int)clist.size() - off});
+            }
+        if ((st = upload_vec(g, &g->d_ring_list_chunks, clist))) return st;
     }
 
     // ---- Chebyshev columns (src/factory.jl:722-728)
@@ -398,20 +426,46 @@ static int32_t build_grid(ss_grid *g) {
 }
 
 // ---------------------------------------------------------------- launches
-template <typename P, typename T>
-static int32_t run_forward(ss_grid *g, cudaStream_t st) {
-    const ss_dims &d = g->d;
-    const int nv = (int)d.nvars, bk = (int)d.b_kDim;
-    if (g->rlz) {
-        ChebLaunch Cl{};
-        Cl.in = g->phys; Cl.out = g->C; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
-        Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = bk; Cl.nvars = nv;
-        const int N = (int)d.kDim, half = (N + 1) / 2;
-        size_t smem = (size_t(64) * (N | 1) + size_t(bk) * half) * sizeof(T);
-        StageScope sc(g, SS_STAGE_CHEB_FWD, st);
-        CUDA_TRY((launch_cheb_forward<P, T>(Cl, smem, st, N)));
-        g->launches[SS_STAGE_CHEB_FWD]++;
+// Every stage launches either over the whole grid or over one radial chunk
+// (rings [chunk_r0[c], chunk_r0[c+1]), i.e. physical columns
+// [ring_jofs[r0], ring_jofs[r1])).  The host-overlapped transforms run the
+// ring and Chebyshev stages chunk by chunk and move each chunk's physical
+// columns between host and device on copy_stream while the next chunk
+// computes; a chunk of every (slot, variable) plane is one strided 2D copy.
+template <typename Fn>
+static int32_t for_ring_segments(ss_grid *g, int chunk, Fn fn) {
+    for (size_t b = 0; b < g->buckets.size(); b++) {
+        const RingBucket &bkt = g->buckets[b];
+        int32_t st = SS_OK;
+        if (chunk < 0) st = fn(g->d_ring_list + bkt.offset, bkt.count, bkt);
+        else if (g->chunk_seg[chunk][b].second > 0)
+            st = fn(g->d_ring_list_chunks + g->chunk_seg[chunk][b].first, g->chunk_seg[chunk][b].second, bkt);
+        if (st) return st;
     }
+    return SS_OK;
+}
+static int64_t chunk_col(const ss_grid *g, int chunk, int end) {
+    return chunk < 0 ? (end ? g->d.jDim : 0) : g->ring_jofs[g->chunk_r0[chunk + end]];
+}
+
+template <typename P, typename T>
+static int32_t fwd_columns(ss_grid *g, cudaStream_t st, int chunk) {
+    const ss_dims &d = g->d;
+    ChebLaunch Cl{};
+    Cl.in = g->phys; Cl.out = g->C; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
+    Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = (int)d.b_kDim; Cl.nvars = (int)d.nvars;
+    Cl.col0 = chunk_col(g, chunk, 0); Cl.col1 = chunk_col(g, chunk, 1);
+    const int N = (int)d.kDim, half = (N + 1) / 2;
+    size_t smem = (size_t(64) * (N | 1) + size_t(Cl.bk) * half) * sizeof(T);
+    StageScope sc(g, SS_STAGE_CHEB_FWD, st);
+    CUDA_TRY((launch_cheb_forward<P, T>(Cl, smem, st, N)));
+    g->launches[SS_STAGE_CHEB_FWD]++;
+    return SS_OK;
+}
+
+template <typename P, typename T>
+static int32_t fwd_rings(ss_grid *g, cudaStream_t st, int chunk) {
+    const ss_dims &d = g->d;
     RingLaunch L{};
     L.rings = g->d_rings;
     L.ring_var_stride = g->rlz ? 0 : d.iDim;
@@ -420,56 +474,60 @@ static int32_t run_forward(ss_grid *g, cudaStream_t st) {
     L.out = g->F;
     L.in_item_stride = d.n_physical;
     L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
-    L.nitems = g->nitems; L.nvars = nv; L.bk = bk; L.rlz = g->rlz;
-    {
-        StageScope sc(g, SS_STAGE_RING_FWD, st);
-        for (const RingBucket &bkt : g->buckets) {
-            L.ring_list = g->d_ring_list + bkt.offset;
-            size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
-            L.ib = ring_batch(smem, g->nitems, bkt.count, 4 * g->sms, g->ring_threads_fwd, bkt.max_buf);
-            CUDA_TRY((launch_ring_forward<P, T>(L, bkt.count, g->nitems, smem, g->ring_threads_fwd, st)));
-            g->launches[SS_STAGE_RING_FWD]++;
-        }
-    }
+    L.nitems = g->nitems; L.nvars = (int)d.nvars; L.bk = (int)d.b_kDim; L.rlz = g->rlz;
+    StageScope sc(g, SS_STAGE_RING_FWD, st);
+    return for_ring_segments(g, chunk, [&](const int *list, int count, const RingBucket &bkt) -> int32_t {
+        L.ring_list = list;
+        size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
+        L.ib = ring_batch(smem, g->nitems, count, 4 * g->sms, g->ring_threads_fwd, bkt.max_buf);
+        CUDA_TRY((launch_ring_forward<P, T>(L, count, g->nitems, smem, g->ring_threads_fwd, st)));
+        g->launches[SS_STAGE_RING_FWD]++;
+        return SS_OK;
+    });
+}
+
+template <typename P, typename T>
+static int32_t fwd_sb(ss_grid *g, cudaStream_t st) {
+    const ss_dims &d = g->d;
     SbLaunch S{};
     S.F = g->F; S.spec = g->spec; S.spl = g->d_spl; S.fofs = g->d_fofs;
     S.fw = g->filtered ? g->d_fw : nullptr;
     S.cw = g->filtered ? g->d_cw : nullptr;
     S.frows = g->frows; S.nspec = d.n_spectral;
     S.iDim = (int)d.iDim; S.b = (int)d.b_iDim; S.mubar = g->p.mubar; S.pOL = g->pOL; S.K = (int)d.kDim_wn;
-    S.nslots_z = g->nslots_z; S.bk = bk; S.filtered = g->filtered;
-    {
-        StageScope sc(g, SS_STAGE_SB, st);
-        CUDA_TRY((launch_sb_project<P, T>(S, g->nitems, st)));
-        g->launches[SS_STAGE_SB]++;
-    }
+    S.nslots_z = g->nslots_z; S.bk = (int)d.b_kDim; S.filtered = g->filtered;
+    StageScope sc(g, SS_STAGE_SB, st);
+    CUDA_TRY((launch_sb_project<P, T>(S, g->nitems, st)));
+    g->launches[SS_STAGE_SB]++;
     return SS_OK;
 }
 
 template <typename P, typename T>
-static int32_t run_inverse(ss_grid *g, cudaStream_t st, int coeffs = 0) {
+static int32_t inv_sa(ss_grid *g, cudaStream_t st, int coeffs) {
     const ss_dims &d = g->d;
-    const int nv = (int)d.nvars, bk = (int)d.b_kDim;
     SaLaunch A{};
     A.spec = g->spec; A.G = g->G; A.spl = g->d_spl; A.fofs = g->d_fofs; A.ahat = g->d_ahat;
     A.frows = g->frows; A.nspec = d.n_spectral; A.nblocks = d.n_blocks;
     A.iDim = (int)d.iDim; A.b = (int)d.b_iDim; A.ld = (A.b % 2) ? A.b : A.b + 1;
-    A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = bk; A.nitems = g->nitems; A.coeffs = coeffs;
+    A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = (int)d.b_kDim; A.nitems = g->nitems; A.coeffs = coeffs;
     int nmax = 0;
     for (auto &sh : g->spl_host) nmax = std::max(nmax, sh.Min);
     const size_t ssz = (sizeof(T) == 4) ? 4 : 8;  // solve type: float (FP32 mode) or double
     size_t smem = (size_t(32) * A.ld + size_t(5) * nmax) * ssz;
     if (g->tl != TL_F64) smem += size_t(32) * A.ld * ssz;  // FP32 residuals / df64 coefficients
-    {
-        StageScope sc(g, SS_STAGE_SA_SI, st);
-        if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
-            CUDA_TRY((launch_sa_si_f32<P>(A, g->nitems, (float *)g->sa_x, (float *)g->sa_y, st)));
-        } else {
-            CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
-        }
-        g->launches[SS_STAGE_SA_SI]++;
+    StageScope sc(g, SS_STAGE_SA_SI, st);
+    if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
+        CUDA_TRY((launch_sa_si_f32<P>(A, g->nitems, (float *)g->sa_x, (float *)g->sa_y, st)));
+    } else {
+        CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
     }
+    g->launches[SS_STAGE_SA_SI]++;
+    return SS_OK;
+}
 
+template <typename P, typename T>
+static int32_t inv_rings(ss_grid *g, cudaStream_t st, int chunk) {
+    const ss_dims &d = g->d;
     RingLaunch L{};
     L.rings = g->d_rings;
     L.ring_var_stride = g->rlz ? 0 : d.iDim;
@@ -477,27 +535,107 @@ static int32_t run_inverse(ss_grid *g, cudaStream_t st, int coeffs = 0) {
     L.in = g->G;
     L.out = g->rlz ? g->H : g->phys;
     L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
-    L.nitems = g->nitems; L.nvars = nv; L.bk = bk; L.rlz = g->rlz;
-    {
-        StageScope sc(g, SS_STAGE_RING_INV, st);
-        for (const RingBucket &bkt : g->buckets) {
-            L.ring_list = g->d_ring_list + bkt.offset;
-            size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
-            L.ib = ring_batch(sm, g->nitems, bkt.count, 4 * g->sms, g->ring_threads_inv, bkt.max_buf);
-            CUDA_TRY((launch_ring_inverse<P, T>(L, bkt.count, g->nitems, sm, g->ring_threads_inv, st)));
-            g->launches[SS_STAGE_RING_INV]++;
-        }
+    L.nitems = g->nitems; L.nvars = (int)d.nvars; L.bk = (int)d.b_kDim; L.rlz = g->rlz;
+    StageScope sc(g, SS_STAGE_RING_INV, st);
+    return for_ring_segments(g, chunk, [&](const int *list, int count, const RingBucket &bkt) -> int32_t {
+        L.ring_list = list;
+        size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
+        L.ib = ring_batch(sm, g->nitems, count, 4 * g->sms, g->ring_threads_inv, bkt.max_buf);
+        CUDA_TRY((launch_ring_inverse<P, T>(L, count, g->nitems, sm, g->ring_threads_inv, st)));
+        g->launches[SS_STAGE_RING_INV]++;
+        return SS_OK;
+    });
+}
+
+template <typename P, typename T>
+static int32_t inv_columns(ss_grid *g, cudaStream_t st, int chunk) {
+    const ss_dims &d = g->d;
+    ChebLaunch Cl{};
+    Cl.in = g->H; Cl.out = g->phys; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
+    Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = (int)d.b_kDim; Cl.nvars = (int)d.nvars;
+    Cl.col0 = chunk_col(g, chunk, 0); Cl.col1 = chunk_col(g, chunk, 1);
+    const int N = (int)d.kDim;
+    StageScope sc(g, SS_STAGE_CHEB_INV, st);
+    CUDA_TRY((launch_cheb_inverse<P, T>(Cl, 0, st, N)));
+    g->launches[SS_STAGE_CHEB_INV]++;
+    return SS_OK;
+}
+
+static int32_t ensure_copy_stream(ss_grid *g) {
+    if (!g->copy_stream) CUDA_TRY(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    while (g->chunk_ev.size() < g->chunk_r0.size()) {  // one per chunk, one to join the streams
+        cudaEvent_t e = nullptr;
+        CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        g->chunk_ev.push_back(e);
     }
-    if (g->rlz) {
-        ChebLaunch Cl{};
-        Cl.in = g->H; Cl.out = g->phys; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
-        Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = bk; Cl.nvars = nv;
-        const int N = (int)d.kDim, half = (N + 1) / 2, ne = (N + 1) / 2, no = std::max(N / 2, 1);
-        size_t sm = (size_t(128) * (N | 1) + size_t(half) * ne + size_t(half) * no + size_t(64) * (bk | 1)) * sizeof(T);
-        StageScope sc(g, SS_STAGE_CHEB_INV, st);
-        CUDA_TRY((launch_cheb_inverse<P, T>(Cl, sm, st, N)));
-        g->launches[SS_STAGE_CHEB_INV]++;
+    return SS_OK;
+}
+// physical columns of one chunk in `rows` (slot, variable) planes from the
+// first: one linear copy per plane (measured faster than one pitched copy
+// while long kernels occupy the SMs)
+static cudaError_t copy_chunk(ss_grid *g, int chunk, void *host, bool to_host, int rows, cudaStream_t s) {
+    const size_t es = g->esz, kz = (size_t)g->d.kDim, pitch = size_t(g->d.n_physical) * es;
+    const size_t off = size_t(chunk_col(g, chunk, 0)) * kz * es;
+    const size_t width = size_t(chunk_col(g, chunk, 1) - chunk_col(g, chunk, 0)) * kz * es;
+    if (width == 0) return cudaSuccess;
+    for (int row = 0; row < rows; row++) {
+        char *dev = (char *)g->phys + off + row * pitch, *h = (char *)host + off + row * pitch;
+        const cudaError_t e = to_host ? cudaMemcpyAsync(h, dev, width, cudaMemcpyDeviceToHost, s)
+                                      : cudaMemcpyAsync(dev, h, width, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
     }
+    return cudaSuccess;
+}
+
+template <typename P, typename T>
+static int32_t run_forward(ss_grid *g, cudaStream_t st, const void *host_slot1 = nullptr) {
+    int32_t rc;
+    if (!host_slot1) {
+        if (g->rlz && (rc = fwd_columns<P, T>(g, st, -1))) return rc;
+        if ((rc = fwd_rings<P, T>(g, st, -1))) return rc;
+        return fwd_sb<P, T>(g, st);
+    }
+    if ((rc = ensure_copy_stream(g))) return rc;
+    const int nch = (int)g->chunk_r0.size() - 1;
+    // the copies start after the work already queued on the stream (it may read phys)
+    CUDA_TRY(cudaEventRecord(g->chunk_ev[nch], st));
+    CUDA_TRY(cudaStreamWaitEvent(g->copy_stream, g->chunk_ev[nch], 0));
+    for (int c = 0; c < nch; c++) {
+        CUDA_TRY(copy_chunk(g, c, (void *)host_slot1, false, (int)g->d.nvars, g->copy_stream));
+        CUDA_TRY(cudaEventRecord(g->chunk_ev[c], g->copy_stream));
+        CUDA_TRY(cudaStreamWaitEvent(st, g->chunk_ev[c], 0));
+        if (g->rlz && (rc = fwd_columns<P, T>(g, st, c))) return rc;
+        if ((rc = fwd_rings<P, T>(g, st, c))) return rc;
+    }
+    return fwd_sb<P, T>(g, st);
+}
+
+template <typename P, typename T>
+static int32_t run_inverse(ss_grid *g, cudaStream_t st, int coeffs = 0, void *host_all = nullptr) {
+    int32_t rc;
+    if ((rc = inv_sa<P, T>(g, st, coeffs))) return rc;
+    if (!host_all) {
+        if ((rc = inv_rings<P, T>(g, st, -1))) return rc;
+        return g->rlz ? inv_columns<P, T>(g, st, -1) : SS_OK;
+    }
+    if ((rc = ensure_copy_stream(g))) return rc;
+    const int nch = (int)g->chunk_r0.size() - 1;
+    // every chunk's compute is queued before its copies, so that a pageable
+    // host buffer (whose copies return to the caller only when done) still
+    // overlaps the remaining chunks
+    for (int c = 0; c < nch; c++) {
+        if ((rc = inv_rings<P, T>(g, st, c))) return rc;
+        if (g->rlz && (rc = inv_columns<P, T>(g, st, c))) return rc;
+        CUDA_TRY(cudaEventRecord(g->chunk_ev[c], st));
+    }
+    const int rows = (int)(g->d.nslots * g->d.nvars);
+    for (int c = 0; c < nch; c++) {
+        CUDA_TRY(cudaStreamWaitEvent(g->copy_stream, g->chunk_ev[c], 0));
+        CUDA_TRY(copy_chunk(g, c, host_all, true, rows, g->copy_stream));
+    }
+    // later work on the stream (which may overwrite phys) waits for the copies
+    CUDA_TRY(cudaEventRecord(g->chunk_ev[nch], g->copy_stream));
+    CUDA_TRY(cudaStreamWaitEvent(st, g->chunk_ev[nch], 0));
     return SS_OK;
 }
 
@@ -516,6 +654,16 @@ int32_t grid_inverse_coeffs(ss_grid *g, cudaStream_t s) {
     if (g->tl == TL_DF64) return run_inverse<double, df64>(g, s, 1);
     if (g->tl == TL_F64) return run_inverse<double, double>(g, s, 1);
     return run_inverse<float, float>(g, s, 1);
+}
+static int32_t grid_forward_host(ss_grid *g, cudaStream_t s, const void *host_slot1) {
+    if (g->tl == TL_DF64) return run_forward<double, df64>(g, s, host_slot1);
+    if (g->tl == TL_F64) return run_forward<double, double>(g, s, host_slot1);
+    return run_forward<float, float>(g, s, host_slot1);
+}
+static int32_t grid_inverse_host(ss_grid *g, cudaStream_t s, void *host_all) {
+    if (g->tl == TL_DF64) return run_inverse<double, df64>(g, s, 0, host_all);
+    if (g->tl == TL_F64) return run_inverse<double, double>(g, s, 0, host_all);
+    return run_inverse<float, float>(g, s, 0, host_all);
 }
 }  // namespace ss
 
@@ -706,6 +854,35 @@ int32_t ss_spectral_transform(ss_grid *g, void *stream) {
 int32_t ss_grid_transform(ss_grid *g, void *stream) {
     CHECK_GRID(g);
     return grid_inverse(g, pick(g, stream));
+}
+
+int32_t ss_spectral_transform_from_host(ss_grid *g, const void *host_slot1, int32_t dtype, void *stream) {
+    CHECK_GRID(g);
+    if (!host_slot1 || (dtype != SS_DTYPE_F64 && dtype != SS_DTYPE_F32)) { set_error("bad host buffer or dtype"); return SS_BAD_ARG; }
+    cudaStream_t s = pick(g, stream);
+    if ((dtype == SS_DTYPE_F64 ? 8u : 4u) != g->esz) {  // converting copy: upload, then transform
+        int32_t rc = ss_upload_physical(g, host_slot1, dtype, 1, stream);
+        return rc ? rc : grid_forward(g, s);
+    }
+    int32_t rc = grid_forward_host(g, s, host_slot1);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(g->copy_stream));  // the host buffer is free again
+    return SS_OK;
+}
+
+int32_t ss_grid_transform_to_host(ss_grid *g, void *host_all, int32_t dtype, void *stream) {
+    CHECK_GRID(g);
+    if (!host_all || (dtype != SS_DTYPE_F64 && dtype != SS_DTYPE_F32)) { set_error("bad host buffer or dtype"); return SS_BAD_ARG; }
+    cudaStream_t s = pick(g, stream);
+    if ((dtype == SS_DTYPE_F64 ? 8u : 4u) != g->esz) {  // converting copy: transform, then download
+        int32_t rc = grid_inverse(g, s);
+        return rc ? rc : ss_download_physical(g, host_all, dtype, 0, stream);
+    }
+    int32_t rc = grid_inverse_host(g, s, host_all);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(g->copy_stream));
+    CUDA_TRY(cudaGetLastError());
+    return SS_OK;
 }
 
 int32_t ss_grid_set_filter(ss_grid *g, int32_t var, const double *fw, const double *cw) {

@@ -4,11 +4,16 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ss_internal.h"
 
 using namespace ss;
+
+// radial chunks of the host-overlapped transforms (copies of one chunk run
+// while the next one computes)
+constexpr int kHostChunks = 4;
 
 struct RingBucket {
     int offset;   // into the ring list
@@ -48,6 +53,15 @@ struct ss_grid {
     int ring_threads_fwd = 256, ring_threads_inv = 256;  // CTA size of the ring kernels (autotuned by batches)
     int sms = 152;                                        // SMs of the grid's device
     std::vector<RingBucket> buckets;
+    // radial chunks of the host-overlapped transforms: chunk c holds rings
+    // [chunk_r0[c], chunk_r0[c+1]); its rings of bucket b are the segment
+    // chunk_seg[c][b] = (offset, count) of d_ring_list_chunks
+    std::vector<int> chunk_r0;
+    std::vector<std::vector<std::pair<int, int>>> chunk_seg;
+    int *d_ring_list_chunks = nullptr;
+    std::vector<int64_t> ring_jofs;  // first ring point of every ring, jDim at the end
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> chunk_ev;
     std::vector<void *> allocs;
     std::vector<SplineHost> spl_host;
     // stage instrumentation

@@ -445,10 +445,10 @@ __global__ void __launch_bounds__(128) cheb_forward_tiled_kernel(ChebLaunch C) {
     // tables once per CTA (host-transposed: coalesced)
     for (int e = threadIdx.x; e < half * KEP; e += blockDim.x) fe[e] = ld_real<T>(cb.fwd_et_t, e);
     for (int e = threadIdx.x; e < half * KOP; e += blockDim.x) fo[e] = ld_real<T>(cb.fwd_ot_t, e);
-    const int64_t nblk = (C.jDim + COLS - 1) / COLS;
+    const int64_t nblk = (C.col1 - C.col0 + COLS - 1) / COLS;
     for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
-    const int64_t c0 = blk * COLS;
-    const int ncol = (int)((C.jDim - c0) < COLS ? (C.jDim - c0) : COLS);
+    const int64_t c0 = C.col0 + blk * COLS;
+    const int ncol = (int)((C.col1 - c0) < COLS ? (C.col1 - c0) : COLS);
     const P *in = (const P *)C.in + (size_t)v * C.np + c0 * N;
     if constexpr (std::is_same<P, T>::value) {
         for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) cp_async<sizeof(T)>(xs + (e / N) * ldx + (e % N), in + e);
@@ -553,8 +553,8 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
     T *xe = reinterpret_cast<T *>(smem_raw);  // Ke × COLS: even inputs b_{2i'}, then s = Uᵀ b
     T *xo = xe + (size_t)Ke * COLS;            // Ko × COLS: odd inputs b_{2i'+1}, then s
     T *us = xo + (size_t)Ko * COLS;            // COLS × ldn outputs
-    const int64_t c0 = (int64_t)blockIdx.x * COLS;
-    const int ncol = (int)((C.jDim - c0) < COLS ? (C.jDim - c0) : COLS);
+    const int64_t c0 = C.col0 + (int64_t)blockIdx.x * COLS;
+    const int ncol = (int)((C.col1 - c0) < COLS ? (C.col1 - c0) : COLS);
     for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
         if (c < ncol) {
             const int64_t q = c0 + c;
@@ -711,7 +711,8 @@ cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t s
     (void)smem;
     const size_t sm = cheb_forward_tiled_smem<T>(N, C.bk);
     set_smem(cheb_forward_tiled_kernel<P, T>, sm);
-    const int64_t nblk = (C.jDim + 63) / 64;
+    const int64_t nblk = (C.col1 - C.col0 + 63) / 64;
+    if (nblk <= 0) return cudaSuccess;
     const int64_t want = std::max<int64_t>(1, (int64_t)resident_ctas(sm, 128) / std::max(C.nvars, 1));
     dim3 grid((unsigned)std::min(nblk, want), C.nvars);
     cheb_forward_tiled_kernel<P, T><<<grid, 128, sm, st>>>(C);
@@ -724,7 +725,8 @@ cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t s
     (void)smem;
     const size_t sm = cheb_inverse_m_smem<T>(N, C.bk);
     set_smem(cheb_inverse_m_kernel<P, T>, sm);
-    dim3 grid((unsigned)((C.jDim + 63) / 64), C.nvars, 5);
+    if (C.col1 <= C.col0) return cudaSuccess;
+    dim3 grid((unsigned)((C.col1 - C.col0 + 63) / 64), C.nvars, 5);
     cheb_inverse_m_kernel<P, T><<<grid, 128, sm, st>>>(C);
     return cudaGetLastError();
 }

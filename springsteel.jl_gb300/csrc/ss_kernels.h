@@ -71,6 +71,7 @@ struct ChebLaunch {
     const ChebDev *cheb;       // per variable
     const RingDesc *rings;     // ring start table (jofs) for column → ring lookup
     int64_t jDim, np;
+    int64_t col0, col1;        // columns (ring points) [col0, col1) of this launch
     int iDim, bk, nvars;
 };
 

@@ -473,6 +473,39 @@ spectralTransform = spectralTransform_b
 gridTransform = gridTransform_b
 
 
+def spectralTransform_from_host(grid, physical, stream=None):
+    """spectralTransform!(grid) reading physical slot 1 from a host array: an
+    (n × nvars) array, or the whole (n × nvars × nslots) physical array of the
+    reference's layout (column-major).  The upload of each radial chunk overlaps
+    the transform of the previous one; returns once the array may be reused."""
+    n, nv, ns = grid.physical_shape
+    a = np.asarray(physical)
+    if a.ndim == 3:
+        a = a[:, :, 0]
+    a = np.asfortranarray(a)
+    if a.dtype not in _DTYPES:
+        a = a.astype(np.float64, order="F")
+    if a.shape != (n, nv):
+        raise ValueError("physical slot 1 shape %s, expected %s" % (a.shape, (n, nv)))
+    _check(load_library().ss_spectral_transform_from_host(grid.handle, a.ctypes.data_as(C.c_void_p),
+                                                          _DTYPES[a.dtype], stream))
+    return grid
+
+
+def gridTransform_to_host(grid, out=None, dtype=np.float64, stream=None):
+    """gridTransform!(grid) into a host array (n × nvars × nslots, column-major):
+    the download of each radial chunk overlaps the transform of the next.
+    Returns `out` (allocated when None)."""
+    n, nv, ns = grid.physical_shape
+    if out is None:
+        out = np.empty((n, nv, ns), dtype=dtype, order="F")
+    if out.shape != (n, nv, ns) or not out.flags.f_contiguous or out.dtype not in _DTYPES:
+        raise ValueError("output must be a column-major %s float32/float64 array" % ((n, nv, ns),))
+    _check(load_library().ss_grid_transform_to_host(grid.handle, out.ctypes.data_as(C.c_void_p),
+                                                    _DTYPES[out.dtype], stream))
+    return out
+
+
 def getGridpoints(grid):
     """getGridpoints (src/transforms_cylindrical.jl:75-90, 454-476)."""
     gp = grid.params

@@ -148,7 +148,8 @@ EXPORTED = [
     "ss_version", "ss_last_error_string", "ss_grid_create", "ss_grid_destroy", "ss_grid_dims",
     "ss_grid_stream", "ss_grid_device_physical", "ss_grid_device_spectral",
     "ss_upload_physical", "ss_download_physical", "ss_upload_spectral", "ss_download_spectral",
-    "ss_spectral_transform", "ss_grid_transform", "ss_grid_set_filter", "ss_grid_set_ahat",
+    "ss_spectral_transform", "ss_grid_transform", "ss_spectral_transform_from_host",
+    "ss_grid_transform_to_host", "ss_grid_set_filter", "ss_grid_set_ahat",
     "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
     "ss_spectral_transform_noalloc",
     "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads",
@@ -201,6 +202,8 @@ def bind(lib):
         "ss_download_spectral": ([vp, vp, i32, vp], i32),
         "ss_spectral_transform": ([vp, vp], i32),
         "ss_grid_transform": ([vp, vp], i32),
+        "ss_spectral_transform_from_host": ([vp, vp, i32, vp], i32),
+        "ss_grid_transform_to_host": ([vp, vp, i32, vp], i32),
         "ss_grid_set_filter": ([vp, i32, vp, vp], i32),
         "ss_grid_set_ahat": ([vp, i32, i32, vp], i32),
         "ss_grid_clear_ahat": ([vp], i32),
