@@ -529,6 +529,16 @@ def run_ours(args):
     e2e_val, (ph_in, ph_out) = e2e_loop(True)
     seq_val, (sq_up, sq_rest) = e2e_loop(False)
     e2e_phase_ms = {"spectral_from_host": ph_in, "grid_to_host": ph_out}
+    # stage events of one overlapped round trip (chunked launches)
+    chk(lib.ss_grid_profile(grid.handle, 1))
+    chk(lib.ss_spectral_transform_from_host(grid.handle, C.c_void_p(h_in.data_ptr()), dt_code, None))
+    chk(lib.ss_grid_transform_to_host(grid.handle, C.c_void_p(h_out.data_ptr()), dt_code, None))
+    grid.synchronize()
+    ov_ms, ov_n = (C.c_double * 6)(), (C.c_int64 * 6)()
+    chk(lib.ss_grid_profile_read(grid.handle, ov_ms, ov_n))
+    chk(lib.ss_grid_profile(grid.handle, 0))
+    e2e_phase_ms["stage_ms"] = {abi.STAGES[i]: round(ov_ms[i], 2) for i in range(6)}
+    e2e_phase_ms["launches"] = [int(ov_n[i]) for i in range(6)]
     e2e_sequential = {"value": seq_val, "upload_ms": sq_up, "transforms_and_download_ms": sq_rest}
 
     # ---- roofline of the dominant stage
