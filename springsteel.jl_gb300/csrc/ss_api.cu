@@ -194,12 +194,12 @@ static int32_t build_grid(ss_grid *g) {
     // ---- rings (src/factory.jl:608-624) and FFT plans
     TwiddlePool pool;
     PlanSet plans;
-    // binary32 butterflies are issue-bound and keep Bluestein above 127 (measured
-    // faster than Rader there at limits 41-127); the FP64 pipe favours direct
-    // prime passes up to 67 and Rader above (measured on the 200-cell RLZ grid:
-    // ring_inverse 46.9 ms at 67, 47.1 at 101, 49.2 at 199, 48.0 at 41)
-    plans.max_prime = (g->tl == TL_F32) ? 127 : 67;
-    plans.rader = g->tl != TL_F32;
+    // direct prime passes up to 67 and one Rader pass above, in every precision
+    // (measured: 200-cell FP64 RLZ ring_inverse 43.4 ms at 67, 44.4 at 41; 400-cell
+    // FP32 ring_inverse 84.1 ms with Rader above 67, 86.2 above 127, 91.9 with
+    // Bluestein above 127)
+    plans.max_prime = 67;
+    plans.rader = true;
     // tuning override of the direct-pass limit (odd, 13 ≤ limit ≤ 199)
     if (const char *e = std::getenv("SS_FFT_MAX_PRIME")) {
         const int v = std::atoi(e);

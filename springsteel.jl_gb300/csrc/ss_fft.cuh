@@ -127,18 +127,20 @@ __device__ __forceinline__ const void *tab_at(const void *pool, int64_t off) {
 // Radix-R pass for an odd prime R > 13 (up to kMaxPrimeRadix).  A first
 // sweep twiddles each butterfly's inputs (skipped when Ns = 1) and replaces
 // them in place by the pairs a_q = v_q + v_{R−q} (at q) and b_q = v_q − v_{R−q}
-// (at R−q), q = 1..(R−1)/2; then each work item computes one conjugate output
-// pair (s, R−s) of one butterfly:
+// (at R−q), q = 1..(R−1)/2; then each work item computes kPrimeGroup conjugate
+// output pairs (s, R−s) of one butterfly:
 //   re = v_0 + Σ_q a_q cos(2πqs/R),  im = Σ_q b_q sin(2πqs/R),
 //   X_s = re ∓ i·im, X_{R−s} = re ± i·im  (upper signs forward), X_0 = v_0 + Σ a_q.
 // cos/sin(2πe/R) are the N-point twiddles at e·N/R.  Four FMAs per term and
-// output pair instead of a length ≥ 2N−1 chirp-z convolution.
+// output pair instead of a length ≥ 2N−1 chirp-z convolution; each a_q, b_q
+// load from shared memory serves all of the item's pairs.
+template <typename T> constexpr int kPrimeGroup = sizeof(T) == 4 ? 2 : 4;  // output pairs per work item of a prime pass
 template <int SIGN, typename T>
 __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N, int Ns, int R,
                            const void *__restrict__ tw, int nb, int bs) {
     const int NR = N / R, H = (R - 1) / 2;
     const int tstride = N / (Ns * R), rstep = N / R;
-    const float inv_ns = 1.0f / (float)Ns, inv_h = 1.0f / (float)H, inv_h1 = 1.0f / (float)(H + 1);
+    const float inv_ns = 1.0f / (float)Ns, inv_h = 1.0f / (float)H;
     {
         const int per = NR * H;
         for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
@@ -161,52 +163,57 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
         }
         __syncthreads();
     }
-    const int per = NR * (H + 1);
+    // each work item: S consecutive output pairs s = s0 .. s0+S−1 of one
+    // butterfly, so every a_q, b_q load feeds S pairs (s = 0 gives X_0 = v_0 + Σ a_q
+    // through the unit twiddle; entries with s > H are computed and dropped).
+    // S = 2 for binary32, whose ring kernels run at 64 registers per thread.
+    constexpr int S = kPrimeGroup<T>;
+    const int G = (H + 1 + S - 1) / S;
+    const int per = NR * G;
+    const float inv_g = 1.0f / (float)G;
     for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
         const int bi = nb == 1 ? 0 : t / per, rest = t - bi * per;
-        const int j = div_small(rest, H + 1, inv_h1), s = rest - j * (H + 1);
+        const int j = div_small(rest, G, inv_g), s0 = (rest - j * G) * S;
         const cpx<T> *sv = src + (size_t)bi * bs + j;
         cpx<T> *d = dst + (size_t)bi * bs;
         const int jq = div_small(j, Ns, inv_ns), k = j - jq * Ns;
         const int idxD = jq * Ns * R + k;
         const cpx<T> x0 = sv[0];
-        if (s == 0) {
-            cpx<T> acc = x0;
-            for (int q = 1; q <= H; q++) acc = c_add(acc, sv[q * NR]);
-            d[idxD] = acc;
-            continue;
-        }
-        cpx<T> re = x0, im = c_zero<T>();
-        int e = 0;
+        cpx<T> re[S], im[S];
+        int e[S];
+#pragma unroll
+        for (int i = 0; i < S; i++) { re[i] = x0; im[i] = c_zero<T>(); e[i] = 0; }
         for (int q = 1; q <= H; q++) {
-            e += s;
-            if (e >= R) e -= R;
-            const cpx<T> w = ld_cplx<T>(tw, (int64_t)e * rstep);  // (cos, −sin)(2πe/R)
             const cpx<T> a = sv[q * NR], b = sv[(R - q) * NR];
-            re.x = re.x + a.x * w.x;
-            re.y = re.y + a.y * w.x;
-            im.x = im.x - b.x * w.y;
-            im.y = im.y - b.y * w.y;
+#pragma unroll
+            for (int i = 0; i < S; i++) {
+                e[i] += s0 + i;  // e = q·s mod R (s ≤ R − 1 keeps one subtraction enough)
+                if (e[i] >= R) e[i] -= R;
+                const cpx<T> w = ld_cplx<T>(tw, (int64_t)e[i] * rstep);  // (cos, −sin)(2πe/R)
+                re[i].x = re[i].x + a.x * w.x;
+                re[i].y = re[i].y + a.y * w.x;
+                im[i].x = im[i].x - b.x * w.y;
+                im[i].y = im[i].y - b.y * w.y;
+            }
         }
-        const cpx<T> iim = {-im.y, im.x};
-        if (SIGN < 0) {
-            d[idxD + s * Ns] = c_sub(re, iim);
-            d[idxD + (R - s) * Ns] = c_add(re, iim);
-        } else {
-            d[idxD + s * Ns] = c_add(re, iim);
-            d[idxD + (R - s) * Ns] = c_sub(re, iim);
+#pragma unroll
+        for (int i = 0; i < S; i++) {
+            const int s = s0 + i;
+            if (s > H) break;
+            if (s == 0) {
+                d[idxD] = re[i];
+                continue;
+            }
+            const cpx<T> iim = {-im[i].y, im[i].x};
+            if (SIGN < 0) {
+                d[idxD + s * Ns] = c_sub(re[i], iim);
+                d[idxD + (R - s) * Ns] = c_add(re[i], iim);
+            } else {
+                d[idxD + s * Ns] = c_add(re[i], iim);
+                d[idxD + (R - s) * Ns] = c_sub(re[i], iim);
+            }
         }
     }
-}
-
-__device__ __forceinline__ int mod_pow_i(int b, int e, int m) {
-    int r = 1;
-    while (e > 0) {
-        if (e & 1) r = r * b % m;
-        b = b * b % m;
-        e >>= 1;
-    }
-    return r;
 }
 
 // Stockham passes rad[s_begin..nrad) over ping-pong buffers, Ns0 = product of the
@@ -246,13 +253,14 @@ __device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, i
 // holding the pass's outputs (either a or b).
 template <int SIGN, typename T>
 __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl, const void *pool, int nb, int bs) {
-    const int p = pl.rp, P1 = p - 1, NR = N / p, g = pl.rg;
+    const int p = pl.rp, P1 = p - 1, NR = N / p;
     const float inv_p = 1.0f / (float)p, inv_p1 = 1.0f / (float)P1;
     const void *H = tab_at<T>(pool, pl.rH);
+    const void *perm = tab_at<T>(pool, pl.rperm);  // (g^a, g^{−a}) mod p
     for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {  // gather: (j, a), a = p−1 → x_0
         const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
         const int j = div_small(e, p, inv_p), a = e - j * p;
-        const int q = a < P1 ? mod_pow_i(g, a, p) : 0;
+        const int q = a < P1 ? ld_index_pair<T>(perm, a).x : 0;
         cpx<T> v = src[(size_t)bi * bs + j + q * NR];
         if (SIGN > 0) v.y = -v.y;
         dst[(size_t)bi * bs + (a < P1 ? j * P1 + a : N + j)] = v;
@@ -274,7 +282,6 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
         r2 = (rr == d0) ? dst : src;  // same choice for every item
     }
     cpx<T> *out = (r2 == dst) ? src : dst;
-    const int ginv = mod_pow_i(g, p - 2, p);
     for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {  // scatter: (j, b), b = p−1 → X_0
         const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
         const int j = div_small(e, p, inv_p), b = e - j * p;
@@ -286,7 +293,7 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
             s = 0;
         } else {
             X = c_add(dst[(size_t)bi * bs + N + j], rb[j * P1 + b]);
-            s = mod_pow_i(ginv, b, p);
+            s = ld_index_pair<T>(perm, b).y;
         }
         if (SIGN > 0) X.y = -X.y;
         out[(size_t)bi * bs + j * p + s] = X;  // Ns = 1: butterfly j's outputs at j·p + s

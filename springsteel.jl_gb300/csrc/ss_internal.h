@@ -57,6 +57,7 @@ struct FftPlan {
     int rrad[kMaxRadices];
     int64_t rtw;     // pool offset of W_{p−1}^t, t < p−1
     int64_t rH;      // pool offset of H, p−1 entries
+    int64_t rperm;   // pool offset of (g^a mod p, g^{−a} mod p), a < p−1, as exact reals
 };
 
 // One Fourier ring (src/factory.jl:608-624): L = 4+4ri points, kmax, bDim = 2ri+1.

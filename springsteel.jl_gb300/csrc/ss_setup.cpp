@@ -507,6 +507,16 @@ static bool rader_plan(int N, int max_prime, FftPlan &p, TwiddlePool &pool) {
         H[2 * k + 1] = acc.imag() / P1;
     }
     p.rH = pool.push(H);
+    // index permutations of the gather (g^a) and the scatter (g^{−b})
+    std::vector<double> perm(2 * (size_t)P1);
+    long ga = 1, gb = 1;
+    for (int a = 0; a < P1; a++) {
+        perm[2 * a] = (double)ga;
+        perm[2 * a + 1] = (double)gb;
+        ga = ga * p.rg % P;
+        gb = gb * ginv % P;
+    }
+    p.rperm = pool.push(perm);
     return true;
 }
 

@@ -76,6 +76,22 @@ __device__ __forceinline__ cpx<df64> ld_cplx<df64>(const void *tab, int64_t i) {
     return {df64(v.x, v.y), df64(v.z, v.w)};
 }
 
+// a pair of small non-negative integers stored as the (re, im) reals of a
+// complex table entry (exact in every layout below 2^24)
+template <typename T>
+__device__ __forceinline__ int2 ld_index_pair(const void *tab, int64_t i) {
+    if constexpr (std::is_same<T, double>::value) {
+        const double2 v = __ldg((const double2 *)tab + i);
+        return make_int2((int)v.x, (int)v.y);
+    } else if constexpr (std::is_same<T, float>::value) {
+        const float2 v = __ldg((const float2 *)tab + i);
+        return make_int2((int)v.x, (int)v.y);
+    } else {
+        const float4 v = __ldg((const float4 *)tab + i);
+        return make_int2((int)v.x, (int)v.z);
+    }
+}
+
 // storage → compute and back
 template <typename T, typename P>
 __device__ __forceinline__ T to_compute(P v) {
