@@ -553,6 +553,7 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
     T *xe = reinterpret_cast<T *>(smem_raw);  // Ke × COLS: even inputs b_{2i'}, then s = Uᵀ b
     T *xo = xe + (size_t)Ke * COLS;            // Ko × COLS: odd inputs b_{2i'+1}, then s
     T *us = xo + (size_t)Ko * COLS;            // COLS × ldn outputs
+    T *ms = us + (size_t)COLS * ldn;           // 2 × kcap × JP: M_d of both output halves
     const int64_t c0 = C.col0 + (int64_t)blockIdx.x * COLS;
     const int ncol = (int)((C.col1 - c0) < COLS ? (C.col1 - c0) : COLS);
     for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
@@ -584,9 +585,20 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
         }
     __syncthreads();
     const int nd = (var == 0) ? 3 : 1;
+    const T *mtab = (const T *)cb.inv_m_t;
     for (int dd = 0; dd < nd; dd++) {
+        // M_d of both halves into shared memory (16-byte copies: JP and kcap·JP are
+        // multiples of 4 entries, so every row start is 16-byte aligned)
+        {
+            const int nm = 2 * cb.kcap * JP, per16 = 16 / (int)sizeof(T);
+            const T *src = mtab + (int64_t)(dd * 2) * cb.kcap * JP;
+            if (dd > 0) __syncthreads();  // the previous derivative's tiles have read ms
+            for (int e = threadIdx.x * per16; e < nm; e += blockDim.x * per16) cp_async<16>(ms + e, src + e);
+            cp_async_wait_all();
+            __syncthreads();
+        }
         // output half pe reads the inputs of parity (pe + dd) mod 2
-        const int64_t me = (int64_t)(dd * 2) * cb.kcap * JP, mo = me + (int64_t)cb.kcap * JP;
+        const int64_t me = 0, mo = (int64_t)cb.kcap * JP;
         const T *ie = (dd & 1) ? xo : xe, *io = (dd & 1) ? xe : xo;
         const int Kie = (dd & 1) ? Ko : Ke, Kio = (dd & 1) ? Ke : Ko;
         for (int t = threadIdx.x; t < JT * CT; t += blockDim.x) {
@@ -600,7 +612,7 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
             for (int k = 0; k < Kie; k++) {
                 T w[TJ], b[TC];
 #pragma unroll
-                for (int i = 0; i < TJ; i++) w[i] = ld_real<T>(cb.inv_m_t, me + (int64_t)k * JP + j0 + i);
+                load_row<T, TJ>(ms + me + (size_t)k * JP + j0, w);
                 load_row<T, TC>(ie + (size_t)k * COLS + cc, b);
 #pragma unroll
                 for (int i = 0; i < TJ; i++)
@@ -610,7 +622,7 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
             for (int k = 0; k < Kio; k++) {
                 T w[TJ], b[TC];
 #pragma unroll
-                for (int i = 0; i < TJ; i++) w[i] = ld_real<T>(cb.inv_m_t, mo + (int64_t)k * JP + j0 + i);
+                load_row<T, TJ>(ms + mo + (size_t)k * JP + j0, w);
                 load_row<T, TC>(io + (size_t)k * COLS + cc, b);
 #pragma unroll
                 for (int i = 0; i < TJ; i++)
@@ -634,14 +646,19 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
         if (var == 0) slot = (dd == 0) ? 1 : (dd == 1 ? 6 : 7);
         else slot = (var == 1) ? 4 : (var == 2 ? 5 : (var == 3 ? 2 : 3));
         P *dst = (P *)C.out + ((size_t)(slot - 1) * C.nvars + v) * C.np + c0 * N;
-        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) dst[e] = to_storage<P>(us[(e / N) * ldn + (e % N)]);
+        const float inv_n = 1.0f / (float)N;
+        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) {
+            const int col = div_small(e, N, inv_n);
+            dst[e] = to_storage<P>(us[col * ldn + (e - col * N)]);
+        }
         __syncthreads();
     }
 }
 
 template <typename T>
 size_t cheb_inverse_m_smem(int N, int bk) {  // rank of the Γ fold ≤ 2: two s rows per input set
-    return ((size_t)(bk + 4) * 64 + (size_t)64 * (N | 1)) * sizeof(T);
+    const size_t kcap = (size_t)(bk + 1) / 2 + 2, jp = (size_t)cheb_pad4((N + 1) / 2);
+    return ((size_t)(bk + 4) * 64 + (size_t)64 * (N | 1) + 2 * kcap * jp) * sizeof(T);
 }
 
 // ====================================================================
