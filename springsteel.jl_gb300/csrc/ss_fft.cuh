@@ -3,12 +3,13 @@
 // The ring transforms of the reference call FFTW's R2HC/HC2R on rings of
 // L = 4+4ri points (src/Fourier.jl:192-193, 388-395, 463-468).  Ring lengths
 // have arbitrary prime factors, so a length-N complex DFT (N = L/2 after real
-// packing) is evaluated either by mixed-radix Stockham autosort passes
-// (radices 4,2,3,5,7,11,13 in registers, odd primes up to kMaxPrimeRadix as
-// output-pair passes) or, when N has a larger prime factor, by Bluestein's
-// chirp-z convolution of smooth length M >= 2N-1 whose two FFTs are again
-// Stockham passes.  Twiddles come from FP64-accurate tables built on
-// the host (ss_setup.cpp), stored in the compute type's layout.
+// packing) is evaluated by mixed-radix Stockham autosort passes (radices
+// 4,2,3,5,7,11,13 in registers, odd primes up to the plan set's limit as
+// output-pair passes); a larger prime factor p gets one Rader pass (a
+// (p−1)-point cyclic convolution by two inner Stockham DFTs), and lengths with
+// no such plan fall back to Bluestein's chirp-z convolution of smooth length
+// M >= 2N-1.  Twiddles and index tables come from FP64-accurate tables built
+// on the host (ss_setup.cpp), stored in the compute type's layout.
 //
 // Every routine transforms a batch of `nb` independent sequences of the same
 // plan, `bs` complex entries apart in shared memory: one barrier per pass
