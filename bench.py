@@ -282,6 +282,31 @@ def _bytes_per_roundtrip(dims, w):
     return w * dims["nvars"] * (dims["n_physical"] * (1 + dims["nslots"]) + 2 * dims["n_spectral"])
 
 
+def _ring_fft_flops(dims):
+    """Conventional flops of one real DFT per ring, z-mode and variable."""
+    pol = dims["kDim_wn"] - dims["iDim"]  # patchOffsetL
+    per = sum(2.5 * L * np.log2(L) for L in (4 + 4 * (r + pol) for r in range(1, dims["iDim"] + 1)))
+    return per * dims["b_kDim"] * dims["nvars"]
+
+
+def _matmul_tflops(dtype, n=4096):
+    """Dense matmul rate of `dtype` on the current GPU (best of 3, CUDA events)."""
+    import torch
+
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    torch.matmul(a, a)
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, a)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        best = t if best is None else min(best, t)
+    return 2.0 * n ** 3 / best / 1e12
+
+
 def _stage_bytes(dims, w):
     """Compulsory bytes of each stage for one round trip (all variables)."""
     nv, bk, jD, fr = dims["nvars"], dims["b_kDim"], dims["jDim"], dims["b_jDim"]
@@ -556,6 +581,20 @@ def run_ours(args):
             "stage_ms_per_step": per_step_ms,
             "path_achieved_gbs": path_gbs, "path_frac": path_gbs / peak}
     gpu_launches = int(sum(launches[i] for i in range(6)))
+    # the ring stages are bound by the arithmetic pipe of the compute type, not by
+    # HBM: their conventional FFT flops (2.5·L·log2 L per real length-L transform;
+    # 5 inverse and 1 forward transform per ring, z-mode and variable) over the live
+    # stage time, against a dense matmul of the same type timed here
+    pipe_peak = _matmul_tflops(torch.float64 if w == 8 else torch.float32)
+    ring_flops = _ring_fft_flops(dims)
+    roof["pipe"] = {
+        "unit": "TFLOP/s", "peak": pipe_peak,
+        "peak_source": "torch.matmul %s 4096^3 on this GPU, best of 3" % ("float64" if w == 8 else "float32"),
+        "flop_model": "2.5*L*log2(L) per real ring transform (FFT convention)",
+    }
+    for st, nt in (("ring_inverse", 5), ("ring_forward", 1)):
+        t = per_step_ms[st] * 1e-3
+        roof["pipe"][st] = {"achieved": nt * ring_flops / t / 1e12, "frac": nt * ring_flops / t / 1e12 / pipe_peak}
 
     line = {
         "metric": "RLZ transforms/s", "value": value, "unit": "round trips/s", "n_gpus": ws,
