@@ -60,7 +60,7 @@ WORKLOADS = {
 
 
 def run_batch(args):
-    """Config 3's batched workload: one step = spectralTransform! + gridTransform! of
+    """Batched workload of 64 uneven RL grids: one step = spectralTransform! + gridTransform! of
     every grid of the batch (all variables, all 5 slots), replayed as one CUDA graph
     with autotuned ring-kernel CTA sizes.  Also reported: the same grids as
     individual calls (no graph), and e2e with every grid's slot 1 uploaded and all
@@ -176,7 +176,7 @@ def run_elliptic(args):
     torch.cuda.set_device(local)
     w = WORKLOADS["elliptic-rl200"]
     n_eval = min(w["eval_seeds"], max(args.steps, 1) * 100) if args.steps < 10 else w["eval_seeds"]
-    gp = fields.config5_params(num_cells=w["num_cells"], rmax=w["rmax"])
+    gp = fields.elliptic_rl200_params(num_cells=w["num_cells"], rmax=w["rmax"])
     grid = S.createGrid(gp)
     k2 = fields.k2_profile(fields.radial_mish(gp), seed=w["k2_seed"], rmax=w["rmax"])
     prob = S.SpringsteelProblem(grid, k2, tol=w["tol"], restart=w["restart"], maxiter=20000)
@@ -255,9 +255,9 @@ def _params(wl):
 
     w = WORKLOADS[wl]
     if w["precision"] != "f32":
-        return fields.config2_params(precision=w["precision"], num_cells=w["num_cells"], kDim=w["kDim"],
+        return fields.rlz_params(precision=w["precision"], num_cells=w["num_cells"], kDim=w["kDim"],
                                      nvars=w["nvars"])
-    return fields.config4_params(precision="f32", num_cells=w["num_cells"], kDim=w["kDim"], nvars=w["nvars"])
+    return fields.rlz400_f32_params(precision="f32", num_cells=w["num_cells"], kDim=w["kDim"], nvars=w["nvars"])
 
 
 def _config(wl, dims):
@@ -402,7 +402,7 @@ def _oracle_sample(wl, threads, seconds_hint=None):
 
     w = dict(WORKLOADS[wl])
     gp = _params(wl)
-    gp1 = fields.config2_params(num_cells=w["num_cells"], kDim=w["kDim"], nvars=1)
+    gp1 = fields.rlz_params(num_cells=w["num_cells"], kDim=w["kDim"], nvars=1)
     o = O.OracleGrid(gp1.to_abi())
     O.set_threads(threads)
     pts = o.gridpoints()

@@ -976,7 +976,7 @@ int32_t ss_grid_synchronize(ss_grid *g) {
 // the fixed array below instead of the grid's scratch buffer.
 //
 // Limit: kStaticScratchDoubles = 1,048,576 FP64 values (8 MiB), i.e.
-// nvars × Σ_r (1 + 2 ri) ≤ 1,048,576 (config 1 needs 90,600).  Every GPU that
+// nvars × Σ_r (1 + 2 ri) ≤ 1,048,576 (the 100-cell one-variable RL grid needs 90,600).  Every GPU that
 // loads the library keeps this 8 MiB reserved until the process exits.
 // Every call shares the array and it keeps the last call's contents; the
 // kernels write every entry they later read within one call, so nothing has

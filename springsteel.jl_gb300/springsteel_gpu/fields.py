@@ -47,7 +47,7 @@ def blob_sum(points, seed, nblobs=8, rmax=None, zmin=0.0, zmax=1.0, wmin=5.0, wm
 
 
 # ---------------------------------------------------------------- benchmark shapes
-def config1_params(precision="f64"):
+def rl100_params(precision="f64"):
     """RL, radius 0-100, 100 cells × 3 Gauss points, rings of 4+4r, one variable.
     NaturalBC at both ends (the reference has no RL axis-regularity BC)."""
     return SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=100.0, num_cells=100,
@@ -55,7 +55,7 @@ def config1_params(precision="f64"):
                                      vars={"u": 1}, precision=precision)
 
 
-def config2_params(precision="f64", num_cells=200, kDim=32, nvars=5):
+def rlz_params(precision="f64", num_cells=200, kDim=32, nvars=5):
     """RLZ, 200 cells on r ∈ [0, 200] (DX = 1), 32 Chebyshev levels on z ∈ [0, 20000],
     5 variables, Dirichlet in z (Chebyshev R1T0 both ends)."""
     vars_ = {"v%d" % i: i for i in range(1, nvars + 1)}
@@ -65,7 +65,7 @@ def config2_params(precision="f64", num_cells=200, kDim=32, nvars=5):
                                      precision=precision)
 
 
-def config4_params(precision="f32", num_cells=400, kDim=64, nvars=8):
+def rlz400_f32_params(precision="f32", num_cells=400, kDim=64, nvars=8):
     """RLZ, 400 cells (r ∈ [0, 400]), 64 Chebyshev levels on z ∈ [0, 20000], 8 variables."""
     vars_ = {"v%d" % i: i for i in range(1, nvars + 1)}
     return SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=float(num_cells), num_cells=num_cells,
@@ -83,7 +83,7 @@ def rlz_blob_fields(points, nvars, base_seed=2, zmax=20000.0, noise=0.0):
 
 
 # ----------------------------------------------------------------- elliptic solve
-def config5_params(num_cells=200, rmax=100.0):
+def elliptic_rl200_params(num_cells=200, rmax=100.0):
     """RL, 200 cells on r ∈ [0, 100], rings of 4+4r, one variable, native FP64."""
     return SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=float(rmax), num_cells=num_cells,
                                      BCL={"default": NaturalBC()}, BCR={"default": NaturalBC()},

@@ -21,7 +21,7 @@ def _fill(g, seed):
     return u
 
 
-def test_config3_chain_parity():
+def test_rl_chain_40_120_40_parity():
     ps = S.chain_grid_params([0.0, 40.0, 100.0, 140.0], [40, 120, 40], vars={"u": 1, "w": 2})
     gs = [S.createGrid(p) for p in ps]
     os_ = [O.OracleGrid(p.to_abi()) for p in ps]
@@ -99,7 +99,7 @@ def _sum_spectral_tile(patch_spec, tile_spec, pp, tp):
 
 
 def test_rlz_tiles_halo_sum_matches_oracle():
-    gp = fields.config2_params(num_cells=40, nvars=2)
+    gp = fields.rlz_params(num_cells=40, nvars=2)
     patch = S.createGrid(gp)
     u = _fill(patch, seed=9)
     S.spectralTransform_b(patch)

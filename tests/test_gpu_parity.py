@@ -6,7 +6,7 @@ floored by the field's natural scale for a derivative of order d along a
 domain of length L (r: iMax - iMin, λ: 1, z: kMax - kMin).  The floor only
 matters for derivative slots that vanish analytically (e.g. ∂rr of a field
 linear in r), where both sides are pure round-off.
-FP64 path tolerance: 1e-12 (spec bound).  FP32+refinement: below.
+FP64 path tolerance: 1e-12 (the stated FP64 parity bound).  FP32+refinement: below.
 """
 import numpy as np
 import pytest
@@ -87,8 +87,8 @@ def _assert_parity(spec_g, spec_o, phys_g, phys_o, gp, tol=TOL64):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f64_fast"])
-def test_rl_config1_parity(precision):
-    gp = fields.config1_params(precision=precision)
+def test_rl100_one_var_parity(precision):
+    gp = fields.rl100_params(precision=precision)
     pts = S.getGridpoints(S.createGrid(gp))
     u = fields.gaussian_ring_field(pts, seed=1)
     _, _, sg, so, pg, po = _run_both(gp, u[:, None])
@@ -96,7 +96,7 @@ def test_rl_config1_parity(precision):
 
 
 def test_rl_gridpoints_match_oracle():
-    gp = fields.config1_params()
+    gp = fields.rl100_params()
     g = S.createGrid(gp)
     o = O.OracleGrid(gp.to_abi())
     assert np.max(np.abs(S.getGridpoints(g) - o.gridpoints())) < 1e-13
@@ -157,9 +157,9 @@ def test_rlz_parity_bcs(bcb, bct):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f64_fast"])
-def test_rlz_config2_shape_reduced(precision):
+def test_rlz_5var_kz32_reduced(precision):
     # the configuration-2 layout (kz = 32, 5 variables, Dirichlet in z) at 40 cells
-    gp = fields.config2_params(num_cells=40, precision=precision)
+    gp = fields.rlz_params(num_cells=40, precision=precision)
     pts = S.getGridpoints(S.createGrid(gp))
     u = fields.rlz_blob_fields(pts, 5, zmax=20000.0)
     _, _, sg, so, pg, po = _run_both(gp, u)
@@ -206,7 +206,7 @@ def test_fp32_refined_error_vs_fp64_oracle():
 @pytest.mark.parametrize("precision", ["f64", "f64_fast"])
 def test_rlz_kz64_parity(precision):
     # the configuration-4 column length (64 levels) in FP64 arithmetic
-    gp = fields.config4_params(precision=precision, num_cells=12, kDim=64, nvars=2)
+    gp = fields.rlz400_f32_params(precision=precision, num_cells=12, kDim=64, nvars=2)
     pts = S.getGridpoints(S.createGrid(gp))
     u = fields.rlz_blob_fields(pts, 2, zmax=20000.0)
     _, _, sg, so, pg, po = _run_both(gp, u)
@@ -214,7 +214,7 @@ def test_rlz_kz64_parity(precision):
 
 
 def test_fp32_kz64_error_vs_fp64_oracle():
-    gp = fields.config4_params(precision="f32", num_cells=24, kDim=64, nvars=2)
+    gp = fields.rlz400_f32_params(precision="f32", num_cells=24, kDim=64, nvars=2)
     pts = S.getGridpoints(S.createGrid(gp))
     u = fields.rlz_blob_fields(pts, 2, zmax=20000.0)
     _, o, sg, so, pg, po = _run_both(gp, u)

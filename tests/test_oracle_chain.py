@@ -61,7 +61,7 @@ def test_chain_rejects_unsupported_ratio():
 
 @pytest.mark.parametrize("ntiles", [1, 2, 5, 8])
 def test_calc_tile_sizes_cover_patch(ntiles):
-    gp = fields.config2_params()
+    gp = fields.rlz_params()
     tiles = S.calcTileSizes(gp, ntiles)
     assert sum(t.num_cells for t in tiles) == gp.num_cells
     assert all(t.num_cells >= 3 for t in tiles)

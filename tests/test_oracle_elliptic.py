@@ -121,7 +121,7 @@ def test_oracle_tile_b_vectors_sum_to_patch():
     (sumSpectralTile!, src/tiling.jl:1101-1136) reproduces the patch exactly."""
     from test_gpu_multi import _sum_spectral_tile
 
-    gp = fields.config2_params(num_cells=24, nvars=1, kDim=8)
+    gp = fields.rlz_params(num_cells=24, nvars=1, kDim=8)
     op = O.OracleGrid(gp.to_abi())
     pts = S.getGridpoints(_HostGrid(gp))
     u = fields.blob_sum(pts, seed=3, nblobs=6, wmin=3.0, wmax=12.0, zmax=20000.0)
