@@ -312,6 +312,12 @@ static int32_t build_grid(ss_grid *g) {
                 g->chunk_seg[c].push_back({off, (int)clist.size() - off});
             }
         if ((st = upload_vec(g, &g->d_ring_list_chunks, clist))) return st;
+        if (g->rlz) {  // column → ring for the Chebyshev stages (one load instead of a search)
+            std::vector<int> cr(g->ring_jofs[iDim]);
+            for (int r = 0; r < iDim; r++)
+                for (int64_t q = g->ring_jofs[r]; q < g->ring_jofs[r + 1]; q++) cr[q] = r;
+            if ((st = upload_vec(g, &g->d_col_ring, cr))) return st;
+        }
     }
 
     // ---- Chebyshev columns (src/factory.jl:722-728)
@@ -452,7 +458,7 @@ template <typename P, typename T>
 static int32_t fwd_columns(ss_grid *g, cudaStream_t st, int chunk) {
     const ss_dims &d = g->d;
     ChebLaunch Cl{};
-    Cl.in = g->phys; Cl.out = g->C; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
+    Cl.in = g->phys; Cl.out = g->C; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings; Cl.col_ring = g->d_col_ring;
     Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = (int)d.b_kDim; Cl.nvars = (int)d.nvars;
     Cl.col0 = chunk_col(g, chunk, 0); Cl.col1 = chunk_col(g, chunk, 1);
     const int N = (int)d.kDim, half = (N + 1) / 2;
@@ -551,7 +557,7 @@ template <typename P, typename T>
 static int32_t inv_columns(ss_grid *g, cudaStream_t st, int chunk) {
     const ss_dims &d = g->d;
     ChebLaunch Cl{};
-    Cl.in = g->H; Cl.out = g->phys; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings;
+    Cl.in = g->H; Cl.out = g->phys; Cl.cheb = g->d_cheb; Cl.rings = g->d_rings; Cl.col_ring = g->d_col_ring;
     Cl.jDim = d.jDim; Cl.np = d.n_physical; Cl.iDim = (int)d.iDim; Cl.bk = (int)d.b_kDim; Cl.nvars = (int)d.nvars;
     Cl.col0 = chunk_col(g, chunk, 0); Cl.col1 = chunk_col(g, chunk, 1);
     const int N = (int)d.kDim;

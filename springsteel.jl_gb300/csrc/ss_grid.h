@@ -59,6 +59,7 @@ struct ss_grid {
     std::vector<int> chunk_r0;
     std::vector<std::vector<std::pair<int, int>>> chunk_seg;
     int *d_ring_list_chunks = nullptr;
+    int *d_col_ring = nullptr;       // RLZ: ring index of every column (ring point)
     std::vector<int64_t> ring_jofs;  // first ring point of every ring, jDim at the end
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> chunk_ev;

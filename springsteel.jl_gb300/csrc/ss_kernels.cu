@@ -384,16 +384,6 @@ __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
 // cheb_forward: DCT-I of each kz-point column, scaled 1/(2(kz-1)), first bk modes
 // (CBtransform!, src/Chebyshev.jl:417-426).  CTA = 64 consecutive columns.
 // ====================================================================
-__device__ __forceinline__ int ring_of_column(const RingDesc *rings, int iDim, int64_t q) {
-    int lo = 0, hi = iDim - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (rings[mid].jofs <= q) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 // K consecutive shared-memory values (16-byte aligned rows: vector loads for float/double)
 template <typename T, int K>
 __device__ __forceinline__ void load_row(const T *p, T (&v)[K]) {
@@ -458,7 +448,7 @@ __global__ void __launch_bounds__(128) cheb_forward_tiled_kernel(ChebLaunch C) {
     for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
         if (c < ncol) {
             const int64_t q = c0 + c;
-            const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
+            const RingDesc &rd = C.rings[C.col_ring[q]];
             col_base[c] = (int64_t)C.bk * rd.jofs + (q - rd.jofs);
             col_L[c] = rd.L;
         }
@@ -559,7 +549,7 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
     for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
         if (c < ncol) {
             const int64_t q = c0 + c;
-            const RingDesc &rd = C.rings[ring_of_column(C.rings, C.iDim, q)];
+            const RingDesc &rd = C.rings[C.col_ring[q]];
             col_base[c] = (int64_t)C.bk * rd.jofs + (q - rd.jofs);
             col_L[c] = rd.L;
         }
@@ -574,15 +564,20 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
     }
     cp_async_wait_all();
     __syncthreads();
-    // s_p = Σ_i gu[p][i] b_i (the rank term of the Γ fold), appended to both input sets
-    for (int c = threadIdx.x; c < COLS; c += blockDim.x)
-        for (int p = 0; p < nr; p++) {
-            T acc = T(0.0f);
-            for (int i = 0; i < bk; i++)
-                acc = acc + ld_real<T>(cb.gu_t, (int64_t)p * bk + i) * ((i & 1) ? xo : xe)[(size_t)(i >> 1) * COLS + c];
-            xe[(size_t)((bk + 1) / 2 + p) * COLS + c] = acc;
-            xo[(size_t)(bk / 2 + p) * COLS + c] = acc;
+    // s_p = Σ_i gu[p][i] b_i (the rank term of the Γ fold), appended to both input
+    // sets: one (column, p) per thread, even and odd inputs as two partial sums
+    for (int t = threadIdx.x; t < COLS * nr; t += blockDim.x) {
+        const int c = t % COLS, p = t / COLS;
+        const int64_t g0 = (int64_t)p * bk;
+        T se = T(0.0f), so = T(0.0f);
+        for (int i2 = 0; 2 * i2 < bk; i2++) {
+            se = se + ld_real<T>(cb.gu_t, g0 + 2 * i2) * xe[(size_t)i2 * COLS + c];
+            if (2 * i2 + 1 < bk) so = so + ld_real<T>(cb.gu_t, g0 + 2 * i2 + 1) * xo[(size_t)i2 * COLS + c];
         }
+        const T acc = se + so;
+        xe[(size_t)((bk + 1) / 2 + p) * COLS + c] = acc;
+        xo[(size_t)(bk / 2 + p) * COLS + c] = acc;
+    }
     __syncthreads();
     const int nd = (var == 0) ? 3 : 1;
     const T *mtab = (const T *)cb.inv_m_t;

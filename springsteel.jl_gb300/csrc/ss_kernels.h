@@ -69,7 +69,8 @@ struct ChebLaunch {
     const void *in;
     void *out;
     const ChebDev *cheb;       // per variable
-    const RingDesc *rings;     // ring start table (jofs) for column → ring lookup
+    const RingDesc *rings;     // ring start table (jofs, L)
+    const int *col_ring;       // ring index of every column (ring point)
     int64_t jDim, np;
     int64_t col0, col1;        // columns (ring points) [col0, col1) of this launch
     int iDim, bk, nvars;
