@@ -430,13 +430,17 @@ def run_reference(args):
         times.append(dt * nv)  # one full round trip = nv variables
     per = sum(times) / len(times)
     val = 1.0 / per
-    from springsteel_gpu import fields  # noqa: F401
+    import oracle as O
+
+    # the same config object as the GPU arm, its sizes from the oracle's own grid
+    dims = O.OracleGrid(_params(wl).to_abi()).dims
+    config = dict(_config(wl, dims), parallelism="replicas" if ws > 1 else "single")
 
     line = {
         "impl": "reference", "metric": "RLZ transforms/s", "value": val, "unit": "round trips/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOADS[wl], "sample": "1 variable round trip per step, scaled by nvars"},
+        "config": config,
         "cpu_baseline": {"value": val, "unit": "round trips/s", "cores": threads, "kind": "port",
                          "sample": "one of %d variables per step (FP64 C port of the reference path, OpenMP "
                                    "over rings/columns), time x nvars" % WORKLOADS[wl]["nvars"]},
