@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -206,6 +207,16 @@ static int32_t build_grid(ss_grid *g) {
         if (v >= 13 && v <= kMaxPrimeRadix) plans.max_prime = v;
     }
     if (const char *e = std::getenv("SS_FFT_RADER")) plans.rader = std::atoi(e) != 0;
+    // CTA size of the ring kernels: FP64 butterflies leave fewer idle threads per
+    // pass at 128 (measured on the 200-cell RLZ grid: 73.4 ms per round trip
+    // against 77.2 at 256); binary32 is faster at 256 (156.9 against 172.2 ms on
+    // the 400-cell grid).  Batches autotune it per grid.
+    g->ring_threads_fwd = g->ring_threads_inv = (g->tl == TL_F64) ? 128 : 256;
+    // tuning override (64, 128 or 256 threads)
+    if (const char *e = std::getenv("SS_RING_THREADS")) {
+        const int t = std::atoi(e);
+        if (t == 64 || t == 128 || t == 256) g->ring_threads_fwd = g->ring_threads_inv = t;
+    }
     std::vector<double> phase;
     const int nring_sets = g->rlz ? 1 : nv;
     std::vector<RingDesc> rings(size_t(nring_sets) * iDim);
