@@ -9,6 +9,7 @@ Springsteel.jl                         here
 ``createGrid(gp)``                     :func:`createGrid` → :class:`SpringsteelGrid`
 ``spectralTransform!(grid)``           :func:`spectralTransform_b` (alias ``spectralTransform``)
 ``gridTransform!(grid)``               :func:`gridTransform_b` (alias ``gridTransform``)
+the same on a host physical array      :func:`spectralTransform_from_host`, :func:`gridTransform_to_host`
 ``getGridpoints(grid)``                :func:`getGridpoints`
 ``NaturalBC()``, ``DirichletBC()``…    same names (src/Springsteel.jl:68-137)
 ``SpectralFilter``/``GaussianFilter``  same names (src/filtering.jl:31-127)
