@@ -395,6 +395,18 @@ def _dist():
     return ws, rank, local
 
 
+def _max_over_ranks(x, device="cuda"):
+    """The largest `x` over all ranks of the process group (x itself on one rank)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _oracle_sample(wl, threads, seconds_hint=None):
     """One round trip of ONE variable of the workload grid on the host (FP64 oracle)."""
     import oracle as O
@@ -517,10 +529,7 @@ def run_ours(args):
     launches = (C.c_int64 * 6)()
     chk(lib.ss_grid_profile_read(grid.handle, stage_ms, launches))
     chk(lib.ss_grid_profile(grid.handle, 0))
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = _max_over_ranks(ms)
     ms_step = ms / args.steps
     value = ws * args.steps / (ms / 1e3)
 
@@ -549,10 +558,7 @@ def run_ours(args):
             phases.append(((tb - ta) * 1e3, (tc - tb) * 1e3))
         barrier()
         e2e_s = time.perf_counter() - t0
-        if ws > 1:
-            t = torch.tensor([e2e_s], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = _max_over_ranks(e2e_s)
         return ws * e2e_steps / e2e_s, [round(float(np.median([p[i] for p in phases])), 2) for i in range(2)]
 
     with ClockSampler(local) as e2e_clk:
