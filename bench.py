@@ -19,7 +19,12 @@ FP32+refinement grid instead.
   roofline  the dominant stage, timed live with CUDA events inside the timed
             region (the library's stage instrumentation)
   cpu_baseline  the FP64 oracle (C port of the reference path) on the host
-            cores, on one variable of the same grid, scaled to the workload
+            cores: one whole round trip of every variable of the same grid and
+            inputs (the 400-cell FP32 grid: its first variable, host RAM)
+  check     the GPU round trip of the same inputs against that oracle output,
+            per variable and derivative slot (the run fails above 1e-12 in FP64)
+  secondary the default run also measures the 8-variable 400-cell / 64-level
+            FP32+refinement grid and nests its line under "secondary"
 
 ``--impl reference`` times the reference's CPU path instead: Julia is not
 available on either machine, so that arm runs the C port of the reference
@@ -46,10 +51,10 @@ import numpy as np  # noqa: E402
 WORKLOADS = {
     "rlz200-f64": dict(num_cells=200, kDim=32, nvars=5, precision="f64"),
     "rlz200-f64fast": dict(num_cells=200, kDim=32, nvars=5, precision="f64_fast"),
-    "rlz400-f32": dict(num_cells=400, kDim=64, nvars=8, precision="f32"),
+    "rlz400-f32": dict(num_cells=400, kDim=64, nvars=8, precision="f32", noise=1e-2),
     # small case for profiling captures (same kernels, a few hundred MB)
     "rlz100-f64": dict(num_cells=100, kDim=32, nvars=2, precision="f64"),
-    "rlz200-f32": dict(num_cells=200, kDim=64, nvars=2, precision="f32"),
+    "rlz200-f32": dict(num_cells=200, kDim=64, nvars=2, precision="f32", noise=1e-2),
     # 64 uneven RL grids (50-400 cells, 1-4 variables) as one batch under a CUDA graph
     "batch-rl64": dict(ngrids=64, nc_min=50, nc_max=400, nv_min=1, nv_max=4, precision="f64", seed=3),
     "batch-rl64-f32": dict(ngrids=64, nc_min=50, nc_max=400, nv_min=1, nv_max=4, precision="f32", seed=3),
@@ -271,7 +276,8 @@ def _config(wl, dims):
         "geometry": "RLZ", "num_cells": w["num_cells"], "iDim": dims["iDim"], "kDim": w["kDim"],
         "b_kDim": dims["b_kDim"], "nvars": w["nvars"], "jDim": dims["jDim"],
         "physical_points_per_var": dims["n_physical"], "spectral_per_var": dims["n_spectral"],
-        "fields": "seeded Gaussian-blob sums (8 blobs, widths 5-30, z in [0, 20000])",
+        "fields": "seeded Gaussian-blob sums (8 blobs, widths 5-30, z in [0, 20000])" + (
+            " plus N(0, %g) noise" % w["noise"] if w.get("noise") else ""),
         "l2": "inputs larger than L2 (physical slot 1 > 129 MB)",
     }
 
@@ -407,55 +413,114 @@ def _max_over_ranks(x, device="cuda"):
     return float(t.item())
 
 
-def _oracle_sample(wl, threads, seconds_hint=None):
-    """One round trip of ONE variable of the workload grid on the host (FP64 oracle)."""
-    import oracle as O
+def _device_inputs(grid, wl, seed):
+    """Seeded blob-sum fields (plus the workload's noise) written into physical
+    slot 1 on the device; returns a pinned host copy of slot 1, (nvars, n) rows."""
+    import torch
+
     from springsteel_gpu import fields
 
-    w = dict(WORKLOADS[wl])
-    gp = _params(wl)
-    gp1 = fields.rlz_params(num_cells=w["num_cells"], kDim=w["kDim"], nvars=1)
-    o = O.OracleGrid(gp1.to_abi())
+    w = WORKLOADS[wl]
+    fields.fill_rlz_blobs_device(grid, base_seed=seed, zmax=20000.0, noise=w.get("noise", 0.0))
+    d = grid.dims
+    dt = torch.float32 if w["precision"] == "f32" else torch.float64
+    h = torch.empty((d["nvars"], d["n_physical"]), dtype=dt).pin_memory()
+    for v in range(d["nvars"]):
+        h[v].copy_(grid.device_array("physical", v, slot=1))
+    return h
+
+
+def _slot_errors(planes, phys_o, gp):
+    """max|gpu − oracle| / scale per (variable, slot): scale = max(max|oracle slot|,
+    max|oracle f|/ℓ^d) for a derivative of order d along a domain of length ℓ (the
+    tests' parity norm).  planes(v, s) returns the GPU plane as float64 numpy."""
+    lengths = {"r": gp.iMax - gp.iMin, "l": 1.0, "z": (gp.kMax - gp.kMin) or 1.0}
+    deriv = [(None, 0), ("r", 1), ("r", 2), ("l", 1), ("l", 2), ("z", 1), ("z", 2)]
+    out = np.zeros(phys_o.shape[1:])
+    for v in range(phys_o.shape[1]):
+        fmax = np.max(np.abs(phys_o[:, v, 0]))
+        for s in range(phys_o.shape[2]):
+            dirn, d = deriv[s]
+            den = max(np.max(np.abs(phys_o[:, v, s])), fmax / lengths[dirn] ** d if dirn else 0.0)
+            out[v, s] = np.max(np.abs(planes(v, s) - phys_o[:, v, s])) / den if den > 0 else 0.0
+    return out
+
+
+def _oracle_roundtrip(gp, slot1, threads, var_index=None):
+    """spectralTransform! + gridTransform! of the FP64 oracle (the C port of the
+    reference path) on host inputs `slot1` (nvars, n); with var_index, only that
+    variable, on a one-variable grid of the same shape.  Returns (seconds, physical)."""
+    import copy
+
+    import oracle as O
+
     O.set_threads(threads)
-    pts = o.gridpoints()
+    if var_index is not None:
+        g1 = copy.copy(gp)
+        g1.vars = {gp.var_names()[0]: 1}
+        gp, rows = g1, [var_index]
+    else:
+        rows = list(range(slot1.shape[0]))
+    o = O.OracleGrid(gp.to_abi())
     ph = np.zeros(o.physical_shape, order="F")
-    ph[:, 0, 0] = fields.blob_sum(pts, seed=2000, zmax=20000.0)
+    for i, v in enumerate(rows):
+        ph[:, i, 0] = slot1[v]
     t0 = time.perf_counter()
-    sp = o.spectral_transform(ph)
-    o.grid_transform(sp)
+    out = o.grid_transform(o.spectral_transform(ph))
     dt = time.perf_counter() - t0
-    del gp
-    return dt, w["nvars"]
+    o.close()
+    return dt, out
+
+
+# Measured DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum, summed over
+# every bucket launch of one stage pass) per round trip, from ncu captures of the
+# bench workloads themselves (profiles/traffic_ring_stages.md)
+MEASURED_TRAFFIC = {}
 
 
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
+    from springsteel_gpu import fields
+
     threads = os.cpu_count() or 1
     wl = args.workload
-    for _ in range(args.warmup):
-        _oracle_sample(wl, threads)
-    times = []
-    for _ in range(args.steps):
-        dt, nv = _oracle_sample(wl, threads)
-        times.append(dt * nv)  # one full round trip = nv variables
-    per = sum(times) / len(times)
-    val = 1.0 / per
+    w = WORKLOADS[wl]
+    gp = _params(wl)
     import oracle as O
 
-    # the same config object as the GPU arm, its sizes from the oracle's own grid
-    dims = O.OracleGrid(_params(wl).to_abi()).dims
+    o = O.OracleGrid(gp.to_abi())
+    dims = o.dims
+    pts = o.gridpoints()
+    o.close()
+    slot1 = np.stack([fields.blob_sum(pts, seed=2000 + v, zmax=20000.0, noise=w.get("noise", 0.0))
+                      for v in range(dims["nvars"])])
+    del pts
+    one_var = w["precision"] == "f32"  # the 400-cell grid's FP64 oracle exceeds host RAM with all 8 variables
+    times = []
+    for i in range(args.warmup + args.steps):
+        if one_var:
+            dt, _ = _oracle_roundtrip(gp, slot1, threads, var_index=i % dims["nvars"])
+        else:
+            dt, _ = _oracle_roundtrip(gp, slot1, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    per = sum(times) / len(times)
+    units = 1.0 / dims["nvars"] if one_var else 1.0  # round trips per step
+    val = units / per
     config = dict(_config(wl, dims), parallelism="replicas" if ws > 1 else "single")
-
+    sample = ("every variable of the grid per step (one full round trip, spectralTransform! + "
+              "gridTransform!), FP64 C port of the reference path, OpenMP over rings and columns")
+    if one_var:
+        sample = ("one variable per step (1/%d of a round trip, variables in turn), FP64 C port of the "
+                  "reference path; value = round trips per second of measured time" % dims["nvars"])
     line = {
         "impl": "reference", "metric": "RLZ transforms/s", "value": val, "unit": "round trips/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config,
-        "cpu_baseline": {"value": val, "unit": "round trips/s", "cores": threads, "kind": "port",
-                         "sample": "one of %d variables per step (FP64 C port of the reference path, OpenMP "
-                                   "over rings/columns), time x nvars" % WORKLOADS[wl]["nvars"]},
+        "cpu_baseline": {"value": val, "unit": "round trips/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": "round trips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "Julia/FFTW are not installed; the reference arm runs the oracle's C restatement",
     }
@@ -463,29 +528,19 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
+def measure(wl, args, lib, ws, rank, local, cpu_baseline=True):
+    """Device-resident and end-to-end round trips of workload `wl`, the live stage
+    roofline, the CPU baseline (oracle) and a check of the GPU output against it."""
     import torch
 
     import springsteel_gpu as S
-    from springsteel_gpu import abi, fields
+    from springsteel_gpu import abi
 
-    ws, rank, local = _dist()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
-    lib = S.load_library()
-    wl = args.workload
     gp = _params(wl)
     grid = S.createGrid(gp)
     dims = grid.dims
     w = 4 if gp.precision == "f32" else 8
-    pts = S.getGridpoints(grid)
-    u = fields.rlz_blob_fields(pts, dims["nvars"], base_seed=2 + rank, zmax=20000.0)
-    host_dtype = np.float64 if w == 8 else np.float32
-    # pinned host buffers for the end-to-end leg
-    h_in = torch.from_numpy(np.ascontiguousarray(u.T.astype(host_dtype))).pin_memory()
+    h_in = _device_inputs(grid, wl, seed=2 + rank)
     n_out = dims["n_physical"] * dims["nvars"] * dims["nslots"]
     h_out = torch.empty(n_out, dtype=torch.float64 if w == 8 else torch.float32).pin_memory()
     dt_code = abi.SS_DTYPE_F64 if w == 8 else abi.SS_DTYPE_F32
@@ -495,9 +550,7 @@ def run_ours(args):
     def chk(st):
         S._check(st)
 
-    chk(lib.ss_upload_physical(grid.handle, C.c_void_p(h_in.data_ptr()), dt_code, 1, None))
-    sptr = grid.stream()
-    stream = torch.cuda.ExternalStream(sptr)
+    stream = torch.cuda.ExternalStream(grid.stream())
 
     def step():
         chk(lib.ss_spectral_transform(grid.handle, None))
@@ -557,15 +610,15 @@ def run_ours(args):
             tc = time.perf_counter()
             phases.append(((tb - ta) * 1e3, (tc - tb) * 1e3))
         barrier()
-        e2e_s = time.perf_counter() - t0
-        e2e_s = _max_over_ranks(e2e_s)
+        e2e_s = _max_over_ranks(time.perf_counter() - t0)
         return ws * e2e_steps / e2e_s, [round(float(np.median([p[i] for p in phases])), 2) for i in range(2)]
 
     with ClockSampler(local) as e2e_clk:
         e2e_val, (ph_in, ph_out) = e2e_loop(True)
         seq_val, (sq_up, sq_rest) = e2e_loop(False)
     e2e_phase_ms = {"spectral_from_host": ph_in, "grid_to_host": ph_out}
-    # stage events of one overlapped round trip (chunked launches)
+    # stage events of one overlapped round trip (chunked launches); its output is
+    # the one round trip of h_in that the check below compares with the oracle
     chk(lib.ss_grid_profile(grid.handle, 1))
     chk(lib.ss_spectral_transform_from_host(grid.handle, C.c_void_p(h_in.data_ptr()), dt_code, None))
     chk(lib.ss_grid_transform_to_host(grid.handle, C.c_void_p(h_out.data_ptr()), dt_code, None))
@@ -585,12 +638,10 @@ def run_ours(args):
     peak, peak_kind = _peaks()
     achieved = sb[dom] / (per_step_ms[dom] * 1e-3) / 1e9
     path_gbs = _bytes_per_roundtrip(dims, w) / (ms_step * 1e-3) / 1e9
-    # DRAM traffic of ring_inverse: one ncu capture of the 100-cell FP64 case gave
-    # 0.706 × its algorithmic bytes (both grow with rings × z-modes × variables);
-    # other stages and precisions were not captured
-    traffic = round(sb[dom] * 0.706) if (dom == "ring_inverse" and w == 8) else None
+    traffic = MEASURED_TRAFFIC.get((wl, dom))
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "traffic_source": "ncu capture of this workload (profiles/traffic_ring_stages.md)" if traffic else None,
             "algorithmic_bytes_per_launch": sb[dom],
             "stage_ms_per_step": per_step_ms,
             "path_achieved_gbs": path_gbs, "path_frac": path_gbs / peak}
@@ -610,7 +661,7 @@ def run_ours(args):
         t = per_step_ms[st] * 1e-3
         roof["pipe"][st] = {"achieved": nt * ring_flops / t / 1e12, "frac": nt * ring_flops / t / 1e12 / pipe_peak}
 
-    line = {
+    res = {
         "metric": "RLZ transforms/s", "value": value, "unit": "round trips/s", "n_gpus": ws,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if w == 8 else "f32",
@@ -622,19 +673,56 @@ def run_ours(args):
         "gpu_launches": gpu_launches,
         "roofline": roof,
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and cpu_baseline:
         threads = os.cpu_count() or 1
-        dt, nv = _oracle_sample(wl, threads)
-        line["cpu_baseline"] = {
-            "value": 1.0 / (dt * nv), "unit": "round trips/s", "cores": threads, "kind": "port",
-            "sample": "one of %d variables of the same grid, forward+inverse, FP64 C port (oracle), "
-                      "%.2f s, scaled x%d" % (nv, dt, nv)}
+        slot1 = h_in.numpy()
+        nv = dims["nvars"]
+        one_var = w == 4  # the 400-cell grid's FP64 oracle holds ~10 GB per variable
+        dt, phys_o = _oracle_roundtrip(gp, slot1.astype(np.float64), threads, var_index=0 if one_var else None)
+        out = h_out.numpy().reshape(dims["nslots"], nv, dims["n_physical"])
+        errs = _slot_errors(lambda v, s: out[s, v].astype(np.float64), phys_o, gp)
+        units = 1.0 / nv if one_var else 1.0
+        res["cpu_baseline"] = {
+            "value": units / dt, "unit": "round trips/s", "cores": threads, "kind": "port",
+            "sample": ("variable 1 of %d of the same grid and inputs (host RAM), forward+inverse, FP64 C port "
+                       "(oracle), %.2f s; value = 1/%d round trip over that time" % (nv, dt, nv)) if one_var else
+                      ("every variable of the same grid and inputs, one round trip (forward+inverse), FP64 C port "
+                       "(oracle), %.2f s" % dt)}
+        tol = 1e-12 if gp.precision == "f64" else None
+        res["check"] = {
+            "against": "FP64 oracle on the same inputs, one round trip",
+            "variables": [0] if one_var else list(range(nv)),
+            "max_rel_err_per_slot": [float(x) for x in errs.max(axis=0)],
+            "max_rel_err": float(errs.max()), "tolerance": tol,
+            "pass": bool(tol is None or errs.max() <= tol)}
     grid.close()
+    return res
+
+
+def run_ours(args):
+    import torch
+
+    import springsteel_gpu as S
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    lib = S.load_library()
+    line = measure(args.workload, args, lib, ws, rank, local, cpu_baseline=not args.no_cpu_baseline)
+    if args.workload == "rlz200-f64" and not args.no_secondary:
+        # the FP32+refinement 400-cell grid, measured in the same run
+        sec = measure("rlz400-f32", args, lib, ws, rank, local, cpu_baseline=not args.no_cpu_baseline)
+        line["secondary"] = {"rlz400-f32": sec}
     if ws > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    return 0
+    failed = [c for c in [line.get("check")] + [v.get("check") for v in line.get("secondary", {}).values()]
+              if c and not c["pass"]]
+    return 3 if failed else 0
 
 
 def main():
@@ -645,6 +733,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rlz200-f64", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the FP32 400-cell grid of the default run")
     args = ap.parse_args()
     if args.workload == "elliptic-rl200":
         return run_elliptic(args)

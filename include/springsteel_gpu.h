@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define SS_ABI_VERSION 1
+#define SS_ABI_VERSION 2
 
 /* ---- status codes (no exceptions cross the ABI) ------------------------ */
 enum {
@@ -106,9 +106,18 @@ typedef struct ss_grid_params {
     const ss_spline_bc *BCR;           /* nvars entries, NULL → R0              */
     const int32_t *BCB;                /* nvars entries, NULL → SS_CBC_R0       */
     const int32_t *BCT;                /* nvars entries, NULL → SS_CBC_R0       */
-    const int32_t *max_wavenumber;     /* nvars entries, NULL → -1 (ring kmax = ri).
-                                          RLZ rings are shared by all variables
-                                          (src/factory.jl:730-738): entry 0 is used. */
+    const int32_t *max_wavenumber;     /* nvars entries, NULL → -1 (ring kmax = ri);
+                                          RL: one ring set per variable              */
+    /* RLZ rings are shared by all variables (src/factory.jl:730-738).  Their
+     * kmax is the reference's var_kmax: the "default" entry of max_wavenumber,
+     * overridden by each variable's own entry in the order the caller's vars
+     * Dict iterates, so the last variable (in that order) that has an entry of
+     * its own wins.  A caller that knows which variables have their own entry
+     * passes that value in ring_kmax with ring_kmax_set = 1; with
+     * ring_kmax_set = 0 the rings take max_wavenumber[nvars-1] (the loop's
+     * result when every variable has its own entry). */
+    int32_t ring_kmax_set;
+    int32_t ring_kmax;
 } ss_grid_params;
 
 /* Derived dimensions (src/factory.jl:153-175, 290-298, 658-661, 700-706). */

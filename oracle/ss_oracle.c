@@ -1059,7 +1059,12 @@ int32_t or_grid_create(const ss_grid_params *p, or_grid **out) {
         int r = q % g->iDim + 1;
         int ri = r + g->pOL;
         int L = 4 + 4 * ri, kmax = ri;
-        int var_kmax = p->max_wavenumber ? p->max_wavenumber[v] : -1;
+        /* RLZ: rings shared by all variables, var_kmax of src/factory.jl:730-733
+           (the caller's resolved value, else the last variable's entry) */
+        int var_kmax = -1;
+        if (g->geom == SS_GEOM_RL) var_kmax = p->max_wavenumber ? p->max_wavenumber[v] : -1;
+        else if (p->ring_kmax_set) var_kmax = p->ring_kmax;
+        else if (p->max_wavenumber && g->nvars > 0) var_kmax = p->max_wavenumber[g->nvars - 1];
         if (var_kmax >= 0) kmax = var_kmax < ri ? var_kmax : ri;
         double dl = 2 * PI / L;
         double offset = 0.5 * dl * (ri - 1);

@@ -229,7 +229,7 @@ static int32_t build_grid(ss_grid *g) {
             rd.L = 4 + 4 * ri;
             rd.ri = ri;
             int kmax = ri;
-            const int var_kmax = g->kmaxv[g->rlz ? 0 : set];
+            const int var_kmax = g->rlz ? g->ring_kmax : g->kmaxv[set];
             if (var_kmax >= 0) kmax = std::min(var_kmax, ri);
             rd.kmax = kmax;
             rd.plan = plans.plan_for(rd.L / 2, pool);
@@ -790,6 +790,8 @@ int32_t ss_grid_create(const ss_grid_params *params, ss_grid **out) {
         if (p.BCT) g->bct[v] = p.BCT[v];
         if (p.max_wavenumber) g->kmaxv[v] = p.max_wavenumber[v];
     }
+    // RLZ rings shared by all variables: the reference's var_kmax (src/factory.jl:730-733)
+    g->ring_kmax = p.ring_kmax_set ? p.ring_kmax : (nv > 0 ? g->kmaxv[nv - 1] : -1);
     g->p.l_q = nullptr; g->p.BCL = g->p.BCR = nullptr; g->p.BCB = g->p.BCT = nullptr; g->p.max_wavenumber = nullptr;
     cudaGetDevice(&g->device);
     if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -913,6 +915,7 @@ int32_t ss_grid_set_filter(ss_grid *g, int32_t var, const double *fw, const doub
     CUDA_TRY(cudaMemcpyAsync(g->d_cw + size_t(var) * bk, c.data(), c.size() * 8, cudaMemcpyHostToDevice, g->stream));
     CUDA_TRY(cudaStreamSynchronize(g->stream));
     if (fw || cw) g->filtered = 1;
+    g->generation++;
     return SS_OK;
 }
 
@@ -926,6 +929,7 @@ int32_t ss_grid_set_ahat(ss_grid *g, int32_t var, int32_t block, const double *a
     if (!g->d_ahat) {
         int32_t st = dev_alloc(g, (void **)&g->d_ahat, size_t(g->d.nvars) * g->d.n_blocks * b * 8);
         if (st) return st;
+        g->generation++;
     }
     CUDA_TRY(cudaMemcpyAsync(g->d_ahat + (size_t(var) * g->d.n_blocks + block) * b, ahat, b * 8, cudaMemcpyHostToDevice,
                              g->stream));
@@ -940,6 +944,7 @@ int32_t ss_grid_clear_ahat(ss_grid *g) {
         cudaFree(g->d_ahat);
         g->allocs.erase(std::remove(g->allocs.begin(), g->allocs.end(), (void *)g->d_ahat), g->allocs.end());
         g->d_ahat = nullptr;
+        g->generation++;
     }
     return SS_OK;
 }

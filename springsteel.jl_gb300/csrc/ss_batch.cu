@@ -33,7 +33,16 @@ struct ss_batch {
     std::vector<cudaEvent_t> ev;
     cudaGraph_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<uint64_t> gen[4];  // each grid's generation when graph[what] was captured
 };
+
+// The grids' generation counters; a graph whose grids have changed since (ahat registered or cleared, filter set) is captured again,
+// because its launches hold the old pointers and flags.
+static std::vector<uint64_t> generations(const ss_batch *bt) {
+    std::vector<uint64_t> out;
+    for (const ss_grid *g : bt->grids) out.push_back(g->generation);
+    return out;
+}
 
 static int32_t run_direction(ss_grid *g, int what, cudaStream_t st) {
     int32_t r = SS_OK;
@@ -152,6 +161,13 @@ extern "C" int32_t ss_batch_run(ss_batch *bt, int32_t what, int32_t use_graph, v
     for (ss_grid *g : bt->grids)
         if (g->profiling) { set_error("disable stage profiling on batched grids"); return SS_BAD_ARG; }
     if (!use_graph) return enqueue_batch(bt, what, st);
+    if (bt->exec[what] && bt->gen[what] != generations(bt)) {
+        CUDA_TRY(cudaStreamSynchronize(st));  // a replay in flight still uses the old graph
+        cudaGraphExecDestroy(bt->exec[what]);
+        cudaGraphDestroy(bt->graph[what]);
+        bt->exec[what] = nullptr;
+        bt->graph[what] = nullptr;
+    }
     if (!bt->exec[what]) {
         // capture on the batch's own stream, then launch the graph on `st`
         CUDA_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeRelaxed));
@@ -162,6 +178,7 @@ extern "C" int32_t ss_batch_run(ss_batch *bt, int32_t what, int32_t use_graph, v
         if (e != cudaSuccess) { set_error("graph capture failed: %s", cudaGetErrorString(e)); return SS_CUDA_ERROR; }
         bt->graph[what] = graph;
         CUDA_TRY(cudaGraphInstantiate(&bt->exec[what], graph, 0));
+        bt->gen[what] = generations(bt);
     }
     CUDA_TRY(cudaGraphLaunch(bt->exec[what], st));
     return SS_OK;

@@ -27,6 +27,10 @@ struct ss_grid {
     std::vector<double> l_q;
     std::vector<ss_spline_bc> bcl, bcr;
     std::vector<int32_t> bcb, bct, kmaxv;
+    int32_t ring_kmax = -1;  // RLZ: kmax cap of the rings all variables share
+    // bumped by every call that changes what a launch sequence captures (the
+    // ahat pointer, the filter flag): batches re-capture their graphs on change
+    uint64_t generation = 0;
     ss_dims d{};
     int prec = SS_PREC_F64;
     int tl = TL_F64;   // compute layout of tables and intermediates

@@ -308,6 +308,18 @@ class SpringsteelGridParameters:
             names[v - 1] = k
         return names
 
+    def shared_ring_kmax(self):
+        """kmax cap of the RLZ rings, which every variable shares: the "default"
+        entry, overridden by each variable's own entry in the order ``vars``
+        iterates (src/factory.jl:730-733).  The reference's vars is a Julia Dict
+        (hash order); here it is a Python dict (insertion order), and a Julia
+        caller computes the same value with the same loop over its own Dict."""
+        km = int(self.max_wavenumber.get("default", -1))
+        for key in self.vars:
+            if key in self.max_wavenumber:
+                km = int(self.max_wavenumber[key])
+        return km
+
     def to_abi(self):
         names = self.var_names()
         nv = len(names)
@@ -323,6 +335,7 @@ class SpringsteelGridParameters:
             max_wavenumber=[int(_per_var(self.max_wavenumber, n, -1)) for n in names],
         )
         if self.geometry == "RLZ":
+            kw["ring_kmax"] = self.shared_ring_kmax()
             kw.update(kDim=self.kDim, b_kDim=self.b_kDim, kMin=self.kMin, kMax=self.kMax,
                       BCB=[_bc_to_chebyshev(_per_var(self.BCB, n, CHEB_R0)) for n in names],
                       BCT=[_bc_to_chebyshev(_per_var(self.BCT, n, CHEB_R0)) for n in names])
@@ -386,6 +399,28 @@ class SpringsteelGrid:
         _check(load_library().ss_download_physical(self._h, out.ctypes.data_as(C.c_void_p),
                                                    _DTYPES[np.dtype(dtype)], int(slot), None))
         return out
+
+    def device_array(self, which, var, slot=1):
+        """One variable's column of grid.physical (slot 1-based) or grid.spectral
+        as a torch CUDA tensor viewing the grid's own device memory (no copy),
+        for checks that must not download every variable of a large grid."""
+        import torch
+
+        d = self.dims
+        n = d["n_physical"] if which == "physical" else d["n_spectral"]
+        p = C.c_void_p()
+        fn = load_library().ss_grid_device_physical if which == "physical" else load_library().ss_grid_device_spectral
+        _check(fn(self._h, C.byref(p)))
+        esz = 4 if self.params.precision == "f32" else 8
+        plane = ((slot - 1) * d["nvars"] + var) if which == "physical" else var
+        self.synchronize()
+
+        class _View:
+            __cuda_array_interface__ = {
+                "shape": (n,), "typestr": "<f4" if esz == 4 else "<f8",
+                "data": (p.value + plane * n * esz, False), "version": 3, "strides": None}
+
+        return torch.as_tensor(_View(), device="cuda")
 
     def set_physical(self, arr, slot=1):
         n, nv, ns = self.physical_shape

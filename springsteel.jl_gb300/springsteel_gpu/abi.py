@@ -72,6 +72,8 @@ class ss_grid_params(C.Structure):
         ("BCB", C.POINTER(C.c_int32)),
         ("BCT", C.POINTER(C.c_int32)),
         ("max_wavenumber", C.POINTER(C.c_int32)),
+        ("ring_kmax_set", C.c_int32),
+        ("ring_kmax", C.c_int32),
     ]
 
 
@@ -98,10 +100,12 @@ class ParamBundle:
 
 def make_params(geometry, num_cells, iMin, iMax, nvars, *, mubar=3, quadrature=SS_QUAD_GAUSS,
                 kDim=0, b_kDim=0, kMin=0.0, kMax=0.0, patchOffsetL=0, precision=SS_PREC_F64,
-                l_q=None, BCL=None, BCR=None, BCB=None, BCT=None, max_wavenumber=None):
+                l_q=None, BCL=None, BCR=None, BCB=None, BCT=None, max_wavenumber=None, ring_kmax=None):
     """Build an ``ss_grid_params``.  Per-variable entries are sequences of
     length ``nvars``: l_q floats, BCL/BCR ``(kind, alpha, beta)`` tuples,
-    BCB/BCT Chebyshev kinds, max_wavenumber ints (-1 = ring kmax)."""
+    BCB/BCT Chebyshev kinds, max_wavenumber ints (-1 = ring kmax).
+    ``ring_kmax`` (RLZ) is the kmax cap of the rings every variable shares;
+    None leaves it to the library (the last variable's entry)."""
     keep = []
 
     def arr(ctype, vals):
@@ -139,6 +143,8 @@ def make_params(geometry, num_cells, iMin, iMax, nvars, *, mubar=3, quadrature=S
         p.BCT = arr(C.c_int32, [int(x) for x in BCT])
     if max_wavenumber is not None:
         p.max_wavenumber = arr(C.c_int32, [int(x) for x in max_wavenumber])
+    if ring_kmax is not None:
+        p.ring_kmax_set, p.ring_kmax = 1, int(ring_kmax)
     return ParamBundle(p, keep)
 
 

@@ -138,3 +138,84 @@ def radial_mish(gp):
     else:
         q = (2 * np.arange(1, mb + 1) - 1) / (2 * mb)
     return np.array([gp.iMin + mc * DX + q[mu] * DX for mc in range(nc) for mu in range(mb)])
+
+
+# ------------------------------------------------------------ device-side fields
+def column_coordinates_device(grid):
+    """(r, λ) of every ring point in jDim order and the Chebyshev levels z (for RLZ),
+    as torch CUDA float64 tensors: the getGridpoints coordinates without building
+    the (n_physical, 3) host array."""
+    import math
+
+    import torch
+
+    gp, d = grid.params, grid.dims
+    rmish = torch.tensor(radial_mish(gp), dtype=torch.float64, device="cuda")
+    ri = torch.arange(1, d["iDim"] + 1, device="cuda", dtype=torch.int64) + gp.patchOffsetL
+    L = 4 + 4 * ri
+    ring = torch.repeat_interleave(torch.arange(d["iDim"], device="cuda"), L)
+    start = torch.cumsum(L, 0) - L
+    j = torch.arange(int(L.sum().item()), device="cuda") - start[ring]
+    Lr = L[ring].to(torch.float64)
+    lam = 0.5 * (2 * math.pi / Lr) * (ri[ring].to(torch.float64) - 1) + 2 * math.pi * j.to(torch.float64) / Lr
+    r = rmish[ring]
+    z = None
+    if gp.geometry == "RLZ":
+        N = gp.kDim
+        scale, offset = -0.5 * (gp.kMax - gp.kMin), 0.5 * (gp.kMin + gp.kMax)
+        z = torch.cos(torch.arange(N, device="cuda", dtype=torch.float64) * math.pi / (N - 1)) * scale + offset
+    return r, lam, z
+
+
+def blob_sum_device(coords, seed, nblobs=8, rmax=None, zmin=0.0, zmax=1.0, wmin=5.0, wmax=30.0, vert=100.0,
+                    noise=0.0):
+    """blob_sum evaluated on the GPU (float64) from column_coordinates_device output:
+    the same random draws in the same order, so the field equals blob_sum's to
+    rounding; the optional N(0, noise) term comes from a seeded torch CUDA
+    generator.  Returns a flat tensor in physical-row order (z fastest for RLZ)."""
+    import torch
+
+    r, lam, z = coords
+    rng = np.random.default_rng(seed)
+    x, y = r * torch.cos(lam), r * torch.sin(lam)
+    if rmax is None:
+        rmax = float(r.max().item())
+    kz = 1 if z is None else z.numel()
+    out = torch.zeros((r.numel(), kz), dtype=torch.float64, device="cuda")
+    for _ in range(nblobs):
+        rc = rmax * np.sqrt(rng.uniform())
+        tc = rng.uniform(0.0, 2 * np.pi)
+        xc, yc = rc * np.cos(tc), rc * np.sin(tc)
+        zc = rng.uniform(zmin, zmax)
+        w = rng.uniform(wmin, wmax)
+        A = rng.normal()
+        e = (((x - xc) ** 2 + (y - yc) ** 2) / (w * w))[:, None]
+        if z is not None:
+            e = e + (((z - zc) / (vert * w)) ** 2)[None, :]
+        out += A * torch.exp(-e)
+    out = out.reshape(-1)
+    if noise:
+        g = torch.Generator(device="cuda")
+        g.manual_seed(int(seed))
+        out += noise * torch.randn(out.shape, dtype=torch.float64, device="cuda", generator=g)
+    return out
+
+
+def fill_rlz_blobs_device(grid, base_seed=2, zmax=20000.0, noise=0.0, variables=None):
+    """Write seeded blob-sum fields into physical slot 1 of `grid` on the device
+    (variables not listed are zeroed); returns {var: float64 tensor of the field}."""
+    coords = column_coordinates_device(grid)
+    out = {}
+    nv = grid.dims["nvars"]
+    for v in range(nv):
+        dst = grid.device_array("physical", v, slot=1)
+        if variables is not None and v not in variables:
+            dst.zero_()
+            continue
+        f = blob_sum_device(coords, seed=base_seed * 1000 + v, zmax=zmax, noise=noise)
+        dst.copy_(f)
+        out[v] = f
+    import torch
+
+    torch.cuda.synchronize()
+    return out

@@ -37,7 +37,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_layout_matches_header():
     assert C.sizeof(abi.ss_spline_bc) == 24
-    assert C.sizeof(abi.ss_grid_params) == 10 * 4 + 4 * 8 + 6 * 8
+    assert C.sizeof(abi.ss_grid_params) == 10 * 4 + 4 * 8 + 6 * 8 + 2 * 4
     assert C.sizeof(abi.ss_dims) == 12 * 8
 
 
@@ -69,7 +69,7 @@ def test_mlp_without_gpu_fails_loudly():
 
 def test_version_and_error_string():
     lib = S.load_library()
-    assert lib.ss_version() == 1
+    assert lib.ss_version() == 2
     assert isinstance(lib.ss_last_error_string(), bytes)
 
 

@@ -1,0 +1,96 @@
+"""GPU parity at the benchmarked sizes, one variable at a time against the FP64 oracle.
+
+* RLZ, 200 cells × 32 Chebyshev levels, 5 variables, FP64 (the headline
+  benchmark grid): every variable and every derivative slot within 1e-12.
+* RLZ, 400 cells × 64 levels, 8 variables, FP32+refinement (the FP32 benchmark
+  grid; blob sums plus N(0, 1e-2) noise): the per-variable, per-slot error
+  against the FP64 oracle is printed and bounded.
+
+The long rings of these grids (up to 4804 points) take the Rader passes, the
+direct prime passes and every FFT bucket that small grids barely exercise.
+The GPU grid holds all variables; the oracle runs one variable per grid so its
+host arrays stay a few GB.  Inputs are generated on the device (seeded) and the
+same values are handed to the oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import springsteel_gpu as S
+from springsteel_gpu import fields
+from test_gpu_parity import TOL64, slot_errors
+
+pytestmark = pytest.mark.gpu
+
+
+def _one_var_params(gp):
+    import copy
+
+    g1 = copy.copy(gp)
+    name = gp.var_names()[0]
+    g1.vars = {name: 1}
+    return g1
+
+
+def _compare_var(grid, gp, v, field):
+    """(spectral error, per-slot errors) of variable v against the oracle run on that variable alone."""
+    g1 = _one_var_params(gp)
+    o = O.OracleGrid(g1.to_abi())
+    ph = np.zeros(o.physical_shape, order="F")
+    ph[:, 0, 0] = field.cpu().numpy()
+    spec_o = o.spectral_transform(ph)
+    phys_o = o.grid_transform(spec_o)
+    spec_g = grid.device_array("spectral", v).double().cpu().numpy()
+    den = np.max(np.abs(spec_o[:, 0]))
+    espec = float(np.max(np.abs(spec_g - spec_o[:, 0])) / den)
+    phys_g = np.empty_like(phys_o)
+    for s in range(phys_o.shape[2]):
+        phys_g[:, 0, s] = grid.device_array("physical", v, slot=s + 1).double().cpu().numpy()
+    errs = slot_errors(phys_g, phys_o, g1)[0]
+    o.close()
+    return espec, errs
+
+
+def test_rlz200_kz32_5var_f64_full_size_parity():
+    gp = fields.rlz_params()  # 200 cells, 32 levels, 5 variables, FP64
+    grid = S.createGrid(gp)
+    assert grid.dims["iDim"] == 600 and grid.dims["nvars"] == 5
+    inputs = fields.fill_rlz_blobs_device(grid, base_seed=2, zmax=20000.0)
+    S.spectralTransform_b(grid)
+    S.gridTransform_b(grid)
+    grid.synchronize()
+    worst = 0.0
+    for v in range(5):
+        espec, errs = _compare_var(grid, gp, v, inputs[v])
+        print("rlz200 f64 var %d: spectral %.2e, slots %s" % (v, espec, np.array2string(errs, precision=2)))
+        assert espec <= TOL64, (v, espec)
+        assert np.all(errs <= TOL64), (v, errs)
+        worst = max(worst, espec, float(errs.max()))
+    print("rlz200 f64 worst relative error %.2e" % worst)
+    grid.close()
+
+
+# FP32 bulk with an FP64 factor and one FP64 refinement step: binary32 storage
+# bounds f near 1e-7; the derivative slots amplify the binary32 rounding of the
+# ring and column transforms (∂λ by k up to 1200, ∂λλ by k², ∂z by the Chebyshev
+# recurrence), and the N(0, 1e-2) noise puts energy up to the highest modes.
+F32_BOUNDS = np.array([2e-6, 2e-4, 2e-3, 2e-4, 2e-3, 2e-4, 2e-3])
+
+
+def test_rlz400_kz64_8var_f32_per_variable_errors():
+    gp = fields.rlz400_f32_params()  # 400 cells, 64 levels, 8 variables, FP32+refinement
+    grid = S.createGrid(gp)
+    assert grid.dims["iDim"] == 1200 and grid.dims["nvars"] == 8
+    check = (0, 7)
+    inputs = fields.fill_rlz_blobs_device(grid, base_seed=4, zmax=20000.0, noise=1e-2, variables=check)
+    S.spectralTransform_b(grid)
+    S.gridTransform_b(grid)
+    grid.synchronize()
+    for v in check:
+        # the GPU consumed the binary32-rounded field; so does the oracle
+        espec, errs = _compare_var(grid, gp, v, inputs[v].float().double())
+        print("rlz400 f32 var %d: spectral %.2e, slots [f, dr, drr, dl, dll, dz, dzz] %s"
+              % (v, espec, np.array2string(errs, precision=2)))
+        assert espec <= 1e-5, (v, espec)
+        assert np.all(errs <= F32_BOUNDS), (v, errs)
+    grid.close()

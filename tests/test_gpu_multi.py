@@ -85,6 +85,54 @@ def test_batch_matches_single_grid_calls(use_graph, autotune):
         assert all(t in (64, 128, 256) for i in range(6) for t in batch.ring_threads(i))
 
 
+def test_batch_graph_recaptured_after_filter_and_ahat_changes():
+    """A batch graph holds each grid's launch arguments (filter flag, ahat
+    pointer); changing them between runs re-captures it, so replays equal fresh
+    single-grid calls with the new settings."""
+    import ctypes as C
+
+    lib = S.load_library()
+    gps = [S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=20.0, num_cells=20),
+           S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=20.0, num_cells=12,
+                                       BCL={"default": S.FixedBC()})]
+    grids = [S.createGrid(gp) for gp in gps]
+    inputs = [_fill(g, seed=20 + i) for i, g in enumerate(grids)]
+    b1 = grids[1].dims["b_iDim"]
+    ahat = np.zeros(b1)
+    ahat[:3] = (0.7, -0.2, 0.4)
+    batch = S.Batch(grids)
+
+    def run_batch():
+        for g, u in zip(grids, inputs):
+            g.set_physical(u, slot=1)
+        batch.run(what=3, use_graph=True)
+        batch.synchronize()
+        return [g.get_physical() for g in grids]
+
+    def singles():
+        out = []
+        for g, u in zip(grids, inputs):
+            g.set_physical(u, slot=1)
+            S.spectralTransform_b(g)
+            S.gridTransform_b(g)
+            out.append(g.get_physical())
+        return out
+
+    run_batch()  # captured without filter or ahat
+    K = grids[0].dims["kDim_wn"]
+    fw = np.array([1.0 if k <= 4 else 0.0 for k in range(K + 1)])
+    S._check(lib.ss_grid_set_filter(grids[0].handle, 0, fw.ctypes.data_as(C.c_void_p), None))
+    grids[1].set_wavenumber_ahat(0, 0, ahat)
+    got, ref = run_batch(), singles()
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    grids[1].clear_wavenumber_ahat()  # frees the registry the captured graph pointed to
+    got, ref = run_batch(), singles()
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    batch.close()
+
+
 def _sum_spectral_tile(patch_spec, tile_spec, pp, tp):
     """sumSpectralTile! for RLZ (src/tiling.jl:1101-1136) on host arrays."""
     siL = tp.spectralIndexL

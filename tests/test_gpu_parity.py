@@ -288,3 +288,17 @@ def test_host_overlapped_transforms_match(geometry, precision, host):
             phys = S.gridTransform_to_host(g, dtype=hdt)
     assert np.array_equal(spec, spec_ref)
     assert np.array_equal(phys, phys_ref)
+
+
+def test_rlz_unequal_max_wavenumber():
+    """Variables with different max_wavenumber entries on RLZ: the shared rings take
+    the last own entry in vars order (src/factory.jl:730-733) on both sides."""
+    gp = S.SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=40.0, num_cells=20, kMin=0.0,
+                                     kMax=20000.0, kDim=16, vars={"w": 3, "u": 1, "v": 2},
+                                     max_wavenumber={"default": 9, "w": 4, "u": 6},
+                                     BCB={"default": S.DirichletBC()}, BCT={"default": S.NeumannBC()})
+    assert gp.shared_ring_kmax() == 6
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = fields.rlz_blob_fields(pts, 3, zmax=20000.0)
+    _, o, sg, so, pg, po = _run_both(gp, u)
+    _assert_parity(sg, so, pg, po, gp)

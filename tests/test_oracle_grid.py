@@ -141,3 +141,41 @@ def test_unsupported_spline_periodic():
     with pytest.raises(O.OracleError) as e:
         _rl(4, 10.0, BCL=[(abi.SS_SBC_PERIODIC, 0, 0)], BCR=[(abi.SS_SBC_PERIODIC, 0, 0)])
     assert e.value.status == abi.SS_UNSUPPORTED_BC
+
+
+def _rlz_spectral_wavenumber_norms(gp):
+    """max |coefficient| per Fourier wavenumber k of an RLZ oracle transform of a
+    field rich in λ (all variables), spectral layout [z_b][k0 | k1 re | k1 im | …][b]."""
+    o = O.OracleGrid(gp.to_abi())
+    pts = o.gridpoints()
+    ph = np.zeros(o.physical_shape, order="F")
+    for v in range(o.physical_shape[1]):
+        ph[:, v, 0] = sum(np.cos(k * pts[:, 1] + 0.3 * v) for k in range(12)) * (1 + pts[:, 0] / 10.0)
+    sp = o.spectral_transform(ph)
+    d = o.dims
+    b, K = d["b_iDim"], d["kDim_wn"]
+    blocks = sp.reshape(d["b_kDim"], 1 + 2 * K, b, -1)
+    return np.array([np.max(np.abs(blocks[:, 0 if k == 0 else 2 * k - 1: 1 if k == 0 else 2 * k + 1]))
+                     for k in range(K + 1)])
+
+
+@pytest.mark.parametrize("vars_, mw, expect", [
+    ({"a": 1, "b": 2, "c": 3}, {"default": -1, "a": 3, "b": 5}, 5),   # last key with an entry: b
+    ({"c": 3, "b": 2, "a": 1}, {"default": -1, "a": 3, "b": 5}, 3),   # iteration order c, b, a: a wins
+    ({"a": 1, "b": 2}, {"default": 4}, 4),                            # no own entry: the default
+    ({"a": 1, "b": 2}, {"default": 2, "a": -1}, None),                # an own -1 lifts the default cap
+])
+def test_rlz_shared_ring_kmax_rule(vars_, mw, expect):
+    """RLZ rings are shared by every variable; their kmax is the default entry
+    overridden by each variable's own entry in vars order (src/factory.jl:730-733)."""
+    import springsteel_gpu as S
+
+    gp = S.SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=10.0, num_cells=4, kMin=0.0, kMax=1.0,
+                                     kDim=6, vars=vars_, max_wavenumber=mw)
+    assert gp.shared_ring_kmax() == (-1 if expect is None else expect)
+    norms = _rlz_spectral_wavenumber_norms(gp)
+    if expect is None:
+        assert np.all(norms[1:12] > 1e-8)
+    else:
+        assert np.all(norms[: expect + 1] > 1e-8), norms
+        assert np.all(norms[expect + 1:] == 0.0), norms

@@ -29,11 +29,17 @@ def _reference_spectral(grid, u):
     return grid.get_spectral()
 
 
-def test_noalloc_matches_spectral_transform_twice():
+@pytest.mark.parametrize("precision", ["f64", "f64_fast"])
+def test_noalloc_matches_spectral_transform_twice(precision):
+    """Both FP64-storage precisions the entry point accepts: binary64 arithmetic
+    and the double-float FFT arithmetic of SS_PREC_F64_FAST; the reference
+    result is the existing entry point on the same grid, so the same
+    tolerance applies to both."""
     import torch
 
     lib = S.load_library()
-    gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=100.0, num_cells=100, vars={"u": 1, "v": 2})
+    gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=100.0, num_cells=100, vars={"u": 1, "v": 2},
+                                     precision=precision)
     grid = S.createGrid(gp)
     pts = S.getGridpoints(grid)
     d = grid.dims
