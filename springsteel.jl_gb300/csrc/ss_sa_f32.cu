@@ -4,8 +4,10 @@
 // banded system Γ(P+Q)Γᵀ x = Γ b and unfolds a = Γᵀ x (+ ahat); SIxcoeff/
 // SIxxcoeff evaluate f, ∂r, ∂rr at the mish points from 4-tap windows of a.
 // In binary32 the solve runs on the FP32-rounded Cholesky factor, followed by
-// one residual r = Γb − A x in df64 against the FP64 open-form band and a
-// correction solve (x += L⁻ᵀL⁻¹ r).
+// one refinement step in FP64: the residual r = Γb − A x against the FP64
+// open-form band and the correction solve x += L⁻ᵀL⁻¹ r with the FP64 factor
+// (FP64 arithmetic throughout; the forward sweep's intermediate is kept in
+// binary32 between the two sweeps, an error of order 2^-24·|c| ≈ 2^-48·|x|).
 //
 // Layout: one thread per spectral slot, 128 consecutive slots per CTA, every
 // thread solving.  The per-slot vectors live in two slot-interleaved scratch
@@ -15,9 +17,9 @@
 //   1  stage b in 32-row chunks through shared memory; b̃ = b − PQ·ahat;
 //      Γ fold → X; forward substitution L y = Γb → Y
 //   2  backward substitution Lᵀ x = y, in place in Y
-//   3  residual r = Γb − A x (df64) fused with the forward substitution of the
-//      correction → X
-//   4  backward substitution of the correction, x + c, unfold a = Γᵀ x + ahat
+//   3  residual r = Γb − A x (FP64) fused with the FP64 forward substitution
+//      of the correction → X
+//   4  FP64 backward substitution of the correction, x + c, unfold a = Γᵀ x + ahat
 //      written shifted by rankL into Y (descending rows, so every row is read
 //      before it is overwritten), boundary rows last
 //   5  SI / SIx / SIxx at the mish points of every ring that carries the slot,
@@ -73,6 +75,7 @@ __global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, floa
         }
     }
     float y1 = 0.f, y2 = 0.f, y3 = 0.f;
+    double g0d = 0.0, g1d = 0.0, gm2d = 0.0, gm1d = 0.0;  // Γb rows 0, 1, n−2, n−1 in FP64 (the residual's)
     for (int m0 = 0; m0 < Md; m0 += kSaChunk) {
         const int mc = min(kSaChunk, Md - m0);
         __syncthreads();
@@ -96,16 +99,24 @@ __global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, floa
             if (i < 0 || i >= n) continue;
             // Γ fold (src/CubicBSpline.jl:427-463): row i = b_{i+rankL} + boundary terms
             float gb = bm;
-            if (i == 0) {
-                if (sp.lk == BC_A1) gb += aL * b0;
-                else if (sp.lk == BC_A2) gb += aL * b0 + bL * b1;
+            if (i <= 1 || i >= n - 2) {  // boundary rows: the fold in FP64 for the residual
+                double gd = (double)bm;
+                if (i == 0) {
+                    if (sp.lk == BC_A1) gd += sp.aL * (double)b0;
+                    else if (sp.lk == BC_A2) gd += sp.aL * (double)b0 + sp.bL * (double)b1;
+                }
+                if (i == 1 && sp.lk == BC_A1) gd += sp.bL * (double)b0;
+                if (i == n - 1) {
+                    if (sp.rk == BC_A1) gd += sp.aR * (double)bM1;
+                    else if (sp.rk == BC_A2) gd += sp.aR * (double)bM1 + sp.bR * (double)bM2;
+                }
+                if (i == n - 2 && sp.rk == BC_A1) gd += sp.bR * (double)bM1;
+                if (i == 0) g0d = gd;
+                if (i == 1) g1d = gd;
+                if (i == n - 2) gm2d = gd;
+                if (i == n - 1) gm1d = gd;
+                gb = (float)gd;
             }
-            if (i == 1 && sp.lk == BC_A1) gb += bL * b0;
-            if (i == n - 1) {
-                if (sp.rk == BC_A1) gb += aR * bM1;
-                else if (sp.rk == BC_A2) gb += aR * bM1 + bR * bM2;
-            }
-            if (i == n - 2 && sp.rk == BC_A1) gb += bR * bM1;
             Xc[(size_t)i * ns] = gb;
             float acc = gb;
             if (i >= 3) acc -= Lf[(i - 3) * 4 + 3] * y3;
@@ -139,15 +150,16 @@ __global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, floa
             }
         }
 
-        // ---- sweep 3: r = Γb − A x in df64, window w[q] = x_{i+q−3}; forward
-        //      substitution of the correction L c' = r → X
+        // ---- sweep 3: r = Γb − A x in FP64, window w[q] = x_{i+q−3}; FP64 forward
+        //      substitution of the correction L c' = r with the FP64 factor → X
+        const double *Ld = sp.L4, *Dd = sp.dinv, *Ab = sp.Aband;
         float w[7];
 #pragma unroll
         for (int q = 0; q < 7; q++) {
             const int j = q - 3;
             w[q] = (j >= 0 && j < n) ? Yc[(size_t)j * ns] : 0.f;
         }
-        y1 = y2 = y3 = 0.f;
+        double z1 = 0.0, z2 = 0.0, z3 = 0.0;
         for (int lo = 0; lo < n; lo += kSaBlk) {
             float gv[kSaBlk], xn[kSaBlk];
 #pragma unroll
@@ -160,30 +172,29 @@ __global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, floa
             for (int k = 0; k < kSaBlk; k++) {
                 const int i = lo + k;
                 if (i >= n) break;
-                df64 acc = df64(gv[k]);
+                double acc = i == 0 ? g0d : (i == 1 ? g1d : (i == n - 2 ? gm2d : (i == n - 1 ? gm1d : (double)gv[k])));
 #pragma unroll
                 for (int q = 0; q < 7; q++) {
                     const int j = i + q - 3;
                     if (j < 0 || j >= n) continue;
-                    const float2 a = __ldg(sp.Aband_x + min(i, j) * 4 + abs(q - 3));
-                    acc = acc - df_mul_f(df64(a.x, a.y), w[q]);
+                    acc -= __ldg(Ab + min(i, j) * 4 + abs(q - 3)) * (double)w[q];
                 }
-                float c = acc.hi + acc.lo;
-                if (i >= 3) c -= Lf[(i - 3) * 4 + 3] * y3;
-                if (i >= 2) c -= Lf[(i - 2) * 4 + 2] * y2;
-                if (i >= 1) c -= Lf[(i - 1) * 4 + 1] * y1;
-                const float yi = c * Df[i];
-                Xc[(size_t)i * ns] = yi;
-                y3 = y2; y2 = y1; y1 = yi;
+                if (i >= 3) acc -= __ldg(Ld + (i - 3) * 4 + 3) * z3;
+                if (i >= 2) acc -= __ldg(Ld + (i - 2) * 4 + 2) * z2;
+                if (i >= 1) acc -= __ldg(Ld + (i - 1) * 4 + 1) * z1;
+                const double zi = acc * __ldg(Dd + i);
+                Xc[(size_t)i * ns] = (float)zi;
+                z3 = z2; z2 = z1; z1 = zi;
 #pragma unroll
                 for (int q = 0; q < 6; q++) w[q] = w[q + 1];
                 w[6] = xn[k];
             }
         }
 
-        // ---- sweep 4: Lᵀ c = c', x + c, a_{i+rankL} = x_i (+ ahat) → Y row i + rankL
+        // ---- sweep 4: Lᵀ c = c' in FP64 with the FP64 factor, x + c, a_{i+rankL} =
+        //      x_i (+ ahat) → Y row i + rankL
         float x0 = 0.f, xs1 = 0.f, xn1 = 0.f, xn2 = 0.f;
-        x1 = x2 = x3 = 0.f;
+        double c1 = 0.0, c2 = 0.0, c3 = 0.0;
         for (int hi = n - 1; hi >= 0; hi -= kSaBlk) {
             float cv[kSaBlk], xv[kSaBlk];
 #pragma unroll
@@ -196,13 +207,13 @@ __global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, floa
             for (int k = 0; k < kSaBlk; k++) {
                 const int i = hi - k;
                 if (i < 0) break;
-                float acc = cv[k];
-                if (i + 1 < n) acc -= Lf[i * 4 + 1] * x1;
-                if (i + 2 < n) acc -= Lf[i * 4 + 2] * x2;
-                if (i + 3 < n) acc -= Lf[i * 4 + 3] * x3;
-                const float ci = acc * Df[i];
-                x3 = x2; x2 = x1; x1 = ci;
-                const float xf = xv[k] + ci;
+                double acc = (double)cv[k];
+                if (i + 1 < n) acc -= __ldg(Ld + i * 4 + 1) * c1;
+                if (i + 2 < n) acc -= __ldg(Ld + i * 4 + 2) * c2;
+                if (i + 3 < n) acc -= __ldg(Ld + i * 4 + 3) * c3;
+                const double ci = acc * __ldg(Dd + i);
+                c3 = c2; c2 = c1; c1 = ci;
+                const float xf = (float)((double)xv[k] + ci);
                 if (i == n - 1) xn1 = xf;
                 if (i == n - 2) xn2 = xf;
                 if (i == 1) xs1 = xf;

@@ -34,6 +34,9 @@ def _one_var_params(gp):
 
 def _compare_var(grid, gp, v, field):
     """(spectral error, per-slot errors) of variable v against the oracle run on that variable alone."""
+    import os
+
+    O.set_threads(os.cpu_count() or 1)  # every host core (the OpenMP default can be one thread under torch)
     g1 = _one_var_params(gp)
     o = O.OracleGrid(g1.to_abi())
     ph = np.zeros(o.physical_shape, order="F")
@@ -70,11 +73,12 @@ def test_rlz200_kz32_5var_f64_full_size_parity():
     grid.close()
 
 
-# FP32 bulk with an FP64 factor and one FP64 refinement step: binary32 storage
-# bounds f near 1e-7; the derivative slots amplify the binary32 rounding of the
-# ring and column transforms (∂λ by k up to 1200, ∂λλ by k², ∂z by the Chebyshev
-# recurrence), and the N(0, 1e-2) noise puts energy up to the highest modes.
-F32_BOUNDS = np.array([2e-6, 2e-4, 2e-3, 2e-4, 2e-3, 2e-4, 2e-3])
+# FP32 bulk with the FP64-refined spline solve: binary32 storage bounds f near
+# 1e-7; the derivative slots amplify the binary32 rounding of the ring and
+# column transforms.  Measured on GB300 (variables 1 and 8): f 3-5e-7, ∂r
+# 2-4e-6, ∂rr 4-5e-6, ∂λ 1.5-1.8e-6, ∂λλ 3-4e-6, ∂z and ∂zz 4-6e-7; the
+# bounds leave about 10x headroom.
+F32_BOUNDS = np.array([2e-6, 5e-5, 5e-5, 5e-5, 5e-5, 5e-6, 5e-6])
 
 
 def test_rlz400_kz64_8var_f32_per_variable_errors():
