@@ -206,6 +206,20 @@ int32_t ss_grid_clear_ahat(ss_grid *grid);
 
 int32_t ss_grid_synchronize(ss_grid *grid);
 
+/* regularGridTransform(grid, r_pts, λ_pts[, z_pts]) (src/transforms_cylindrical.jl:929-1020
+ * RL, 1168-1287 RLZ): the device-resident spectral array evaluated on the tensor
+ * product of n_r radii, n_lam azimuths and (RLZ) n_z levels: per wavenumber (and
+ * Chebyshev mode) SAtransform! of the spectral block, SI / SIx / SIxx at r, the
+ * Fourier series at λ with the R2HC factor 2 for k ≥ 1, and for RLZ CAtransform!
+ * plus the Chebyshev series at z.  Computed in FP64 for every precision; `out`
+ * is a host array of n_r·n_lam·n_z rows (r outer, λ then z inner) × nvars × 5 (RL)
+ * or 7 (RLZ) slots, column-major like grid.physical.  z_pts is ignored for RL.
+ * No R3X background (ahat) is applied: the reference runs SAtransform! on the
+ * grid's spline objects, whose ahat is zero unless multipatch coupling set it.
+ * Returns once `out` holds the result. */
+int32_t ss_regular_grid_transform(ss_grid *grid, const double *r_pts, int32_t n_r, const double *lam_pts,
+                                  int32_t n_lam, const double *z_pts, int32_t n_z, double *out, void *stream);
+
 /* ---- stage timing (the library's own instrumentation; no reference
  * counterpart: the reference times whole calls with BenchmarkTools,
  * bench/bench_grids.jl:20-38).  With profiling on, CUDA events bracket every

@@ -576,3 +576,28 @@ int64_t PlanSet::unpack_for(int L, TwiddlePool &pool) {
 }
 
 }  // namespace ss
+
+namespace ss {
+// SI / SIx / SIxx weights at arbitrary radii (SItransform(sp, a, points, u, d),
+// src/CubicBSpline.jl:1554-1567, 1650-1654, 1695-1699): the 4-coefficient window
+// m0[i] of point x[i] and the basis values w[(d·n + i)·4 + tap]
+int32_t spline_point_weights(const SplineHost &s, const double *x, int n, std::vector<int> &m0,
+                             std::vector<double> &w) {
+    const int Md = s.bDim, nc = s.nc;
+    m0.assign(n, 0);
+    w.assign(size_t(3) * n * 4, 0.0);
+    for (int i = 0; i < n; i++) {
+        const long xm = (long)std::ceil((x[i] - s.xmin - (2.0 * s.DX)) * s.DXrecip);
+        const int base = std::min(std::max(int(xm) + 1, 0), Md - 4);
+        m0[i] = base;
+        for (int q = 0; q < 4; q++) {
+            const long m = xm + q;
+            if (m < -1 || m > nc + 1) continue;
+            const int idx = int(m + 1) - base;
+            if (idx < 0 || idx > 3) continue;  // a point outside [xmin, xmax]: the terms the window cannot hold
+            for (int d = 0; d < 3; d++) w[(size_t(d) * n + i) * 4 + idx] = bspline(s, int(m), x[i], d);
+        }
+    }
+    return SS_OK;
+}
+}  // namespace ss
