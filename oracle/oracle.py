@@ -423,3 +423,115 @@ class OracleElliptic:
         if getattr(self, "h", None):
             lib().or_elliptic_destroy(self.h)
             self.h = None
+
+
+# ---------------------------------------------------------------- regular-grid output
+def _bc_tuple(arr, v):
+    if not arr:
+        return (0, 0.0, 0.0)
+    return (int(arr[v].kind), float(arr[v].alpha), float(arr[v].beta))
+
+
+def _grid_splines(p):
+    """One Spline1D per variable, the grid's radial template (src/factory.jl:667-680)."""
+    out = []
+    for v in range(p.nvars):
+        lq = float(p.l_q[v]) if p.l_q else 2.0
+        out.append(OracleSpline(p.iMin, p.iMax, p.num_cells, p.mubar, p.quadrature, lq,
+                                _bc_tuple(p.BCL, v), _bc_tuple(p.BCR, v)))
+    return out
+
+
+def _fourier_sums(sv, lam, kdim):
+    """Σ over wavenumbers at arbitrary λ of coefficient rows sv[..., 2K+1]
+    (slot 0: k = 0, 2k−1: cos k, 2k: sin k) with the R2HC half-amplitude factor 2
+    (src/transforms_cylindrical.jl:978-1005): returns f, ∂λ f, ∂λλ f."""
+    k = np.arange(1, kdim + 1, dtype=np.float64)
+    ang = np.outer(lam, k)  # k·λ
+    c, s = np.cos(ang), np.sin(ang)
+    rc, rs = sv[..., 1::2], sv[..., 2::2]
+    f = sv[..., :1] + 2.0 * (rc @ c.T + rs @ s.T)
+    fl = 2.0 * ((-rc * k) @ s.T + (rs * k) @ c.T)
+    fll = -2.0 * ((rc * k * k) @ c.T + (rs * k * k) @ s.T)
+    return f, fl, fll
+
+
+def _cheb_point_matrices(N, zmin, zmax, z):
+    """Value, ∂z and ∂zz of the DCT-I series at arbitrary z as matrices acting on the
+    Chebyshev A-coefficients (_cheb_eval_pts!, _cheb_dz_pts!, _cheb_dzz_pts!,
+    src/transforms_cylindrical.jl:1030-1094), clamps included."""
+    scale, offset = -0.5 * (zmax - zmin), 0.5 * (zmin + zmax)
+    m = np.arange(N, dtype=np.float64)
+    xi0 = np.clip((z - offset) / scale, -1.0 + 1e-14, 1.0 - 1e-14)
+    t0 = np.arccos(xi0)
+    E = 2.0 * np.cos(np.outer(t0, m))
+    E[:, 0] = 1.0
+    E[:, N - 1] = np.cos((N - 1) * t0)
+    xi = np.clip((z - offset) / scale, -1.0 + 1e-10, 1.0 - 1e-10)
+    t = np.arccos(xi)
+    st, ct = np.sin(t), np.cos(t)
+    D1 = -2.0 * m * np.sin(np.outer(t, m))          # df/dt coefficients
+    D1[:, 0] = 0.0
+    D1[:, N - 1] = -(N - 1) * np.sin((N - 1) * t)
+    D2 = -2.0 * m * m * np.cos(np.outer(t, m))      # d²f/dt² coefficients
+    D2[:, 0] = 0.0
+    D2[:, N - 1] = -(N - 1) ** 2 * np.cos((N - 1) * t)
+    Dz = D1 / (-scale * st)[:, None]
+    Dzz = (D2 * st[:, None] - D1 * ct[:, None]) / (scale ** 2 * st ** 3)[:, None]
+    return E, Dz, Dzz
+
+
+def regular_grid_transform(params, spectral, r_pts, lam_pts, z_pts=None):
+    """regularGridTransform (src/transforms_cylindrical.jl:929-1020 RL, 1168-1287 RLZ):
+    per wavenumber (and Chebyshev mode) SAtransform! of the spectral block, SI / SIx /
+    SIxx at r_pts, the Fourier series at lam_pts, and for RLZ CAtransform! plus the
+    Chebyshev series at z_pts.  Rows: r outer, λ (then z) inner; slots f, ∂r, ∂rr,
+    ∂λ, ∂λλ (, ∂z, ∂zz).  `params` is an abi.ParamBundle."""
+    p = params.params
+    r = np.asarray(r_pts, np.float64)
+    lam = np.asarray(lam_pts, np.float64)
+    nc, mubar = p.num_cells, p.mubar
+    b = nc + 3
+    kdim = nc * mubar + p.patchOffsetL
+    nslot = 1 + 2 * kdim
+    splines = _grid_splines(p)
+    spec = np.asarray(spectral, np.float64)
+    if p.geometry == abi.SS_GEOM_RL:
+        out = np.zeros((len(r) * len(lam), p.nvars, 5))
+        for v, sp in enumerate(splines):
+            sv = np.zeros((3, len(r), nslot))
+            for q in range(nslot):  # blocks: k0, then cos k / sin k at 2k−1, 2k
+                a = sp.sa(spec[q * b:(q + 1) * b, v])
+                for d in range(3):
+                    sv[d, :, q] = sp.si(a, d, r)
+            f, fl, fll = _fourier_sums(sv[0], lam, kdim)
+            fr = _fourier_sums(sv[1], lam, kdim)[0]
+            frr = _fourier_sums(sv[2], lam, kdim)[0]
+            for s, arr in enumerate((f, fr, frr, fl, fll)):
+                out[:, v, s] = arr.reshape(-1)
+        return out
+    z = np.asarray(z_pts, np.float64)
+    N = p.kDim
+    bk = p.b_kDim if p.b_kDim > 0 else min(N, (2 * N - 1) // 3 + 1)
+    out = np.zeros((len(r) * len(lam) * len(z), p.nvars, 7))
+    E, Dz, Dzz = _cheb_point_matrices(N, p.kMin, p.kMax, z)
+    for v, sp in enumerate(splines):
+        bcb = int(p.BCB[v]) if p.BCB else 0
+        bct = int(p.BCT[v]) if p.BCT else 0
+        CA = np.column_stack([cheb_ca(np.eye(bk)[i], N, bcb, bct) for i in range(bk)])  # N × bk
+        sv = np.zeros((3, len(r), bk, nslot))
+        for zb in range(bk):
+            base = zb * b * nslot
+            for q in range(nslot):
+                a = sp.sa(spec[base + q * b:base + (q + 1) * b, v])
+                for d in range(3):
+                    sv[d, :, zb, q] = sp.si(a, d, r)
+        f, fl, fll = _fourier_sums(sv[0], lam, kdim)       # (n_r, bk, n_λ)
+        fr = _fourier_sums(sv[1], lam, kdim)[0]
+        frr = _fourier_sums(sv[2], lam, kdim)[0]
+        for slot, arr, mats in ((0, f, (E, Dz, Dzz)), (1, fr, (E,)), (2, frr, (E,)), (3, fl, (E,)), (4, fll, (E,))):
+            coef = np.einsum("nk,rkl->rln", CA, arr)         # CAtransform! per (r, λ) column
+            for i, M in enumerate(mats):
+                s = slot if i == 0 else 4 + i
+                out[:, v, s] = np.einsum("zn,rln->rlz", M, coef).reshape(-1)
+    return out

@@ -1401,7 +1401,7 @@ int32_t or_grid_transform(or_grid *g, const double *spec, double *phys) {
 }
 
 /* ======================================================================
- * RL multi-patch chain (src/multipatch.jl)
+ * RL / RLZ multi-patch chain (src/multipatch.jl)
  * ====================================================================== */
 
 typedef struct {
@@ -1438,8 +1438,9 @@ int32_t or_chain_create(or_grid **grids, int32_t n, or_chain **out) {
     *out = NULL;
     if (n < 2) { set_err("PatchChain requires at least 2 grids, got %d", n); return SS_BAD_ARG; }
     for (int k = 0; k < n; k++)
-        if (grids[k]->geom != SS_GEOM_RL || grids[k]->nvars != grids[0]->nvars) {
-            set_err("the chain supports RL patches with equal variable counts");
+        if (grids[k]->geom != grids[0]->geom || grids[k]->nvars != grids[0]->nvars ||
+            (grids[0]->geom == SS_GEOM_RLZ && grids[k]->bk != grids[0]->bk)) {
+            set_err("the chain supports RL or RLZ patches with equal variable counts (and Chebyshev modes)");
             return SS_BAD_ARG;
         }
     or_chain *c = (or_chain *)calloc(1, sizeof *c);
@@ -1492,29 +1493,32 @@ void or_chain_destroy(or_chain *c) {
     free(c->state); free(c->layer_of); free(c->ifs); free(c->g); free(c);
 }
 
-/* _rl_kernel! (src/multipatch.jl:417-478): SA of each primary wavenumber slot,
- * 3 interface coefficients × coupling matrix, written into the secondary
- * spline object's ahat (k0 / real / imag objects are shared by all
- * wavenumbers) and the whole ahat vector copied into the per-wavenumber
- * registry (src/multipatch_registry.jl:45-62). */
+/* _rl_kernel! (src/multipatch.jl:417-478) and _rlz_kernel! (:496-571): SA of
+ * each primary wavenumber slot (RLZ: of every Chebyshev level z_b, blocks
+ * z_b·(1+2K) + q), 3 interface coefficients × coupling matrix, written into
+ * the secondary spline object's ahat (the k0 / real / imag objects are shared
+ * by all wavenumbers and levels) and the whole ahat vector copied into the
+ * per-wavenumber registry slot (src/multipatch_registry.jl:45-62). */
 static void chain_update_interface(or_chain *c, const or_iface *f, const double *spec_p) {
     or_grid *P = c->g[f->primary], *S = c->g[f->secondary];
     int bp = P->b, bs = S->b;
     int Kp = P->K, Ks = S->K, Kc = Kp < Ks ? Kp : Ks;
+    int nz = P->geom == SS_GEOM_RLZ ? P->bk : 1;
     double *a = (double *)malloc(sizeof(double) * (size_t)bp);
     double *t = (double *)malloc(sizeof(double) * 3 * (size_t)bp);
     for (int v = 0; v < S->nvars; v++) {
         const double *sp = spec_p + (size_t)P->nspec * v;
-        for (int q = 0; q <= 2 * Kc; q++) {
-            /* q: 0 = k0, odd = real k=(q+1)/2, even = imag */
-            int obj = (q == 0) ? 0 : ((q & 1) ? 1 : 2);
-            spline_sa(P->spl[v], sp + (size_t)q * bp, NULL, a, t, t + bp, t + 2 * bp);
-            double ex[3] = {a[f->node[0]], a[f->node[1]], a[f->node[2]]};
-            double *st = c->state[f->secondary] + ((size_t)v * 3 + obj) * bs;
-            double *dst = (f->sside == 0) ? st : st + bs - 3;
-            for (int r = 0; r < 3; r++) dst[r] = f->C[r * 3] * ex[0] + f->C[r * 3 + 1] * ex[1] + f->C[r * 3 + 2] * ex[2];
-            or_grid_set_ahat(S, v, q, st);
-        }
+        for (int zb = 0; zb < nz; zb++)
+            for (int q = 0; q <= 2 * Kc; q++) {
+                /* q: 0 = k0, odd = real k=(q+1)/2, even = imag */
+                int obj = (q == 0) ? 0 : ((q & 1) ? 1 : 2);
+                spline_sa(P->spl[v], sp + ((size_t)zb * (1 + 2 * Kp) + q) * bp, NULL, a, t, t + bp, t + 2 * bp);
+                double ex[3] = {a[f->node[0]], a[f->node[1]], a[f->node[2]]};
+                double *st = c->state[f->secondary] + ((size_t)v * 3 + obj) * bs;
+                double *dst = (f->sside == 0) ? st : st + bs - 3;
+                for (int r = 0; r < 3; r++) dst[r] = f->C[r * 3] * ex[0] + f->C[r * 3 + 1] * ex[1] + f->C[r * 3 + 2] * ex[2];
+                or_grid_set_ahat(S, v, zb * (1 + 2 * Ks) + q, st);
+            }
     }
     free(a); free(t);
 }

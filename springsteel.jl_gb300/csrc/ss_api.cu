@@ -177,14 +177,7 @@ static int32_t build_grid(ss_grid *g) {
         for (size_t i = 0; i < dinvf.size(); i++) dinvf[i] = (float)dinv[i];
         if ((st = upload_vec(g, &sd.L4f, l4f))) return st;
         if ((st = upload_vec(g, &sd.dinvf, dinvf))) return st;
-        {
-            std::vector<float2> ab(sh.Aopen.size());
-            for (size_t i = 0; i < ab.size(); i++) {
-                float h = (float)sh.Aopen[i];
-                ab[i] = make_float2(h, (float)(sh.Aopen[i] - (double)h));
-            }
-            if ((st = upload_vec(g, &sd.Aband_x, ab))) return st;
-        }
+        if ((st = upload_vec(g, &sd.Aband, sh.Aopen))) return st;
         if ((st = upload_bytes(g, &sd.sbw_t, real_layout(sh.sbw, g->tl)))) return st;
         if ((st = upload_bytes(g, &sd.siw_t, real_layout(sh.siw, g->tl)))) return st;
         if ((st = upload_vec(g, &sd.si_m0, sh.si_m0))) return st;
@@ -237,8 +230,10 @@ static int32_t build_grid(ss_grid *g) {
             // PhaseFilter(fp): cos(k*ymin), sin(k*ymin) with ymin = 0.5*(2π/L)*(ri-1)
             const double dl = 2 * 3.14159265358979323846 / rd.L;
             const double ymin = 0.5 * dl * (ri - 1);
+            // cos/sin(k ymin) for every k ≤ ri, whatever this set's kmax: a CTA's
+            // items (variables of an RL grid) index one ring set's table
             rd.phase = (int64_t)phase.size() / 2;
-            for (int k = 1; k <= kmax; k++) {
+            for (int k = 1; k <= ri; k++) {
                 phase.push_back(std::cos(k * ymin));
                 phase.push_back(std::sin(k * ymin));
             }

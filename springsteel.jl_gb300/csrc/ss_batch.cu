@@ -223,8 +223,9 @@ extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **
     if (!out || !grids || n < 2) { set_error("PatchChain requires at least 2 grids, got %d", n); return SS_BAD_ARG; }
     *out = nullptr;
     for (int i = 0; i < n; i++) {
-        if (!grids[i] || grids[i]->rlz || grids[i]->d.nvars != grids[0]->d.nvars) {
-            set_error("the chain supports RL patches with equal variable counts");
+        if (!grids[i] || grids[i]->rlz != grids[0]->rlz || grids[i]->d.nvars != grids[0]->d.nvars ||
+            grids[i]->d.b_kDim != grids[0]->d.b_kDim) {
+            set_error("the chain supports RL or RLZ patches with equal variable counts (and Chebyshev modes)");
             return SS_BAD_ARG;
         }
     }
@@ -280,7 +281,7 @@ extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **
         if (cudaMalloc(&c->state[i], bytes) != cudaSuccess) { cudaGetLastError(); set_error("out of device memory"); return SS_OUT_OF_MEMORY; }
         cudaMemset(c->state[i], 0, bytes);
     }
-    c->coupled_len = (size_t)nv * maxq * 3;
+    c->coupled_len = (size_t)nv * grids[0]->d.b_kDim * maxq * 3;
     if (cudaMalloc(&c->coupled, c->coupled_len * sizeof(double)) != cudaSuccess) {
         cudaGetLastError();
         set_error("out of device memory");
@@ -318,6 +319,8 @@ extern "C" int32_t ss_chain_destroy(ss_chain *c) {
 }
 
 // update_interface! for an RL secondary (_rl_kernel!, src/multipatch.jl:417-478)
+// or an RLZ one (_rlz_kernel!, :496-571: every Chebyshev level z_b, primary
+// blocks z_b·(1+2K_p) + q, registry blocks z_b·(1+2K_s) + q)
 static int32_t update_interface(ss_chain *c, const IfaceDev &f, cudaStream_t st) {
     ss_grid *P = c->g[f.primary], *S = c->g[f.secondary];
     ChainLaunch L{};
@@ -333,6 +336,9 @@ static int32_t update_interface(ss_chain *c, const IfaceDev &f, cudaStream_t st)
     L.ld = (L.b_p % 2) ? L.b_p : L.b_p + 1;
     L.nq = 1 + 2 * (int)std::min(P->d.kDim_wn, S->d.kDim_wn);
     L.nvars = (int)P->d.nvars;
+    L.bk = (int)P->d.b_kDim;  // 1 for RL
+    L.zblk_p = 1 + 2 * (int)P->d.kDim_wn;
+    L.zblk_s = 1 + 2 * (int)S->d.kDim_wn;
     L.side = f.sside;
     for (int i = 0; i < 3; i++) L.node[i] = f.node[i];
     std::memcpy(L.C, f.C, sizeof L.C);

@@ -1,4 +1,4 @@
-// ss_fft.cuh — CTA-cooperative complex DFT in shared memory for sm_103a.
+// ss_fft.cuh — CTA-cooperative complex DFTs in shared memory for sm_103a.
 //
 // The ring transforms of the reference call FFTW's R2HC/HC2R on rings of
 // L = 4+4ri points (src/Fourier.jl:192-193, 388-395, 463-468).  Ring lengths
@@ -11,9 +11,13 @@
 // M >= 2N-1.  Twiddles and index tables come from FP64-accurate tables built
 // on the host (ss_setup.cpp), stored in the compute type's layout.
 //
-// Every routine transforms a batch of `nb` independent sequences of the same
-// plan, `bs` complex entries apart in shared memory: one barrier per pass
-// serves the whole batch, and every thread loops over (sequence, index) pairs.
+// Every routine transforms `ns` sequences of the same plan, `ss` complex
+// entries apart in shared memory, with one barrier per pass for all of them.
+// A work unit is one butterfly position of a group of IT sequences: the
+// butterfly's index arithmetic and twiddles are computed once and applied to
+// the IT sequences, and the CTA's threads walk the units (position fastest, so
+// a warp touches consecutive shared-memory entries) without a division per
+// unit.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -87,36 +91,79 @@ __device__ __forceinline__ int div_small(int j, int d, float inv_d) {
     return q;
 }
 
-// One Stockham pass over the batch: Ns = product of the radices already applied.
+// Work units (n, g), n < Nn, spread over the CTA's threads: unit
+// threadIdx.x + i·blockDim.x in (n fastest) order, advanced by adding
+// blockDim.x with one carry instead of a division per unit:
+//   for (UnitWalk u(Nn); u.g < G; u.next()) { ... u.n, u.g ... }
+struct UnitWalk {
+    int n, g, dq, dm, Nn;
+    __device__ __forceinline__ explicit UnitWalk(int Nn_) : Nn(Nn_) {
+        const int T = blockDim.x;
+        const float inv = __frcp_rn((float)Nn);  // div_small corrects the estimate: exact quotients
+        dq = div_small(T, Nn, inv);
+        dm = T - dq * Nn;
+        g = div_small(threadIdx.x, Nn, inv);
+        n = threadIdx.x - g * Nn;
+    }
+    __device__ __forceinline__ void next() {
+        n += dm;
+        g += dq;
+        if (n >= Nn) {
+            n -= Nn;
+            g++;
+        }
+    }
+};
+
+// Sequences a work unit of a radix-R pass carries.  One: the ring kernels are
+// bound by latency and barrier waits, not by instruction issue, so a pass
+// needs as many independent units per barrier as possible (measured on GB300:
+// four sequences per unit at half the occupancy ran ring_inverse 15% slower).
+template <int R, typename T>
+constexpr int kUnitSeqs = 1;
+
+// One Stockham pass over ns sequences: Ns = product of the radices already applied.
 template <int R, int SIGN, typename T>
 __device__ __forceinline__ void stockham_pass(const cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N,
-                                              int Ns, const void *__restrict__ tw, int nb, int bs) {
+                                              int Ns, const void *__restrict__ tw, int ns, int ss) {
+    constexpr int IT = kUnitSeqs<R, T>;
     const int NR = N / R;
     const int tstride = N / (Ns * R);
-    const int total = nb * NR;
     const float inv_ns = 1.0f / (float)Ns;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int bi = nb == 1 ? 0 : t / NR, j = t - bi * NR;  // no division for a single sequence
-        const cpx<T> *s = src + (size_t)bi * bs;
-        cpx<T> *d = dst + (size_t)bi * bs;
+    const int G = (ns + IT - 1) / IT;
+    for (UnitWalk uw_(NR); uw_.g < (G); uw_.next()) {
+        const int j = uw_.n, g = uw_.g;
         const int jq = div_small(j, Ns, inv_ns);
         const int k = j - jq * Ns;
-        cpx<T> v[R];
+        cpx<T> w[R];  // every entry set: a partly uninitialised array is placed in local memory
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = s[j + r * NR];
+        for (int r = 0; r < R; r++) w[r] = {T(1.0f), T(0.0f)};
         if (k > 0) {
             const int step = tstride * k;
 #pragma unroll
             for (int r = 1; r < R; r++) {
-                cpx<T> w = ld_cplx<T>(tw, (int64_t)r * step);
-                if (SIGN > 0) w.y = -w.y;
-                v[r] = c_mul(v[r], w);
+                w[r] = ld_cplx<T>(tw, (int64_t)r * step);
+                if (SIGN > 0) w[r].y = -w[r].y;
             }
         }
-        dft_small<R, SIGN>(v);
         const int idxD = jq * Ns * R + k;
 #pragma unroll
-        for (int r = 0; r < R; r++) d[idxD + r * Ns] = v[r];
+        for (int t = 0; t < IT; t++) {
+            const int sq = g * IT + t;
+            if (sq >= ns) break;
+            const cpx<T> *s = src + (size_t)sq * ss + j;
+            cpx<T> *d = dst + (size_t)sq * ss + idxD;
+            cpx<T> v[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) v[r] = s[r * NR];
+            if (k > 0) {
+#pragma unroll
+                for (int r = 1; r < R; r++) v[r] = c_mul(v[r], w[r]);
+            }
+            dft_small<R, SIGN>(v);
+#pragma unroll
+            for (int r = 0; r < R; r++) d[r * Ns] = v[r];
+        }
     }
 }
 
@@ -125,93 +172,123 @@ __device__ __forceinline__ const void *tab_at(const void *pool, int64_t off) {
     return (const void *)((const typename Tab<T>::cplx_t *)pool + off);
 }
 
-// Radix-R pass for an odd prime R > 13 (up to kMaxPrimeRadix).  A first
-// sweep twiddles each butterfly's inputs (skipped when Ns = 1) and replaces
-// them in place by the pairs a_q = v_q + v_{R−q} (at q) and b_q = v_q − v_{R−q}
-// (at R−q), q = 1..(R−1)/2; then each work item computes kPrimeGroup conjugate
-// output pairs (s, R−s) of one butterfly:
+// Radix-R pass for an odd prime R > 13 (up to the plan set's direct limit).  A
+// first sweep twiddles each butterfly's inputs (skipped when Ns = 1) and
+// replaces them in place by the pairs a_q = v_q + v_{R−q} (at q) and
+// b_q = v_q − v_{R−q} (at R−q), q = 1..(R−1)/2; then each work unit computes
+// S conjugate output pairs (s, R−s) of one butterfly for IT sequences:
 //   re = v_0 + Σ_q a_q cos(2πqs/R),  im = Σ_q b_q sin(2πqs/R),
 //   X_s = re ∓ i·im, X_{R−s} = re ± i·im  (upper signs forward), X_0 = v_0 + Σ a_q.
-// cos/sin(2πe/R) are the N-point twiddles at e·N/R.  Four FMAs per term and
-// output pair instead of a length ≥ 2N−1 chirp-z convolution; each a_q, b_q
-// load from shared memory serves all of the item's pairs.
-template <typename T> constexpr int kPrimeGroup = sizeof(T) == 4 ? 2 : 4;  // output pairs per work item of a prime pass
+// cos/sin(2πe/R) are the N-point twiddles at e·N/R.  Every a_q, b_q load feeds S
+// output pairs and every twiddle load IT sequences: an S × IT register tile of
+// the R × R DFT matrix product.
+template <typename T> constexpr int kPrimeOut = sizeof(T) == 4 ? 2 : 4;  // output pairs per unit
+template <typename T> constexpr int kPrimeSeqs = 1;                      // sequences per unit
 template <int SIGN, typename T>
 __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N, int Ns, int R,
-                           const void *__restrict__ tw, int nb, int bs) {
+                           const void *__restrict__ tw, int ns, int ss) {
     const int NR = N / R, H = (R - 1) / 2;
     const int tstride = N / (Ns * R), rstep = N / R;
-    const float inv_ns = 1.0f / (float)Ns, inv_h = 1.0f / (float)H;
+    const float inv_ns = 1.0f / (float)Ns;
     {
-        const int per = NR * H;
-        for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
-            const int bi = nb == 1 ? 0 : t / per, rest = t - bi * per;
-            const int j = div_small(rest, H, inv_h), q = rest - j * H + 1;
-            cpx<T> *sv = src + (size_t)bi * bs + j;
-            cpx<T> vq = sv[q * NR], vr = sv[(R - q) * NR];
+        constexpr int IT = 1;
+        const int G = (ns + IT - 1) / IT;
+        const float inv_h = 1.0f / (float)H;
+        for (UnitWalk uw_(NR * H); uw_.g < (G); uw_.next()) {
+        const int u = uw_.n, g = uw_.g;
+            const int j = div_small(u, H, inv_h), q = u - j * H + 1;
+            cpx<T> w1 = {T(1.0f), T(0.0f)}, w2 = w1;
+            bool twd = false;
             if (Ns > 1) {
                 const int k = j - div_small(j, Ns, inv_ns) * Ns;
                 if (k > 0) {
-                    cpx<T> w1 = ld_cplx<T>(tw, (int64_t)q * k * tstride);
-                    cpx<T> w2 = ld_cplx<T>(tw, (int64_t)(R - q) * k * tstride);
+                    w1 = ld_cplx<T>(tw, (int64_t)q * k * tstride);
+                    w2 = ld_cplx<T>(tw, (int64_t)(R - q) * k * tstride);
                     if (SIGN > 0) { w1.y = -w1.y; w2.y = -w2.y; }
+                    twd = true;
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < IT; t++) {
+                const int sq = g * IT + t;
+                if (sq >= ns) break;
+                cpx<T> *sv = src + (size_t)sq * ss + j;
+                cpx<T> vq = sv[q * NR], vr = sv[(R - q) * NR];
+                if (twd) {
                     vq = c_mul(vq, w1);
                     vr = c_mul(vr, w2);
                 }
+                sv[q * NR] = c_add(vq, vr);
+                sv[(R - q) * NR] = c_sub(vq, vr);
             }
-            sv[q * NR] = c_add(vq, vr);
-            sv[(R - q) * NR] = c_sub(vq, vr);
         }
         __syncthreads();
     }
-    // each work item: S consecutive output pairs s = s0 .. s0+S−1 of one
-    // butterfly, so every a_q, b_q load feeds S pairs (s = 0 gives X_0 = v_0 + Σ a_q
-    // through the unit twiddle; entries with s > H are computed and dropped).
-    // S = 2 for binary32, whose ring kernels run at 64 registers per thread.
-    constexpr int S = kPrimeGroup<T>;
-    const int G = (H + 1 + S - 1) / S;
-    const int per = NR * G;
-    const float inv_g = 1.0f / (float)G;
-    for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
-        const int bi = nb == 1 ? 0 : t / per, rest = t - bi * per;
-        const int j = div_small(rest, G, inv_g), s0 = (rest - j * G) * S;
-        const cpx<T> *sv = src + (size_t)bi * bs + j;
-        cpx<T> *d = dst + (size_t)bi * bs;
+    // s = 0 gives X_0 = v_0 + Σ a_q through the unit twiddle; entries with s > H
+    // are computed and dropped
+    constexpr int S = kPrimeOut<T>, IT = kPrimeSeqs<T>;
+    const int Gs = (H + 1 + S - 1) / S;
+    const int G = (ns + IT - 1) / IT;
+    const float inv_gs = 1.0f / (float)Gs;
+    for (UnitWalk uw_(NR * Gs); uw_.g < (G); uw_.next()) {
+        const int u = uw_.n, g = uw_.g;
+        const int j = div_small(u, Gs, inv_gs), s0 = (u - j * Gs) * S;
         const int jq = div_small(j, Ns, inv_ns), k = j - jq * Ns;
         const int idxD = jq * Ns * R + k;
-        const cpx<T> x0 = sv[0];
-        cpx<T> re[S], im[S];
+        cpx<T> re[S][IT], im[S][IT];
         int e[S];
 #pragma unroll
-        for (int i = 0; i < S; i++) { re[i] = x0; im[i] = c_zero<T>(); e[i] = 0; }
+        for (int t = 0; t < IT; t++) {
+            const int sq = min(g * IT + t, ns - 1);  // a clamped duplicate is computed and not stored
+            const cpx<T> x0 = src[(size_t)sq * ss + j];
+#pragma unroll
+            for (int i = 0; i < S; i++) { re[i][t] = x0; im[i][t] = c_zero<T>(); }
+        }
+#pragma unroll
+        for (int i = 0; i < S; i++) e[i] = 0;
         for (int q = 1; q <= H; q++) {
-            const cpx<T> a = sv[q * NR], b = sv[(R - q) * NR];
+            cpx<T> a[IT], b[IT];
+#pragma unroll
+            for (int t = 0; t < IT; t++) {
+                const cpx<T> *sv = src + (size_t)min(g * IT + t, ns - 1) * ss + j;
+                a[t] = sv[q * NR];
+                b[t] = sv[(R - q) * NR];
+            }
 #pragma unroll
             for (int i = 0; i < S; i++) {
                 e[i] += s0 + i;  // e = q·s mod R (s ≤ R − 1 keeps one subtraction enough)
                 if (e[i] >= R) e[i] -= R;
                 const cpx<T> w = ld_cplx<T>(tw, (int64_t)e[i] * rstep);  // (cos, −sin)(2πe/R)
-                re[i].x = re[i].x + a.x * w.x;
-                re[i].y = re[i].y + a.y * w.x;
-                im[i].x = im[i].x - b.x * w.y;
-                im[i].y = im[i].y - b.y * w.y;
+#pragma unroll
+                for (int t = 0; t < IT; t++) {
+                    re[i][t].x = re[i][t].x + a[t].x * w.x;
+                    re[i][t].y = re[i][t].y + a[t].y * w.x;
+                    im[i][t].x = im[i][t].x - b[t].x * w.y;
+                    im[i][t].y = im[i][t].y - b[t].y * w.y;
+                }
             }
         }
 #pragma unroll
-        for (int i = 0; i < S; i++) {
-            const int s = s0 + i;
-            if (s > H) break;
-            if (s == 0) {
-                d[idxD] = re[i];
-                continue;
-            }
-            const cpx<T> iim = {-im[i].y, im[i].x};
-            if (SIGN < 0) {
-                d[idxD + s * Ns] = c_sub(re[i], iim);
-                d[idxD + (R - s) * Ns] = c_add(re[i], iim);
-            } else {
-                d[idxD + s * Ns] = c_add(re[i], iim);
-                d[idxD + (R - s) * Ns] = c_sub(re[i], iim);
+        for (int t = 0; t < IT; t++) {
+            const int sq = g * IT + t;
+            if (sq >= ns) break;
+            cpx<T> *d = dst + (size_t)sq * ss + idxD;
+#pragma unroll
+            for (int i = 0; i < S; i++) {
+                const int s = s0 + i;
+                if (s > H) break;
+                if (s == 0) {
+                    d[0] = re[i][t];
+                    continue;
+                }
+                const cpx<T> iim = {-im[i][t].y, im[i][t].x};
+                if (SIGN < 0) {
+                    d[s * Ns] = c_sub(re[i][t], iim);
+                    d[(R - s) * Ns] = c_add(re[i][t], iim);
+                } else {
+                    d[s * Ns] = c_add(re[i][t], iim);
+                    d[(R - s) * Ns] = c_sub(re[i][t], iim);
+                }
             }
         }
     }
@@ -220,20 +297,20 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
 // Stockham passes rad[s_begin..nrad) over ping-pong buffers, Ns0 = product of the
 // radices already applied; returns the buffer holding the result.
 template <int SIGN, typename T>
-__device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int nb,
-                                  int bs, int s_begin = 0, int Ns0 = 1) {
+__device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int ns,
+                                  int ss, int s_begin = 0, int Ns0 = 1) {
     int Ns = Ns0;
     for (int s = s_begin; s < nrad; s++) {
         const int R = rad[s];
         switch (R) {
-        case 4: stockham_pass<4, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        case 2: stockham_pass<2, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        case 3: stockham_pass<3, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        case 5: stockham_pass<5, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        case 7: stockham_pass<7, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        case 11: stockham_pass<11, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        case 13: stockham_pass<13, SIGN>(a, b, N, Ns, tw, nb, bs); break;
-        default: prime_pass<SIGN, T>(a, b, N, Ns, R, tw, nb, bs); break;
+        case 4: stockham_pass<4, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        case 2: stockham_pass<2, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        case 3: stockham_pass<3, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        case 5: stockham_pass<5, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        case 7: stockham_pass<7, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        case 11: stockham_pass<11, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        case 13: stockham_pass<13, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        default: prime_pass<SIGN, T>(a, b, N, Ns, R, tw, ns, ss); break;
         }
         __syncthreads();
         cpx<T> *t = a;
@@ -245,59 +322,58 @@ __device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, i
 }
 
 // Radix-p pass by Rader's algorithm (p prime, first pass: Ns = 1, no input
-// twiddles).  Per butterfly j (NR = N/p of them):
-//   u_a = x_{g^a} (a < p−1) into dst[j(p−1) + a], x_0 into dst's tail dst[N + j];
+// twiddles) over `nb` sequences of length N, `ss` apart.  Per butterfly j
+// (NR = N/p of them) of sequence b:
+//   u_a = x_{g^a} (a < p−1) into dst[(b·NR + j)(p−1) + a] (every inner
+//   sequence p−1 apart), x_0 into dst[tail + b·NR + j];
 //   c = u ⊛ h by two (p−1)-point DFTs (inner plan) and H = DFT(h)/(p−1);
-//   X_0 = x_0 + DFT(u)_0 (kept in src's tail), X_{g^{−b}} = x_0 + c_b.
-// The inverse transform runs as conj(forward(conj x)).  The tails beyond the N
-// data entries are never touched by the inner passes.  Returns the buffer
-// holding the pass's outputs (either a or b).
+//   X_0 = x_0 + DFT(u)_0 (into src[tail + b·NR + j]), X_{g^{−b}} = x_0 + c_b.
+// The inverse transform runs as conj(forward(conj x)).  `tail` lies beyond
+// every sequence's N outputs, so the scatter never overwrites a tail entry it
+// still reads.  Returns the buffer holding the pass's outputs (either a or b).
 template <int SIGN, typename T>
-__device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl, const void *pool, int nb, int bs) {
+__device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl, const void *pool, int nb, int ss,
+                              int tail) {
     const int p = pl.rp, P1 = p - 1, NR = N / p;
-    const float inv_p = 1.0f / (float)p, inv_p1 = 1.0f / (float)P1;
+    const float inv_p = 1.0f / (float)p;
     const void *H = tab_at<T>(pool, pl.rH);
     const void *perm = tab_at<T>(pool, pl.rperm);  // (g^a, g^{−a}) mod p
-    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {  // gather: (j, a), a = p−1 → x_0
-        const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
+    for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
+        const int e = uw_.n, b = uw_.g;  // gather: (j, a), a = p−1 → x_0
         const int j = div_small(e, p, inv_p), a = e - j * p;
         const int q = a < P1 ? ld_index_pair<T>(perm, a).x : 0;
-        cpx<T> v = src[(size_t)bi * bs + j + q * NR];
+        cpx<T> v = src[(size_t)b * ss + j + q * NR];
         if (SIGN > 0) v.y = -v.y;
-        dst[(size_t)bi * bs + (a < P1 ? j * P1 + a : N + j)] = v;
+        dst[a < P1 ? (size_t)(b * NR + j) * P1 + a : (size_t)tail + b * NR + j] = v;
     }
     __syncthreads();
-    cpx<T> *r2 = dst;
-    for (int bi = 0; bi < nb; bi++) {  // inner cyclic convolutions of one item at a time
-        cpx<T> *d0 = dst + (size_t)bi * bs, *s0 = src + (size_t)bi * bs;
-        cpx<T> *r1 = stockham_plain<-1, T>(d0, s0, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), NR, P1);
-        for (int e = threadIdx.x; e < NR * P1; e += blockDim.x) {
-            const int j = div_small(e, P1, inv_p1), k = e - j * P1;
-            const cpx<T> U = r1[e];
-            if (k == 0) s0[N + j] = c_add(d0[N + j], U);  // X_0 into src's tail
-            r1[e] = c_mul(U, ld_cplx<T>(H, k));
-        }
-        __syncthreads();
-        cpx<T> *other = (r1 == d0) ? s0 : d0;
-        cpx<T> *rr = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), NR, P1);
-        r2 = (rr == d0) ? dst : src;  // same choice for every item
+    const int ni = nb * NR;  // inner sequences
+    cpx<T> *r1 = stockham_plain<-1, T>(dst, src, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1);
+    for (UnitWalk uw_(P1); uw_.g < (ni); uw_.next()) {
+        const int k = uw_.n, sq = uw_.g;
+        cpx<T> *u = r1 + (size_t)sq * P1 + k;
+        const cpx<T> U = *u;
+        if (k == 0) src[tail + sq] = c_add(dst[tail + sq], U);  // X_0 into src's tail
+        *u = c_mul(U, ld_cplx<T>(H, k));
     }
+    __syncthreads();
+    cpx<T> *other = (r1 == dst) ? src : dst;
+    cpx<T> *r2 = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1);
     cpx<T> *out = (r2 == dst) ? src : dst;
-    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {  // scatter: (j, b), b = p−1 → X_0
-        const int bi = nb == 1 ? 0 : t / N, e = t - bi * N;
-        const int j = div_small(e, p, inv_p), b = e - j * p;
-        const cpx<T> *rb = r2 + (size_t)bi * bs;
+    for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
+        const int e = uw_.n, b = uw_.g;  // scatter: (j, b'), b' = p−1 → X_0
+        const int j = div_small(e, p, inv_p), bb = e - j * p;
         cpx<T> X;
         int s;
-        if (b == P1) {
-            X = src[(size_t)bi * bs + N + j];
+        if (bb == P1) {
+            X = src[(size_t)tail + b * NR + j];
             s = 0;
         } else {
-            X = c_add(dst[(size_t)bi * bs + N + j], rb[j * P1 + b]);
-            s = ld_index_pair<T>(perm, b).y;
+            X = c_add(dst[(size_t)tail + b * NR + j], r2[(size_t)(b * NR + j) * P1 + bb]);
+            s = ld_index_pair<T>(perm, bb).y;
         }
         if (SIGN > 0) X.y = -X.y;
-        out[(size_t)bi * bs + j * p + s] = X;  // Ns = 1: butterfly j's outputs at j·p + s
+        out[(size_t)b * ss + j * p + s] = X;  // Ns = 1: butterfly j's outputs at j·p + s
     }
     __syncthreads();
     return out;
@@ -306,30 +382,37 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
 // A plan's Stockham DFT: the Rader pass first when the plan has one, then the
 // remaining radix passes; returns the buffer holding the result.
 template <int SIGN, typename T>
-__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int nb, int bs,
-                            const FftPlan *pl, const void *pool) {
+__device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int ns, int ss,
+                            const FftPlan *pl, const void *pool, int tail) {
     if (pl && pl->rp) {
-        cpx<T> *o = rader_pass<SIGN, T>(a, b, N, *pl, pool, nb, bs);
+        cpx<T> *o = rader_pass<SIGN, T>(a, b, N, *pl, pool, ns, ss, tail);
         if (o != a) { b = a; a = o; }
-        return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, nb, bs, 1, pl->rp);
+        return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, 1, pl->rp);
     }
-    return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, nb, bs);
+    return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss);
 }
 
-// Length-N DFTs of the nb sequences in `a` (sign SIGN), sequence i at a + i·bs.
-// Both buffers hold nb × fft_buffer_len(plan) entries (bs ≥ that length).
-// Returns the buffer with the results, laid out like the input.
+// Sequence stride of a plan inside a CTA's ping-pong buffers: N, or M for
+// Bluestein.  A buffer holds `cap` sequences (the CTA's item batch) and, for a
+// Rader plan, a tail of cap·N/p entries after them.
+__host__ __device__ inline int fft_seq_stride(const FftPlan &p) { return p.blu ? p.M : p.N; }
+
+// Length-N DFTs of the nb sequences in `a` (sign SIGN), sequence i at
+// a + i·fft_seq_stride(p).  Both buffers hold cap × fft_buffer_len(plan)
+// entries (cap ≥ nb).  Returns the buffer with the results, laid out like the
+// input.
 template <int SIGN, typename T>
-__device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool, int nb = 1, int bs = 0) {
-    if (!p.blu) return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw), nb, bs, &p, pool);
+__device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool, int nb, int cap) {
+    if (!p.blu)
+        return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw), nb, p.N, &p, pool, cap * p.N);
     const int N = p.N, M = p.M;
     const void *chirp = tab_at<T>(pool, p.chirp);
     const void *filt = tab_at<T>(pool, p.filt);
     // X_k = c_k Σ_j (x_j c_j) conj(c_{k-j}) with c_k = exp(-πi k²/N); the
     // inverse DFT is conj(forward(conj x)).
-    for (int t = threadIdx.x; t < nb * M; t += blockDim.x) {
-        const int bi = nb == 1 ? 0 : t / M, k = t - bi * M;
-        cpx<T> *ab = a + (size_t)bi * bs;
+    for (UnitWalk uw_(M); uw_.g < (nb); uw_.next()) {
+        const int k = uw_.n, bi = uw_.g;
+        cpx<T> *ab = a + (size_t)bi * M;
         cpx<T> v = c_zero<T>();
         if (k < N) {
             v = ab[k];
@@ -339,18 +422,18 @@ __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool,
         ab[k] = v;
     }
     __syncthreads();
-    cpx<T> *r = stockham_plain<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
-    for (int t = threadIdx.x; t < nb * M; t += blockDim.x) {
-        const int bi = nb == 1 ? 0 : t / M, k = t - bi * M;
-        cpx<T> *rb = r + (size_t)bi * bs;
+    cpx<T> *r = stockham_plain<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M);
+    for (UnitWalk uw_(M); uw_.g < (nb); uw_.next()) {
+        const int k = uw_.n, bi = uw_.g;
+        cpx<T> *rb = r + (size_t)bi * M;
         rb[k] = c_mul(rb[k], ld_cplx<T>(filt, k));
     }
     __syncthreads();
     cpx<T> *other = (r == a) ? b : a;
-    cpx<T> *q = stockham_plain<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, bs);
-    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
-        const int bi = nb == 1 ? 0 : t / N, k = t - bi * N;
-        cpx<T> *qb = q + (size_t)bi * bs;
+    cpx<T> *q = stockham_plain<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M);
+    for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
+        const int k = uw_.n, bi = uw_.g;
+        cpx<T> *qb = q + (size_t)bi * M;
         cpx<T> v = c_mul(qb[k], ld_cplx<T>(chirp, k));
         if (SIGN > 0) v.y = -v.y;
         qb[k] = v;

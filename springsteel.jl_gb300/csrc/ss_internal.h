@@ -85,7 +85,7 @@ struct SplineDev {
     double *PQb;        // bDim*7 full P+Q band (R3X only)
     float *L4f;         // FP32-rounded factor (FP32 mode)
     float *dinvf;
-    float2 *Aband_x;    // FP64 open-form Γ(P+Q)Γᵀ band as (hi, lo) pairs (FP32 refinement)
+    double *Aband;      // FP64 open-form Γ(P+Q)Γᵀ band, Aband[j*4+d] = A[j+d][j] (FP32 refinement residual)
     const void *sbw_t;  // bDim*(4 mubar) SB weights (row mi, tap), compute layout
     const void *siw_t;  // 3*mishDim*4 SI weights (derivative, point, tap), compute layout
     int *si_m0;         // mishDim: first coefficient index of the 4-tap window
@@ -137,6 +137,9 @@ struct ChebHost {
     std::vector<double> fwd, inv_e, inv_o, gu, gv, mish;
 };
 int32_t build_cheb(int N, int bk, int bcb, int bct, double zmin, double zmax, ChebHost &out);
+// SI weights at arbitrary radii: window start m0[i], w[(d·n + i)·4 + tap], d = 0, 1, 2
+int32_t spline_point_weights(const SplineHost &s, const double *x, int n, std::vector<int> &m0,
+                             std::vector<double> &w);
 
 // Pool of complex twiddles (interleaved re, im) in FP64.
 struct TwiddlePool {

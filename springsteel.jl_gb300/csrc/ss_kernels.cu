@@ -59,15 +59,18 @@ void fft_init_constants() {
     if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
-// Resident 256-thread CTAs the ring kernels are compiled for: binary32 butterflies
-// fit 64 registers (4 CTAs per SM); binary64 and double-float need more.
+// Resident 256-thread CTAs the ring kernels are compiled for: binary32
+// butterflies fit 64 registers (4 CTAs per SM); binary64 and double-float need more.
 template <typename T>
 constexpr int kRingMinBlocks = std::is_same<T, float>::value ? 4 : 2;
+// sequences per unit of the kernels' element-wise load / pack / store sweeps
+constexpr int kSweepSeqs = 1;
 
 // ====================================================================
 // ring_forward: one CTA per (ring, batch of up to L.ib items); item = v*bk + zb
 // (RLZ) or v (RL).  The items of a batch share the ring's plan and twiddles;
-// their sequences sit `buf` complex entries apart in each ping-pong buffer.
+// their sequences sit fft_seq_stride(plan) complex entries apart in each
+// ping-pong buffer (each buffer holds L.ib × fft_buffer_len(plan) entries).
 // ====================================================================
 template <typename P, typename T>
 __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(RingLaunch L) {
@@ -78,7 +81,7 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(Ri
     const int nb = min(L.ib, L.nitems - item0);
     const RingDesc rd = L.rings[(size_t)(L.rlz ? 0 : item0) * L.ring_var_stride + ring];
     const FftPlan &pl = L.plans[rd.plan];
-    const int buf = fft_buffer_len(pl);
+    const int buf = fft_buffer_len(pl), sq = fft_seq_stride(pl);
     cpx<T> *A = reinterpret_cast<cpx<T> *>(smem_raw);
     cpx<T> *B = A + (size_t)L.ib * buf;
     __shared__ int64_t ioff[kRingBatchMax];  // element offset of each item's ring in the input
@@ -91,51 +94,62 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(Ri
                                   : (int64_t)item * L.in_item_stride + rd.jofs;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
-        const int b = nb == 1 ? 0 : t / N, n = t - b * N;
+    for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
+        const int n = uw_.n, b = uw_.g;
         if (L.rlz) {
             const T *in = (const T *)L.in + ioff[b];
-            A[(size_t)b * buf + n] = {in[2 * n], in[2 * n + 1]};
+            A[(size_t)b * sq + n] = {in[2 * n], in[2 * n + 1]};
         } else {
             const P *in = (const P *)L.in + ioff[b];
-            A[(size_t)b * buf + n] = {to_compute<T>(in[2 * n]), to_compute<T>(in[2 * n + 1])};
+            A[(size_t)b * sq + n] = {to_compute<T>(in[2 * n]), to_compute<T>(in[2 * n + 1])};
         }
     }
     __syncthreads();
-    cpx<T> *Zb = dft<-1, T>(A, B, pl, L.pool, nb, buf);
+    cpx<T> *Zb = dft<-1, T>(A, B, pl, L.pool, nb, L.ib);
 
     const T invL = T(1.0f) / T((float)Lr);
     const int nk = rd.ri + 1;
-    for (int t = threadIdx.x; t < nb * nk; t += blockDim.x) {
-        const int b = nb == 1 ? 0 : t / nk, k = t - b * nk;
-        const cpx<T> *Z = Zb + (size_t)b * buf;
-        T *out = (T *)L.out + (size_t)(item0 + b) * L.frows + rd.fofs;
-        cpx<T> zk = Z[k];
-        cpx<T> zn = c_conj(Z[(N - k) % N]);
-        if (k == 0) {
-            out[0] = (zk.x + zk.y) * invL;
-            continue;
+    const int G = (nb + kSweepSeqs - 1) / kSweepSeqs;
+    for (UnitWalk uw_(nk); uw_.g < (G); uw_.next()) {
+        const int k = uw_.n, g = uw_.g;
+        cpx<T> uw = c_zero<T>(), cs = c_zero<T>();
+        if (k > 0) {
+            uw = ld_cplx<T>(L.pool, rd.utw + k);
+            cs = ld_cplx<T>(L.phase, rd.phase + (k - 1));
         }
-        T bre = T(0.0f), bim = T(0.0f);
-        if (k <= kmx[b]) {
-            cpx<T> e = {scale_f(zk.x + zn.x, 0.5f), scale_f(zk.y + zn.y, 0.5f)};
-            cpx<T> d = {scale_f(zk.x - zn.x, 0.5f), scale_f(zk.y - zn.y, 0.5f)};
-            cpx<T> o = {d.y, -d.x};  // d / i
-            cpx<T> X = c_add(e, c_mul(ld_cplx<T>(L.pool, rd.utw + k), o));
-            T re = X.x * invL, im = X.y * invL;
-            cpx<T> cs = ld_cplx<T>(L.phase, rd.phase + (k - 1));
-            bre = cs.x * re + cs.y * im;
-            bim = -(cs.y * re) + cs.x * im;
+#pragma unroll
+        for (int t = 0; t < kSweepSeqs; t++) {
+            const int b = g * kSweepSeqs + t;
+            if (b >= nb) break;
+            const cpx<T> *Z = Zb + (size_t)b * sq;
+            T *out = (T *)L.out + (size_t)(item0 + b) * L.frows + rd.fofs;
+            const cpx<T> zk = Z[k];
+            const cpx<T> zn = c_conj(Z[(N - k) % N]);
+            if (k == 0) {
+                out[0] = (zk.x + zk.y) * invL;
+                continue;
+            }
+            T bre = T(0.0f), bim = T(0.0f);
+            if (k <= kmx[b]) {
+                cpx<T> e = {scale_f(zk.x + zn.x, 0.5f), scale_f(zk.y + zn.y, 0.5f)};
+                cpx<T> d = {scale_f(zk.x - zn.x, 0.5f), scale_f(zk.y - zn.y, 0.5f)};
+                cpx<T> o = {d.y, -d.x};  // d / i
+                cpx<T> X = c_add(e, c_mul(uw, o));
+                T re = X.x * invL, im = X.y * invL;
+                bre = cs.x * re + cs.y * im;
+                bim = -(cs.y * re) + cs.x * im;
+            }
+            out[2 * k - 1] = bre;
+            out[2 * k] = bim;
         }
-        out[2 * k - 1] = bre;
-        out[2 * k] = bim;
     }
 }
 
 // ====================================================================
-// ring_inverse: one CTA per (ring, item).  For d = 0 (value), 1 (∂r), 2 (∂rr)
-// read the ring's coefficient row, undo the phase rotation (FAtransform!),
-// and run HC2R for the variants: d=0 → f, ∂λ, ∂λλ; d=1 → ∂r; d=2 → ∂rr.
+// ring_inverse: one CTA per (ring, batch of items).  For d = 0 (value), 1 (∂r),
+// 2 (∂rr) read the ring's coefficient rows, undo the phase rotation
+// (FAtransform!), and run HC2R for the variants: d=0 → f, ∂λ, ∂λλ; d=1 → ∂r;
+// d=2 → ∂rr.
 // ====================================================================
 template <typename P, typename T>
 __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(RingLaunch L) {
@@ -146,7 +160,7 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(Ri
     const int nb = min(L.ib, L.nitems - item0);
     const RingDesc rd = L.rings[(size_t)(L.rlz ? 0 : item0) * L.ring_var_stride + ring];
     const FftPlan &pl = L.plans[rd.plan];
-    const int buf = fft_buffer_len(pl);
+    const int buf = fft_buffer_len(pl), sq = fft_seq_stride(pl);
     const int nk = rd.ri + 1;  // Xs stride: kmax ≤ ri
     cpx<T> *A = reinterpret_cast<cpx<T> *>(smem_raw);
     cpx<T> *B = A + (size_t)L.ib * buf;
@@ -162,59 +176,69 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(Ri
                                   : (int64_t)item * L.np + rd.jofs;
     }
     __syncthreads();
+    const int G = (nb + kSweepSeqs - 1) / kSweepSeqs;
 
     for (int d = 0; d < 3; d++) {
         // FAtransform!: a_re = c br - s bi, a_im = s br + c bi (phase_filter.jl:154-190)
-        for (int t = threadIdx.x; t < nb * nk; t += blockDim.x) {
-            const int b = nb == 1 ? 0 : t / nk, k = t - b * nk;
-            if (k > kmx[b]) continue;
-            const T *g = (const T *)L.in + ((size_t)d * L.nitems + item0 + b) * L.frows + rd.fofs;
-            cpx<T> *X = Xs + (size_t)b * nk;
-            if (k == 0) {
-                X[0] = {g[0], T(0.0f)};
-            } else {
-                T br = g[2 * k - 1], bi = g[2 * k];
-                cpx<T> cs = ld_cplx<T>(L.phase, rd.phase + (k - 1));
-                X[k] = {cs.x * br - cs.y * bi, cs.y * br + cs.x * bi};
+        for (UnitWalk uw_(nk); uw_.g < (G); uw_.next()) {
+        const int k = uw_.n, g = uw_.g;
+            const cpx<T> cs = k > 0 ? ld_cplx<T>(L.phase, rd.phase + (k - 1)) : c_zero<T>();
+#pragma unroll
+            for (int t = 0; t < kSweepSeqs; t++) {
+                const int b = g * kSweepSeqs + t;
+                if (b >= nb) break;
+                if (k > kmx[b]) continue;
+                const T *gr = (const T *)L.in + ((size_t)d * L.nitems + item0 + b) * L.frows + rd.fofs;
+                cpx<T> *X = Xs + (size_t)b * nk;
+                if (k == 0) {
+                    X[0] = {gr[0], T(0.0f)};
+                } else {
+                    const T br = gr[2 * k - 1], bi = gr[2 * k];
+                    X[k] = {cs.x * br - cs.y * bi, cs.y * br + cs.x * bi};
+                }
             }
         }
         __syncthreads();
         const int nvar = (d == 0) ? 3 : 1;
         for (int dl = 0; dl < nvar; dl++) {
             // packed spectrum Zp_k = E_k + i O_k, k < N (HC2R of length L via a length-N inverse DFT)
-            for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
-                const int b = nb == 1 ? 0 : t / N, k = t - b * N;
-                const int kmax = kmx[b];
-                const cpx<T> *X = Xs + (size_t)b * nk;
-                cpx<T> xa = c_zero<T>(), xb = c_zero<T>();
-                if (k <= kmax) xa = X[k];
-                if (N - k <= kmax && k > 0) xb = c_conj(X[N - k]);
-                if (dl > 0) {
-                    // FIxcoefficients: X_k → i κ X_k (twice for ∂λλ); κ = k for index k,
-                    // κ = k - N for index k + N (its signed wavenumber k + N - L)
-                    const float ka = (float)k, kb = (float)(k - N);
+            for (UnitWalk uw_(N); uw_.g < (G); uw_.next()) {
+        const int k = uw_.n, g = uw_.g;
+                const cpx<T> uw = c_conj(ld_cplx<T>(L.pool, rd.utw + k));
+                // FIxcoefficients: X_k → i κ X_k (twice for ∂λλ); κ = k for index k,
+                // κ = k - N for index k + N (its signed wavenumber k + N - L)
+                const float ka = (float)k, kb = (float)(k - N);
+#pragma unroll
+                for (int t = 0; t < kSweepSeqs; t++) {
+                    const int b = g * kSweepSeqs + t;
+                    if (b >= nb) break;
+                    const int kmax = kmx[b];
+                    const cpx<T> *X = Xs + (size_t)b * nk;
+                    cpx<T> xa = c_zero<T>(), xb = c_zero<T>();
+                    if (k <= kmax) xa = X[k];
+                    if (N - k <= kmax && k > 0) xb = c_conj(X[N - k]);
                     if (dl == 1) {
                         xa = {scale_f(xa.y, -ka), scale_f(xa.x, ka)};
                         xb = {scale_f(xb.y, -kb), scale_f(xb.x, kb)};
-                    } else {
+                    } else if (dl == 2) {
                         xa = {scale_f(scale_f(xa.x, -ka), ka), scale_f(scale_f(xa.y, -ka), ka)};
                         xb = {scale_f(scale_f(xb.x, -kb), kb), scale_f(scale_f(xb.y, -kb), kb)};
                     }
+                    const cpx<T> e = c_add(xa, xb);
+                    const cpx<T> o = c_mul(c_sub(xa, xb), uw);
+                    A[(size_t)b * sq + k] = {e.x - o.y, e.y + o.x};
                 }
-                cpx<T> e = c_add(xa, xb);
-                cpx<T> o = c_mul(c_sub(xa, xb), c_conj(ld_cplx<T>(L.pool, rd.utw + k)));
-                A[(size_t)b * buf + k] = {e.x - o.y, e.y + o.x};
             }
             __syncthreads();
-            cpx<T> *zb0 = dft<1, T>(A, B, pl, L.pool, nb, buf);
+            cpx<T> *zb0 = dft<1, T>(A, B, pl, L.pool, nb, L.ib);
             int slot;  // 1-based physical slot
             if (d == 0) slot = (dl == 0) ? 1 : (dl == 1 ? 4 : 5);
             else slot = (d == 1) ? 2 : 3;
             const int var = (d == 0) ? dl : (d == 1 ? 3 : 4);  // H variant: 0 f, 1 ∂λ, 2 ∂λλ, 3 ∂r, 4 ∂rr
             const int64_t plane = L.rlz ? (int64_t)var * L.nvars * L.bk * L.jDim : (int64_t)(slot - 1) * L.nvars * L.np;
-            for (int t = threadIdx.x; t < nb * N; t += blockDim.x) {
-                const int b = nb == 1 ? 0 : t / N, n = t - b * N;
-                const cpx<T> w = zb0[(size_t)b * buf + n];
+            for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
+        const int n = uw_.n, b = uw_.g;
+                const cpx<T> w = zb0[(size_t)b * sq + n];
                 if (L.rlz) {
                     T *dst = (T *)L.out + plane + ooff[b];
                     dst[2 * n] = w.x;
@@ -282,9 +306,10 @@ __global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch S) {
 // ====================================================================
 // sa_si: per 32-slot tile, SAtransform! (src/CubicBSpline.jl:1368-1396)
 //   FP64 modes: Γ b → L⁻ᵀL⁻¹ → Γᵀ (+ahat) in binary64;
-//   FP32 mode:  binary32 solve with the FP32-rounded factor, one residual
-//               r = Γb − A x in df64 against the FP64 open-form matrix, a
-//               correction solve, x += dx;
+//   FP32 mode:  binary32 solve with the FP32-rounded factor, then one FP64
+//               refinement step: residual r = Γb − A x against the FP64
+//               open-form matrix, correction solve with the FP64 factor,
+//               x += dx;
 // then the 4-tap SI/SIx/SIxx at the mish points in the compute type.
 // ====================================================================
 template <typename P, typename T>
@@ -335,18 +360,32 @@ __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
             S *r = R + threadIdx.x * ld;
             for (int i = 0; i < n; i++) r[i] = x[i];  // keep Γb
             band_solve(Ls, Di, x, n);
-            // residual r = Γb − A x with A the FP64 open-form band, in df64
+            // one refinement step in FP64: residual r = Γb − A x against the FP64
+            // open-form band, correction L Lᵀ c = r with the FP64 factor
+            // (forward sweep into r, rounded to binary32 between the sweeps),
+            // x ← x + c rounded once
+            double y1 = 0.0, y2 = 0.0, y3 = 0.0;
             for (int i = 0; i < n; i++) {
-                df64 acc = df64(r[i]);
-                for (int j = max(0, i - 3); j <= min(n - 1, i + 3); j++) {
-                    const int lo = min(i, j), dd = abs(i - j);
-                    const float2 a = __ldg(sp.Aband_x + lo * 4 + dd);
-                    acc = acc - df_mul_f(df64(a.x, a.y), x[j]);
-                }
-                r[i] = acc.hi + acc.lo;
+                double acc = (double)r[i];
+                for (int j = max(0, i - 3); j <= min(n - 1, i + 3); j++)
+                    acc -= __ldg(sp.Aband + min(i, j) * 4 + abs(i - j)) * (double)x[j];
+                if (i >= 3) acc -= __ldg(sp.L4 + (i - 3) * 4 + 3) * y3;
+                if (i >= 2) acc -= __ldg(sp.L4 + (i - 2) * 4 + 2) * y2;
+                if (i >= 1) acc -= __ldg(sp.L4 + (i - 1) * 4 + 1) * y1;
+                const double yi = acc * __ldg(sp.dinv + i);
+                r[i] = (S)yi;
+                y3 = y2; y2 = y1; y1 = yi;
             }
-            band_solve(Ls, Di, r, n);
-            for (int i = 0; i < n; i++) x[i] = x[i] + r[i];
+            double c1 = 0.0, c2 = 0.0, c3 = 0.0;
+            for (int i = n - 1; i >= 0; i--) {
+                double acc = (double)r[i];
+                if (i + 1 < n) acc -= __ldg(sp.L4 + i * 4 + 1) * c1;
+                if (i + 2 < n) acc -= __ldg(sp.L4 + i * 4 + 2) * c2;
+                if (i + 3 < n) acc -= __ldg(sp.L4 + i * 4 + 3) * c3;
+                const double ci = acc * __ldg(sp.dinv + i);
+                c3 = c2; c2 = c1; c1 = ci;
+                x[i] = (S)((double)x[i] + ci);
+            }
         } else {
             band_solve(Ls, Di, x, n);
         }
@@ -751,7 +790,7 @@ cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t s
 template <typename P>
 __global__ void __launch_bounds__(32) chain_couple_kernel(ChainLaunch C) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int v = blockIdx.y;
+    const int item = blockIdx.y, v = item / C.bk, zb = item - v * C.bk;  // RLZ: every Chebyshev level
     const SplineDev &sp = C.spl[v];
     const int b = C.b_p, ld = C.ld, n = sp.Min;
     double *X = reinterpret_cast<double *>(smem_raw);
@@ -759,7 +798,7 @@ __global__ void __launch_bounds__(32) chain_couple_kernel(ChainLaunch C) {
     double *Di = Ls + 4 * n;
     const int q0 = blockIdx.x * 32;
     const int nsl = min(32, C.nq - q0);
-    const P *spec = (const P *)C.spec + (size_t)v * C.nspec_p + (size_t)q0 * b;
+    const P *spec = (const P *)C.spec + (size_t)v * C.nspec_p + ((size_t)zb * C.zblk_p + q0) * b;
     for (int e = threadIdx.x; e < nsl * b; e += blockDim.x) X[(e / b) * ld + (e % b)] = (double)spec[e];
     for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) Ls[e] = sp.L4[e];
     for (int e = threadIdx.x; e < n; e += blockDim.x) Di[e] = sp.dinv[e];
@@ -770,29 +809,32 @@ __global__ void __launch_bounds__(32) chain_couple_kernel(ChainLaunch C) {
         band_solve(Ls, Di, x, n);
         gamma_unfold(sp, x, b, n);
         const double e0 = x[C.node[0]], e1 = x[C.node[1]], e2 = x[C.node[2]];
-        double *out = C.coupled + ((size_t)v * C.nq + q0 + threadIdx.x) * 3;
+        double *out = C.coupled + ((size_t)item * C.nq + q0 + threadIdx.x) * 3;
         for (int r = 0; r < 3; r++) out[r] = C.C[r * 3] * e0 + C.C[r * 3 + 1] * e1 + C.C[r * 3 + 2] * e2;
     }
 }
 
-// registry[q] = (spline-object ahat with this interface's side replaced by the
-// coupled values of slot q): _write_interface_ahat! + _set_wavenumber_ahat!
-// copy the whole shared ahat vector, src/multipatch.jl:533-560
+// registry[z_b, q] = (spline-object ahat with this interface's side replaced by
+// the coupled values of that slot): _write_interface_ahat! + _set_wavenumber_ahat!
+// copy the whole shared ahat vector, src/multipatch.jl:433-476 (RL), 522-569 (RLZ,
+// registry block z_b·(1+2K_s) + q)
 __global__ void chain_assemble_kernel(ChainLaunch C) {
-    const int64_t total = (int64_t)C.nvars * C.nq * C.b_s;
+    const int64_t total = (int64_t)C.nvars * C.bk * C.nq * C.b_s;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(e % C.b_s);
         const int q = (int)((e / C.b_s) % C.nq);
-        const int v = (int)(e / ((int64_t)C.b_s * C.nq));
+        const int item = (int)(e / ((int64_t)C.b_s * C.nq));
+        const int v = item / C.bk, zb = item - v * C.bk;
         const int obj = (q == 0) ? 0 : ((q & 1) ? 1 : 2);
         double val = C.state[((size_t)v * 3 + obj) * C.b_s + i];
-        const double *cp = C.coupled + ((size_t)v * C.nq + q) * 3;
+        const double *cp = C.coupled + ((size_t)item * C.nq + q) * 3;
         if (C.side == 0 && i < 3) val = cp[i];
         if (C.side == 1 && i >= C.b_s - 3) val = cp[i - (C.b_s - 3)];
-        C.reg[((size_t)v * C.nblocks_s + q) * C.b_s + i] = val;
+        C.reg[((size_t)v * C.nblocks_s + (size_t)zb * C.zblk_s + q) * C.b_s + i] = val;
     }
 }
-// after the loop over wavenumbers each spline object keeps its last slot's values
+// after the loops over levels and wavenumbers each spline object keeps the
+// values of its last slot (the last level's)
 __global__ void chain_state_kernel(ChainLaunch C) {
     const int v = blockIdx.x, obj = threadIdx.x / 3, r = threadIdx.x % 3;
     if (v >= C.nvars || obj >= 3) return;
@@ -801,17 +843,17 @@ __global__ void chain_state_kernel(ChainLaunch C) {
     else if (C.nq >= 3) q_last = (obj == 1) ? C.nq - 2 : C.nq - 1;
     if (q_last < 0) return;
     double *st = C.state + ((size_t)v * 3 + obj) * C.b_s + (C.side == 0 ? 0 : C.b_s - 3);
-    st[r] = C.coupled[((size_t)v * C.nq + q_last) * 3 + r];
+    st[r] = C.coupled[(((size_t)v * C.bk + C.bk - 1) * C.nq + q_last) * 3 + r];
 }
 
 template <typename P>
 cudaError_t launch_chain_couple(const ChainLaunch &C, size_t smem, cudaStream_t st) {
     set_smem(chain_couple_kernel<P>, smem);
-    chain_couple_kernel<P><<<dim3((C.nq + 31) / 32, C.nvars), 32, smem, st>>>(C);
+    chain_couple_kernel<P><<<dim3((C.nq + 31) / 32, C.nvars * C.bk), 32, smem, st>>>(C);
     return cudaGetLastError();
 }
 cudaError_t launch_chain_assemble(const ChainLaunch &C, cudaStream_t st) {
-    const int64_t total = (int64_t)C.nvars * C.nq * C.b_s;
+    const int64_t total = (int64_t)C.nvars * C.bk * C.nq * C.b_s;
     const int blocks = (int)std::min<int64_t>((total + 255) / 256, 4096);
     chain_assemble_kernel<<<blocks, 256, 0, st>>>(C);
     chain_state_kernel<<<C.nvars, 9, 0, st>>>(C);

@@ -85,6 +85,8 @@ struct ChainLaunch {
     double *reg;               // secondary per-wavenumber registry: [v][nblocks_s][b_s]
     int64_t nspec_p, nblocks_s;
     int b_p, b_s, ld, nq, nvars, side;  // side of the secondary: 0 left, 1 right
+    int bk;                    // Chebyshev levels (RLZ; 1 for RL)
+    int zblk_p, zblk_s;        // spectral blocks per level, 1 + 2 kDim_wn, of primary / secondary
     int node[3];
     double C[9];
 };

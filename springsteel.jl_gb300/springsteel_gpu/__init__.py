@@ -278,7 +278,8 @@ class SpringsteelGridParameters:
     def __init__(self, geometry="RL", iMin=0.0, iMax=0.0, num_cells=0, mubar=3, quadrature="gauss",
                  l_q=None, BCL=None, BCR=None, kMin=0.0, kMax=0.0, kDim=0, b_kDim=None, BCB=None, BCT=None,
                  vars=None, max_wavenumber=None, fourier_filter=None, chebyshev_filter=None,
-                 spectralIndexL=1, patchOffsetL=None, precision="f64", **derived):
+                 spectralIndexL=1, patchOffsetL=None, precision="f64", i_regular_out=None, j_regular_out=None,
+                 k_regular_out=None, **derived):
         geom = {"RL": "RL", "Spline1D_Fourier": "RL", "RLZ": "RLZ"}.get(geometry, geometry)
         if geom not in ("RL", "RLZ"):
             raise ValueError("only RL and RLZ geometries run on the GPU path (got %r)" % geometry)
@@ -301,6 +302,10 @@ class SpringsteelGridParameters:
         self.spectralIndexL = int(spectralIndexL)
         self.patchOffsetL = (self.spectralIndexL - 1) * self.mubar if patchOffsetL is None else int(patchOffsetL)
         self.precision = precision
+        # regular output sizes, src/Springsteel.jl:461-464 defaults
+        self.i_regular_out = self.num_cells + 1 if i_regular_out is None else int(i_regular_out)
+        self.j_regular_out = self.iDim * 2 + 1 if j_regular_out is None else int(j_regular_out)
+        self.k_regular_out = self.kDim + 1 if k_regular_out is None else int(k_regular_out)
 
     def var_names(self):
         names = [None] * len(self.vars)
@@ -651,10 +656,12 @@ def compute_patch_offsets(boundaries, cells, mubar=3):
     return offsets
 
 
-def chain_grid_params(boundaries, cells, vars=None, BCL=None, BCR=None, mubar=3, l_q=None, precision="f64"):
+def chain_grid_params(boundaries, cells, vars=None, BCL=None, BCR=None, mubar=3, l_q=None, precision="f64",
+                      geometry="RL", **column):
     """Per-patch parameters of a chain (_create_chain, src/multipatch.jl:1018-1111):
     at each interface the finer side gets FixedBC (R3X), the coarser NaturalBC;
-    patch offsets follow _compute_patch_offsets."""
+    patch offsets follow _compute_patch_offsets.  geometry="RLZ" chains take the
+    shared column parameters (kMin, kMax, kDim, BCB, BCT) as keywords."""
     n = len(boundaries) - 1
     cells = [cells] * n if isinstance(cells, int) else list(cells)
     vars = vars or {"u": 1}
@@ -675,9 +682,9 @@ def chain_grid_params(boundaries, cells, vars=None, BCL=None, BCR=None, mubar=3,
     bl[0] = BCL or {"default": NaturalBC()}
     br[-1] = BCR or {"default": NaturalBC()}
     offs = compute_patch_offsets(boundaries, cells, mubar)
-    return [SpringsteelGridParameters(geometry="RL", iMin=boundaries[k], iMax=boundaries[k + 1], num_cells=cells[k],
-                                      mubar=mubar, vars=vars, BCL=bl[k], BCR=br[k], l_q=l_q,
-                                      patchOffsetL=offs[k], precision=precision) for k in range(n)]
+    return [SpringsteelGridParameters(geometry=geometry, iMin=boundaries[k], iMax=boundaries[k + 1],
+                                      num_cells=cells[k], mubar=mubar, vars=vars, BCL=bl[k], BCR=br[k], l_q=l_q,
+                                      patchOffsetL=offs[k], precision=precision, **column) for k in range(n)]
 
 
 # ----------------------------------------------------------------- tiles
@@ -763,3 +770,64 @@ def zero_spectral(grid, stream=None):
 
 # ----------------------------------------------------------------- elliptic solve
 from .solver import MLPPreconditioner, SpringsteelProblem, solve  # noqa: E402
+
+
+# ----------------------------------------------------------------- regular-grid output
+def _lin_range(a, b, n):
+    """Julia's LinRange(a, b, n) points, (1 − t)·a + t·b with t = j/(n − 1)."""
+    if n == 1:
+        return np.array([float(a)])
+    t = np.arange(n, dtype=np.float64) / float(n - 1)
+    return (1.0 - t) * a + t * b
+
+
+def regular_axes(gp):
+    """(r, λ, z) axes of getRegularGridpoints (src/transforms_cylindrical.jl:878-898,
+    1117-1138): i_regular_out radii on [iMin, iMax], j_regular_out angles 2π(j−1)/n_λ,
+    k_regular_out levels on [kMin, kMax] (RLZ; None for RL)."""
+    r = _lin_range(gp.iMin, gp.iMax, gp.i_regular_out)
+    n_l = gp.j_regular_out
+    lam = np.array([2 * math.pi * j / n_l for j in range(n_l)])
+    z = _lin_range(gp.kMin, gp.kMax, gp.k_regular_out) if gp.geometry == "RLZ" else None
+    return r, lam, z
+
+
+def getRegularGridpoints(grid_or_params):
+    """getRegularGridpoints: (n_r·n_λ[·n_z], 2|3) points, r outer, λ (then z) inner."""
+    gp = getattr(grid_or_params, "params", grid_or_params)
+    r, lam, z = regular_axes(gp)
+    axes = (r, lam) if z is None else (r, lam, z)
+    mesh = np.meshgrid(*axes, indexing="ij")
+    return np.column_stack([m.reshape(-1) for m in mesh])
+
+
+def regularGridTransform(grid, *points, stream=None):
+    """regularGridTransform(grid, r_pts, λ_pts[, z_pts]) or regularGridTransform(grid,
+    gridpoints) (src/transforms_cylindrical.jl:929-1020 RL, 1168-1287 RLZ) from the
+    device-resident spectral array: returns (n_r·n_λ[·n_z], nvars, 5|7) FP64, slots
+    f, ∂r, ∂rr, ∂λ, ∂λλ (, ∂z, ∂zz).  A single points matrix is split as the
+    reference does: sorted unique r (and z); λ the first n_λ rows (RL) or sorted
+    unique (RLZ)."""
+    gp = grid.params
+    if len(points) == 1:
+        pts = np.asarray(points[0], np.float64)
+        r = np.unique(pts[:, 0])
+        if gp.geometry == "RL":
+            lam = pts[: pts.shape[0] // len(r), 1]
+            z = None
+        else:
+            lam, z = np.unique(pts[:, 1]), np.unique(pts[:, 2])
+    else:
+        r, lam = np.asarray(points[0], np.float64), np.asarray(points[1], np.float64)
+        z = np.asarray(points[2], np.float64) if len(points) > 2 else None
+    if (gp.geometry == "RLZ") != (z is not None):
+        raise ValueError("RLZ grids take r, λ and z points; RL grids r and λ")
+    nz = 1 if z is None else len(z)
+    d = grid.dims
+    out = np.empty((len(r) * len(lam) * nz, d["nvars"], d["nslots"]), order="F")
+    rp, lp = np.ascontiguousarray(r), np.ascontiguousarray(lam)
+    zp = np.ascontiguousarray(z) if z is not None else None
+    _check(load_library().ss_regular_grid_transform(
+        grid.handle, rp.ctypes.data_as(C.c_void_p), len(r), lp.ctypes.data_as(C.c_void_p), len(lam),
+        zp.ctypes.data_as(C.c_void_p) if zp is not None else None, nz, out.ctypes.data_as(C.c_void_p), stream))
+    return out

@@ -44,6 +44,32 @@ def test_rl_chain_40_120_40_parity():
             assert np.all(errs <= TOL64), errs
 
 
+def test_rlz_chain_parity():
+    """RLZ patches coupled per Chebyshev level and wavenumber (_rlz_kernel!,
+    src/multipatch.jl:496-571): a 2-patch chain (2:1 at the interface) and the
+    3-patch 40/120/40-shaped chain at reduced size, twice in a row."""
+    col = dict(kMin=0.0, kMax=20000.0, kDim=16, BCB={"default": S.DirichletBC()}, BCT={"default": S.NeumannBC()})
+    for bounds, cells in (([0.0, 20.0, 30.0], [10, 10]), ([0.0, 12.0, 30.0, 42.0], [6, 18, 6])):
+        ps = S.chain_grid_params(bounds, cells, vars={"u": 1, "w": 2}, geometry="RLZ", **col)
+        gs = [S.createGrid(p) for p in ps]
+        os_ = [O.OracleGrid(p.to_abi()) for p in ps]
+        specs = []
+        for i, (g, o) in enumerate(zip(gs, os_)):
+            u = _fill(g, seed=i + 5)
+            ph = np.zeros(o.physical_shape, order="F")
+            ph[:, :, 0] = u
+            specs.append(o.spectral_transform(ph))
+            S.spectralTransform_b(g)
+        chain = S.PatchChain(gs)
+        och = O.OracleChain(os_)
+        for _ in range(2):
+            chain.multiGridTransform()
+            ref = och.multi_grid_transform(specs)
+            for p, g, r in zip(ps, gs, ref):
+                errs = slot_errors(g.get_physical(), r, p)
+                assert np.all(errs <= TOL64), errs
+
+
 def test_two_patch_chain_linear_exactness():
     gp1 = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=50.0, num_cells=10)
     gp2 = S.SpringsteelGridParameters(geometry="RL", iMin=50.0, iMax=75.0, num_cells=10,
