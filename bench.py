@@ -725,6 +725,66 @@ def run_ours(args):
     return 3 if failed else 0
 
 
+def run_cufft_comparison(args):
+    """Comparison point only, never the product path: the vendor FFT (cuFFT through
+    torch.fft) timed on the same ring lengths and batch sizes as the workload's
+    ring stages — one batched C2R per ring with the inverse stage's 5 real
+    outputs per (variable, Chebyshev mode), one batched R2C per ring for the
+    forward stage.  It leaves out what the library's ring kernels also do (the
+    phase rotation, the λ-derivative scaling, the packed-row gathers), so it is
+    a lower bound on a cuFFT-based ring stage.  Prints one JSON line."""
+    import torch
+
+    _, rank, local = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from springsteel_gpu import abi  # noqa: F401  (same package path as the main arms)
+
+    gp = _params(args.workload)
+    w = WORKLOADS[args.workload]
+    nrings, pol = gp.num_cells * 3, 0
+    items = w["nvars"] * (gp.b_kDim if getattr(gp, "b_kDim", 0) else _bk(w["kDim"]))
+    real = torch.float32 if w["precision"] == "f32" else torch.float64
+    cplx = torch.complex64 if real == torch.float32 else torch.complex128
+    torch.backends.cuda.cufft_plan_cache.max_size = 4096
+    out = {}
+    for stage, batch, inverse in (("ring_inverse", 5 * items, True), ("ring_forward", items, False)):
+        xs = []
+        for r in range(1, nrings + 1):
+            L = 4 + 4 * (r + pol)
+            xs.append((L, torch.randn(batch, L // 2 + 1, dtype=cplx, device="cuda") if inverse
+                       else torch.randn(batch, L, dtype=real, device="cuda")))
+
+        def one():
+            for L, x in xs:
+                torch.fft.irfft(x, n=L) if inverse else torch.fft.rfft(x)
+
+        for _ in range(max(args.warmup, 1)):
+            one()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(max(args.steps, 1)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            one()
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[stage] = {"ms": best, "transforms_per_ring": batch, "rings": nrings}
+        del xs
+        torch.cuda.empty_cache()
+    print(json.dumps({"comparison": "cuFFT (torch.fft, %s) on the ring lengths 4+4r, r = 1..%d" % (
+        torch.version.cuda, nrings), "workload": args.workload, "dtype": str(real).replace("torch.", ""),
+        "stages": out}), flush=True)
+    return 0
+
+
+def _bk(kz):
+    """b_kDim of a kz-level Chebyshev column (src/Springsteel.jl:425-465)."""
+    return min(kz, (2 * kz - 1) // 3 + 1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -734,7 +794,11 @@ def main():
     ap.add_argument("--workload", default="rlz200-f64", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true", help="skip the FP32 400-cell grid of the default run")
+    ap.add_argument("--cufft-comparison", action="store_true",
+                    help="time cuFFT on the workload's ring lengths instead (comparison point only)")
     args = ap.parse_args()
+    if args.cufft_comparison:
+        return run_cufft_comparison(args)
     if args.workload == "elliptic-rl200":
         return run_elliptic(args)
     if args.workload.startswith("batch-"):

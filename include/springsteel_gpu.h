@@ -206,6 +206,21 @@ int32_t ss_grid_clear_ahat(ss_grid *grid);
 
 int32_t ss_grid_synchronize(ss_grid *grid);
 
+/* Tile pipeline (src/tiling.jl).  ss_spline_transform is splineTransform!(
+ * sharedSpectral, tile) (RL :1490-1516, RLZ :1862-1892): SAtransform(spline, b)
+ * of every wavenumber (and Chebyshev-mode) block of `d_shared_spectral`, a
+ * device array in the tile's own spectral layout and storage type (NULL: the
+ * tile's spectral array itself, in place), written as spline coefficients a
+ * into the tile's spectral array.  The two-argument SAtransform applies no R3X
+ * background.  ss_tile_transform is tileTransform!(sharedSpectral, tile,
+ * physical, spectral) (RL :1540-1660, RLZ :1915-2046): the tile's spectral
+ * array holds coefficients a; SI / SIx / SIxx, the ring inverse with its λ
+ * derivatives and, for RLZ, the Chebyshev inverse with its z derivatives fill
+ * every physical slot — gridTransform! without its SAtransform!.  Both queue
+ * on `stream` (NULL: the grid's stream). */
+int32_t ss_spline_transform(ss_grid *grid, const void *d_shared_spectral, void *stream);
+int32_t ss_tile_transform(ss_grid *grid, void *stream);
+
 /* regularGridTransform(grid, r_pts, λ_pts[, z_pts]) (src/transforms_cylindrical.jl:929-1020
  * RL, 1168-1287 RLZ): the device-resident spectral array evaluated on the tensor
  * product of n_r radii, n_lam azimuths and (RLZ) n_z levels: per wavenumber (and

@@ -48,6 +48,8 @@ def lib():
             "or_grid_ring_points": ([vp, i32, vp], i32),
             "or_grid_column_points": ([vp, vp], i32),
             "or_grid_factor": ([vp, i32, vp, C.POINTER(i32)], i32),
+            "or_grid_spline_transform": ([vp, vp, vp], i32),
+            "or_grid_transform_coeffs": ([vp, vp, vp], i32),
             "or_spline_create": ([d, d, i32, i32, i32, d, C.POINTER(abi.ss_spline_bc),
                                   C.POINTER(abi.ss_spline_bc), C.POINTER(vp)], i32),
             "or_spline_destroy": ([vp], None),
@@ -151,6 +153,22 @@ class OracleGrid:
         sp = np.asfortranarray(spectral, dtype=np.float64)
         ph = np.zeros(self.physical_shape, dtype=np.float64, order="F")
         _check(lib().or_grid_transform(self.h, _ptr(sp), _ptr(ph)))
+        return ph
+
+    def spline_transform(self, shared):
+        """splineTransform!(sharedSpectral, tile) (src/tiling.jl:1490-1516, 1862-1892):
+        spline coefficients a of every block of `shared` (the grid's spectral layout)."""
+        sp = np.asfortranarray(shared, dtype=np.float64)
+        a = np.zeros(self.spectral_shape, dtype=np.float64, order="F")
+        _check(lib().or_grid_spline_transform(self.h, _ptr(sp), _ptr(a)))
+        return a
+
+    def tile_transform(self, acoef):
+        """tileTransform!(sharedSpectral, tile, physical, spectral) (src/tiling.jl:1540-1660,
+        1915-2046): every physical slot from spline coefficients a (no SAtransform!)."""
+        a = np.asfortranarray(acoef, dtype=np.float64)
+        ph = np.zeros(self.physical_shape, dtype=np.float64, order="F")
+        _check(lib().or_grid_transform_coeffs(self.h, _ptr(a), _ptr(ph)))
         return ph
 
     def set_ahat(self, var, block, ahat):

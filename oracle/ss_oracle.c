@@ -1680,6 +1680,24 @@ int32_t or_elliptic_solve_spectral(const or_elliptic *e, double *spec) {
     return SS_OK;
 }
 
+/* splineTransform!(sharedSpectral, tile), src/tiling.jl:1490-1516 (RL, blocks
+ * p = 2k) and 1862-1892 (RLZ, blocks z_b·(1+2K) + (k−1)·2 + 1): every block of
+ * b_iDim B-values goes through the two-argument SAtransform(spline, b)
+ * (src/CubicBSpline.jl:1355-1359: Γᵀ (PQ)⁻¹ Γ b, no R3X background) into the
+ * same rows of `acoef`.  Both layouts are one run of b-row blocks per variable. */
+int32_t or_grid_spline_transform(const or_grid *g, const double *shared, double *acoef) {
+    const int b = g->b;
+    const long nblk = (long)g->bk * (1 + 2L * g->K);
+    double *t = (double *)malloc(sizeof(double) * 3 * (size_t)b);
+    for (int v = 0; v < g->nvars; v++)
+        for (long q = 0; q < nblk; q++) {
+            const size_t o = (size_t)g->nspec * v + (size_t)q * b;
+            spline_sa(g->spl[v], shared + o, NULL, acoef + o, t, t + b, t + 2 * b);
+        }
+    free(t);
+    return SS_OK;
+}
+
 /* a-coefficients in spectral layout → physical (the SI + ring stages of gridTransform!) */
 int32_t or_grid_transform_coeffs(or_grid *g, const double *acoef, double *phys) {
     /* SA with the identity: run the inverse driver on a grid whose SA is skipped */

@@ -58,6 +58,8 @@ void or_elliptic_destroy(or_elliptic *e);
 int32_t or_elliptic_operator(const or_elliptic *e, int32_t m, double *G, int32_t *n_out);
 int32_t or_elliptic_solve_spectral(const or_elliptic *e, double *spec);
 int32_t or_grid_transform_coeffs(or_grid *g, const double *acoef, double *phys);
+/* splineTransform! of every spectral block (no R3X background) */
+int32_t or_grid_spline_transform(const or_grid *g, const double *shared, double *acoef);
 
 /* ---- 1-D primitives for the known-answer tests -------------------------- */
 typedef struct or_spline or_spline;

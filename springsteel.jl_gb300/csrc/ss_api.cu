@@ -514,11 +514,14 @@ static int32_t fwd_sb(ss_grid *g, cudaStream_t st) {
     return SS_OK;
 }
 
+// `aout` set: splineTransform! — SAtransform(spline, b) of every block of `spec_in`
+// (the 2-argument form: no R3X background) written as coefficients to `aout`
 template <typename P, typename T>
-static int32_t inv_sa(ss_grid *g, cudaStream_t st, int coeffs) {
+static int32_t inv_sa(ss_grid *g, cudaStream_t st, int coeffs, const void *spec_in = nullptr, void *aout = nullptr) {
     const ss_dims &d = g->d;
     SaLaunch A{};
-    A.spec = g->spec; A.G = g->G; A.spl = g->d_spl; A.fofs = g->d_fofs; A.ahat = g->d_ahat;
+    A.spec = spec_in ? spec_in : g->spec; A.G = g->G; A.spl = g->d_spl; A.fofs = g->d_fofs;
+    A.ahat = aout ? nullptr : g->d_ahat; A.aout = aout;
     A.frows = g->frows; A.nspec = d.n_spectral; A.nblocks = d.n_blocks;
     A.iDim = (int)d.iDim; A.b = (int)d.b_iDim; A.ld = (A.b % 2) ? A.b : A.b + 1;
     A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = (int)d.b_kDim; A.nitems = g->nitems; A.coeffs = coeffs;
@@ -529,7 +532,8 @@ static int32_t inv_sa(ss_grid *g, cudaStream_t st, int coeffs) {
     if (g->tl != TL_F64) smem += size_t(32) * A.ld * ssz;  // FP32 residuals / df64 coefficients
     StageScope sc(g, SS_STAGE_SA_SI, st);
     if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
-        CUDA_TRY((launch_sa_si_f32<P>(A, g->nitems, (float *)g->sa_x, (float *)g->sa_y, st)));
+        if (aout) CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
+        else CUDA_TRY((launch_sa_si_f32<P>(A, g->nitems, (float *)g->sa_x, (float *)g->sa_y, st)));
     } else {
         CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
     }
@@ -666,6 +670,12 @@ int32_t grid_inverse_coeffs(ss_grid *g, cudaStream_t s) {
     if (g->tl == TL_DF64) return run_inverse<double, df64>(g, s, 1);
     if (g->tl == TL_F64) return run_inverse<double, double>(g, s, 1);
     return run_inverse<float, float>(g, s, 1);
+}
+static int32_t grid_spline_coeffs(ss_grid *g, cudaStream_t s, const void *shared) {
+    const void *in = shared ? shared : g->spec;
+    if (g->tl == TL_DF64) return inv_sa<double, df64>(g, s, 0, in, g->spec);
+    if (g->tl == TL_F64) return inv_sa<double, double>(g, s, 0, in, g->spec);
+    return inv_sa<float, float>(g, s, 0, in, g->spec);
 }
 static int32_t grid_forward_host(ss_grid *g, cudaStream_t s, const void *host_slot1) {
     if (g->tl == TL_DF64) return run_forward<double, df64>(g, s, host_slot1);
@@ -868,6 +878,16 @@ int32_t ss_spectral_transform(ss_grid *g, void *stream) {
 int32_t ss_grid_transform(ss_grid *g, void *stream) {
     CHECK_GRID(g);
     return grid_inverse(g, pick(g, stream));
+}
+
+int32_t ss_spline_transform(ss_grid *g, const void *d_shared_spectral, void *stream) {
+    CHECK_GRID(g);
+    return grid_spline_coeffs(g, pick(g, stream), d_shared_spectral);
+}
+
+int32_t ss_tile_transform(ss_grid *g, void *stream) {
+    CHECK_GRID(g);
+    return grid_inverse_coeffs(g, pick(g, stream));
 }
 
 int32_t ss_spectral_transform_from_host(ss_grid *g, const void *host_slot1, int32_t dtype, void *stream) {

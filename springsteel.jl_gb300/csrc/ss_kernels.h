@@ -63,6 +63,8 @@ struct SaLaunch {
     int64_t frows, nspec, nblocks;
     int iDim, b, ld, pOL, nslots_z, bk, nitems;
     int coeffs;                // 1: spectral holds spline coefficients a (skip SAtransform!)
+    void *aout;                // non-null: write the coefficients a (storage type, spectral
+                               // layout) here and skip SI (splineTransform!)
 };
 
 struct ChebLaunch {

@@ -764,6 +764,36 @@ def tile_physical_to_patch(patch, tile, slot=0, stream=None):
     _check(load_library().ss_tile_copy_physical(patch.handle, tile.handle, int(slot), 1, stream))
 
 
+def splineTransform_b(shared, tile, stream=None):
+    """splineTransform!(sharedSpectral, tile) (src/tiling.jl:1490-1516 RL, 1862-1892 RLZ):
+    SAtransform(spline, b) of every wavenumber (and Chebyshev-mode) block of
+    `shared` — a grid whose device spectral array holds B-vectors in the tile's
+    spectral layout and precision, or None for the tile's own spectral array —
+    written as spline coefficients a into the tile's spectral array.  As in the
+    reference, the two-argument SAtransform adds no R3X background."""
+    lib = load_library()
+    ptr = None
+    if shared is not None:
+        if shared.spectral_shape != tile.spectral_shape or \
+                (shared.params.precision == "f32") != (tile.params.precision == "f32"):
+            raise ValueError("shared spectral array must match the tile's spectral shape and storage type")
+        p = C.c_void_p()
+        _check(lib.ss_grid_device_spectral(shared.handle, C.byref(p)))
+        shared.synchronize()
+        ptr = p
+    _check(lib.ss_spline_transform(tile.handle, ptr, stream))
+
+
+def tileTransform_b(shared, tile, stream=None):
+    """tileTransform!(sharedSpectral, tile, physical, spectral) (src/tiling.jl:1540-1660 RL,
+    1915-2046 RLZ): the tile's spectral array holds spline coefficients a (from
+    splineTransform_b); every physical slot is evaluated from them — SI / SIx /
+    SIxx, the ring inverse with ∂λ, ∂λλ and, for RLZ, the Chebyshev inverse with
+    ∂z, ∂zz — gridTransform! without its SAtransform!.  `shared` is unused, as in
+    the reference (kept for the same call shape)."""
+    _check(load_library().ss_tile_transform(tile.handle, stream))
+
+
 def zero_spectral(grid, stream=None):
     _check(load_library().ss_grid_zero_spectral(grid.handle, stream))
 

@@ -157,7 +157,7 @@ EXPORTED = [
     "ss_spectral_transform", "ss_grid_transform", "ss_spectral_transform_from_host",
     "ss_grid_transform_to_host", "ss_grid_set_filter", "ss_grid_set_ahat",
     "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
-    "ss_spectral_transform_noalloc", "ss_regular_grid_transform",
+    "ss_spectral_transform_noalloc", "ss_regular_grid_transform", "ss_spline_transform", "ss_tile_transform",
     "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads",
     "ss_chain_create", "ss_chain_destroy", "ss_multi_grid_transform",
     "ss_tile_sum_spectral", "ss_tile_copy_physical", "ss_grid_zero_spectral",
@@ -218,6 +218,8 @@ def bind(lib):
         "ss_grid_profile_read": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)], i32),
         "ss_spectral_transform_noalloc": ([vp, vp, vp, vp], i32),
         "ss_regular_grid_transform": ([vp, vp, i32, vp, i32, vp, i32, vp, vp], i32),
+        "ss_spline_transform": ([vp, vp, vp], i32),
+        "ss_tile_transform": ([vp, vp], i32),
         "ss_batch_create": ([vp, i32, i32, C.POINTER(vp)], i32),
         "ss_batch_destroy": ([vp], i32),
         "ss_batch_run": ([vp, i32, i32, vp], i32),
