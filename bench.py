@@ -102,20 +102,26 @@ def run_batch(args):
         batch.run(what=3, use_graph=True)
     batch.synchronize()
 
-    def timed(fn, steps):  # wall clock between device-wide synchronisations
+    def timed(fn, steps, on=None):  # wall clock between device-wide synchronisations
         torch.cuda.synchronize()
         for g in grids:
             g.synchronize()
         t0 = time.perf_counter()
         for _ in range(steps):
             fn()
-        batch.synchronize()
+        (on or batch).synchronize()
         for g in grids:
             g.synchronize()
         return (time.perf_counter() - t0) / steps
 
+    # the same grids with per-grid launch sequences on forked streams (graph)
+    seq = S.Batch(grids, autotune=False, fused=False)
+    for _ in range(max(args.warmup, 3)):
+        seq.run(what=3, use_graph=True)
+    seq.synchronize()
     with ClockSampler(local) as clk:
         t_batch = timed(lambda: batch.run(what=3, use_graph=True), args.steps)
+        t_seq = timed(lambda: seq.run(what=3, use_graph=True), args.steps, on=seq)
 
         def singles():
             for g in grids:
@@ -142,20 +148,24 @@ def run_batch(args):
     h2d = sum(p.numel() * p.element_size() for p in pinned)
     d2h = sum(o.numel() * o.element_size() for o in outs)
     peak, peak_kind = _peaks()
+    fused_launches = batch.fused_launches(3)
     line = {
-        "metric": "batched RL transforms/s (64 uneven grids, graph)", "value": 1.0 / t_batch,
+        "metric": "batched RL transforms/s (64 uneven grids, fused launches under a graph)", "value": 1.0 / t_batch,
         "unit": "batch round trips/s", "n_gpus": ws, "steps": args.steps, "warmup": max(args.warmup, 3),
         "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if host_dt == np.float32 else "f64", "data": "synthetic",
         "config": {"workload": args.workload, "grids": len(grids),
                    "cells": [g.params.num_cells for g in grids], "vars": [g.dims["nvars"] for g in grids]},
-        "individual_calls_ms": t_single * 1e3, "graph_speedup": t_single / t_batch,
+        "individual_calls_ms": t_single * 1e3, "speedup_vs_individual_calls": t_single / t_batch,
+        "per_grid_sequences_graph_ms": t_seq * 1e3, "speedup_vs_per_grid_graph": t_seq / t_batch,
+        "fused_launches_per_round_trip": fused_launches,
         "path_gbs": nbytes / t_batch / 1e9, "path_frac": nbytes / t_batch / 1e9 / peak, "peak": peak,
         "peak_source": peak_kind, "clocks": clk.summary(),
         "e2e": {"value": 1.0 / t_e2e, "unit": "batch round trips/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
     }
     batch.close()
+    seq.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -472,10 +482,27 @@ def _oracle_roundtrip(gp, slot1, threads, var_index=None):
     return dt, out
 
 
-# Measured DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum, summed over
-# every bucket launch of one stage pass) per round trip, from ncu captures of the
-# bench workloads themselves (profiles/traffic_ring_stages.md)
-MEASURED_TRAFFIC = {}
+# Measured DRAM traffic of each stage for one round trip: dram__bytes_read.sum +
+# dram__bytes_write.sum summed over the stage's launches (every ring bucket), from
+# one ncu capture (1-pass metrics, --clock-control none) of the full-size bench
+# workload itself: `bench.py --workload W --steps 1 --warmup 3 --no-cpu-baseline
+# --no-secondary` under `ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,
+# dram__bytes_write.sum -k regex:"ring_|cheb_|sa_si|sb_project"`, one warm-up
+# round trip's launches.  Bytes per round trip.
+MEASURED_TRAFFIC = {
+    ("rlz200-f64", "cheb_forward"): 1.538e9,
+    ("rlz200-f64", "ring_forward"): 0.870e9,
+    ("rlz200-f64", "sb_project"): 0.493e9,
+    ("rlz200-f64", "sa_si"): 1.106e9,
+    ("rlz200-f64", "ring_inverse"): 3.957e9,
+    ("rlz200-f64", "cheb_inverse"): 9.643e9,
+    ("rlz400-f32", "cheb_forward"): 9.913e9,
+    ("rlz400-f32", "ring_forward"): 5.917e9,
+    ("rlz400-f32", "sb_project"): 3.279e9,
+    ("rlz400-f32", "sa_si"): 23.999e9,
+    ("rlz400-f32", "ring_inverse"): 26.922e9,
+    ("rlz400-f32", "cheb_inverse"): 64.518e9,
+}
 
 
 def run_reference(args):
@@ -641,9 +668,14 @@ def measure(wl, args, lib, ws, rank, local, cpu_baseline=True):
     traffic = MEASURED_TRAFFIC.get((wl, dom))
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-            "traffic_source": "ncu capture of this workload (profiles/traffic_ring_stages.md)" if traffic else None,
-            "algorithmic_bytes_per_launch": sb[dom],
+            "traffic_source": ("ncu capture of this full-size workload: dram__bytes_read.sum + "
+                               "dram__bytes_write.sum over the stage's launches of one round trip") if traffic else None,
+            "traffic_over_algorithmic": traffic / sb[dom] if traffic else None,
+            "algorithmic_bytes_per_step": sb[dom],
+            "launches_per_step": int(launches[names.index(dom)]) // max(args.steps, 1),
             "stage_ms_per_step": per_step_ms,
+            "stage_traffic_per_step": {k: MEASURED_TRAFFIC.get((wl, k)) for k in names},
+            "stage_algorithmic_bytes_per_step": sb,
             "path_achieved_gbs": path_gbs, "path_frac": path_gbs / peak}
     gpu_launches = int(sum(launches[i] for i in range(6)))
     # the ring stages are bound by the arithmetic pipe of the compute type, not by

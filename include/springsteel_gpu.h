@@ -206,6 +206,38 @@ int32_t ss_grid_clear_ahat(ss_grid *grid);
 
 int32_t ss_grid_synchronize(ss_grid *grid);
 
+/* ---- grid archives: save_grid / load_grid (src/io.jl:410-439) ---------
+ * The reference archives params, spectral and physical in a JLD2 file with a
+ * format-version tag and rebuilds the grid with createGrid(params).  Without
+ * an HDF5/JLD2 library in this build the same components go into a flat
+ * little-endian file:
+ *   "SSGRID01" (8 bytes: magic and format version 01)
+ *   uint32 R, uint32 U        byte counts of the two blocks that follow
+ *   R bytes  parameter record: int32 geometry, precision, num_cells, mubar,
+ *            quadrature, nvars, kDim, b_kDim, patchOffsetL, ring_kmax_set,
+ *            ring_kmax, dtype (SS_DTYPE_*), filtered; double iMin, iMax, kMin,
+ *            kMax; per variable: double l_q, BCL and BCR as ss_spline_bc
+ *            (int32 kind, int32 0, double alpha, double beta), int32 BCB,
+ *            BCT, max_wavenumber, 0; int64 n_spectral, n_physical, nslots,
+ *            nvars, nfw, ncw; nfw + ncw doubles of spectral filter weights
+ *            (Fourier [var][k ≤ kDim_wn], then Chebyshev [var][z_b])
+ *   U bytes  caller block (the host mirror stores its variable names)
+ *   spectral (n_spectral × nvars) then physical (n_physical × nvars × nslots),
+ *            column-major as grid.spectral / grid.physical, in the grid's
+ *            storage type.
+ * The arrays stream between HBM and the file through page-locked staging
+ * buffers, each chunk's copy overlapping the previous chunk's file write
+ * (read, loading).  The R3X background registry is not archived, as in the
+ * reference (it is not part of params).  Every call returns once the file
+ * or the grid is complete. */
+int32_t ss_grid_save(ss_grid *grid, const char *path, const void *user, int64_t user_bytes, void *stream);
+/* load_grid: a new grid from the archived parameters and arrays (and filter). */
+int32_t ss_grid_load(const char *path, ss_grid **out, void *stream);
+/* The archived arrays into an existing grid of the same shape and storage type. */
+int32_t ss_grid_load_arrays(ss_grid *grid, const char *path, void *stream);
+/* The caller block of an archive: copies min(cap, size) bytes, size in *user_bytes. */
+int32_t ss_grid_archive_user(const char *path, void *buf, int64_t cap, int64_t *user_bytes);
+
 /* Tile pipeline (src/tiling.jl).  ss_spline_transform is splineTransform!(
  * sharedSpectral, tile) (RL :1490-1516, RLZ :1862-1892): SAtransform(spline, b)
  * of every wavenumber (and Chebyshev-mode) block of `d_shared_spectral`, a
@@ -253,10 +285,20 @@ enum {
 /* ---- many grids: batches under a CUDA graph ----------------------------
  * No single reference counterpart: the reference transforms grids one call
  * at a time (multipatch layers "can be transformed in parallel",
- * src/multipatch.jl:659-661, but run serially :771-784).  A batch enqueues
- * every grid's stages on forked streams; with use_graph the sequence is
- * captured once into a CUDA graph and replayed.  flags & 1 autotunes the
- * ring-kernel CTA size of each grid at creation (timed on the grid's data). */
+ * src/multipatch.jl:659-661, but run serially :771-784).
+ * Without SS_BATCH_FUSED a batch enqueues every grid's own stage launches on
+ * forked streams.  With SS_BATCH_FUSED the RL grids' stages are fused across
+ * grids: every stage is one launch per shared-memory class (ring stages) or one
+ * launch (SB, SA) whose CTAs each run one grid's record from a device work
+ * list — 64 uneven grids take about ten launches per round trip instead of
+ * ~700; RLZ grids keep their own launch sequences.  Results are bit-identical
+ * to single-grid calls.  With use_graph the sequence is captured once into a
+ * CUDA graph and replayed (captured again after ss_grid_set_ahat /
+ * ss_grid_clear_ahat / ss_grid_set_filter on a member grid).
+ * SS_BATCH_AUTOTUNE times candidate tile shapes at creation on the grids' own
+ * data: per grid the ring-kernel CTA size (64/128/256) without fusion; with
+ * fusion the ring CTA size (128/256) and the items per ring CTA (×1, ×2). */
+enum { SS_BATCH_AUTOTUNE = 1, SS_BATCH_FUSED = 2 };
 typedef struct ss_batch ss_batch;
 int32_t ss_batch_create(ss_grid *const *grids, int32_t n, int32_t flags, ss_batch **out);
 int32_t ss_batch_destroy(ss_batch *batch);
@@ -264,6 +306,9 @@ int32_t ss_batch_destroy(ss_batch *batch);
 int32_t ss_batch_run(ss_batch *batch, int32_t what, int32_t use_graph, void *stream);
 int32_t ss_batch_synchronize(ss_batch *batch);
 int32_t ss_batch_ring_threads(const ss_batch *batch, int32_t index, int32_t *fwd, int32_t *inv);
+/* Kernel launches of a fused batch for `what` (0 without SS_BATCH_FUSED); its
+ * RLZ grids, which keep their own sequences, are not counted. */
+int32_t ss_batch_fused_launches(const ss_batch *batch, int32_t what, int32_t *launches);
 
 /* ---- RL multi-patch chain ---------------------------------------------
  * PatchChain(grids) (src/multipatch.jl:825-848) and multiGridTransform!

@@ -475,22 +475,67 @@ static int32_t fwd_columns(ss_grid *g, cudaStream_t st, int chunk) {
     return SS_OK;
 }
 
-template <typename P, typename T>
-static int32_t fwd_rings(ss_grid *g, cudaStream_t st, int chunk) {
+namespace ss {
+// Launch records of the per-grid stages (also the records of fused batch launches)
+RingLaunch ring_record(const ss_grid *g, bool inverse) {
     const ss_dims &d = g->d;
     RingLaunch L{};
     L.rings = g->d_rings;
     L.ring_var_stride = g->rlz ? 0 : d.iDim;
     L.plans = g->d_plans; L.pool = g->d_pool; L.phase = g->d_phase;
-    L.in = g->rlz ? g->C : g->phys;
-    L.out = g->F;
-    L.in_item_stride = d.n_physical;
+    if (inverse) {
+        L.in = g->G;
+        L.out = g->rlz ? g->H : g->phys;
+    } else {
+        L.in = g->rlz ? g->C : g->phys;
+        L.out = g->F;
+        L.in_item_stride = d.n_physical;
+    }
     L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
     L.nitems = g->nitems; L.nvars = (int)d.nvars; L.bk = (int)d.b_kDim; L.rlz = g->rlz;
+    return L;
+}
+size_t ring_item_smem(const ss_grid *g, const RingBucket &bkt, bool inverse) {
+    // the bucket sizes count 16 bytes per complex entry (binary64 and double-float)
+    const size_t f64 = inverse ? bkt.smem_inv_f64 : bkt.smem_fwd_f64;
+    return g->tl == TL_F32 ? f64 / 2 : f64;
+}
+SbLaunch sb_record(const ss_grid *g) {
+    const ss_dims &d = g->d;
+    SbLaunch S{};
+    S.F = g->F; S.spec = g->spec; S.spl = g->d_spl; S.fofs = g->d_fofs;
+    S.fw = g->filtered ? g->d_fw : nullptr;
+    S.cw = g->filtered ? g->d_cw : nullptr;
+    S.frows = g->frows; S.nspec = d.n_spectral;
+    S.iDim = (int)d.iDim; S.b = (int)d.b_iDim; S.mubar = g->p.mubar; S.pOL = g->pOL; S.K = (int)d.kDim_wn;
+    S.nslots_z = g->nslots_z; S.bk = (int)d.b_kDim; S.filtered = g->filtered;
+    return S;
+}
+SaLaunch sa_record(const ss_grid *g, int coeffs, size_t *smem_generic) {
+    const ss_dims &d = g->d;
+    SaLaunch A{};
+    A.spec = g->spec; A.G = g->G; A.spl = g->d_spl; A.fofs = g->d_fofs; A.ahat = g->d_ahat;
+    A.frows = g->frows; A.nspec = d.n_spectral; A.nblocks = d.n_blocks;
+    A.iDim = (int)d.iDim; A.b = (int)d.b_iDim; A.ld = (A.b % 2) ? A.b : A.b + 1;
+    A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = (int)d.b_kDim; A.nitems = g->nitems; A.coeffs = coeffs;
+    A.sx = (float *)g->sa_x; A.sy = (float *)g->sa_y;
+    int nmax = 0;
+    for (auto &sh : g->spl_host) nmax = std::max(nmax, sh.Min);
+    const size_t ssz = (g->tl == TL_F32) ? 4 : 8;  // solve type: float (FP32 mode) or double
+    size_t smem = (size_t(32) * A.ld + size_t(5) * nmax) * ssz;
+    if (g->tl != TL_F64) smem += size_t(32) * A.ld * ssz;  // FP32 residuals / df64 coefficients
+    if (smem_generic) *smem_generic = smem;
+    return A;
+}
+}  // namespace ss
+
+template <typename P, typename T>
+static int32_t fwd_rings(ss_grid *g, cudaStream_t st, int chunk) {
+    RingLaunch L = ring_record(g, false);
     StageScope sc(g, SS_STAGE_RING_FWD, st);
     return for_ring_segments(g, chunk, [&](const int *list, int count, const RingBucket &bkt) -> int32_t {
         L.ring_list = list;
-        size_t smem = (sizeof(T) == 8) ? bkt.smem_fwd_f64 : bkt.smem_fwd_f64 / 2;
+        const size_t smem = ring_item_smem(g, bkt, false);
         L.ib = ring_batch(smem, g->nitems, count, 4 * g->sms, g->ring_threads_fwd, bkt.max_buf);
         CUDA_TRY((launch_ring_forward<P, T>(L, count, g->nitems, smem, g->ring_threads_fwd, st)));
         g->launches[SS_STAGE_RING_FWD]++;
@@ -500,14 +545,7 @@ static int32_t fwd_rings(ss_grid *g, cudaStream_t st, int chunk) {
 
 template <typename P, typename T>
 static int32_t fwd_sb(ss_grid *g, cudaStream_t st) {
-    const ss_dims &d = g->d;
-    SbLaunch S{};
-    S.F = g->F; S.spec = g->spec; S.spl = g->d_spl; S.fofs = g->d_fofs;
-    S.fw = g->filtered ? g->d_fw : nullptr;
-    S.cw = g->filtered ? g->d_cw : nullptr;
-    S.frows = g->frows; S.nspec = d.n_spectral;
-    S.iDim = (int)d.iDim; S.b = (int)d.b_iDim; S.mubar = g->p.mubar; S.pOL = g->pOL; S.K = (int)d.kDim_wn;
-    S.nslots_z = g->nslots_z; S.bk = (int)d.b_kDim; S.filtered = g->filtered;
+    const SbLaunch S = sb_record(g);
     StageScope sc(g, SS_STAGE_SB, st);
     CUDA_TRY((launch_sb_project<P, T>(S, g->nitems, st)));
     g->launches[SS_STAGE_SB]++;
@@ -518,18 +556,13 @@ static int32_t fwd_sb(ss_grid *g, cudaStream_t st) {
 // (the 2-argument form: no R3X background) written as coefficients to `aout`
 template <typename P, typename T>
 static int32_t inv_sa(ss_grid *g, cudaStream_t st, int coeffs, const void *spec_in = nullptr, void *aout = nullptr) {
-    const ss_dims &d = g->d;
-    SaLaunch A{};
-    A.spec = spec_in ? spec_in : g->spec; A.G = g->G; A.spl = g->d_spl; A.fofs = g->d_fofs;
-    A.ahat = aout ? nullptr : g->d_ahat; A.aout = aout;
-    A.frows = g->frows; A.nspec = d.n_spectral; A.nblocks = d.n_blocks;
-    A.iDim = (int)d.iDim; A.b = (int)d.b_iDim; A.ld = (A.b % 2) ? A.b : A.b + 1;
-    A.pOL = g->pOL; A.nslots_z = g->nslots_z; A.bk = (int)d.b_kDim; A.nitems = g->nitems; A.coeffs = coeffs;
-    int nmax = 0;
-    for (auto &sh : g->spl_host) nmax = std::max(nmax, sh.Min);
-    const size_t ssz = (sizeof(T) == 4) ? 4 : 8;  // solve type: float (FP32 mode) or double
-    size_t smem = (size_t(32) * A.ld + size_t(5) * nmax) * ssz;
-    if (g->tl != TL_F64) smem += size_t(32) * A.ld * ssz;  // FP32 residuals / df64 coefficients
+    size_t smem = 0;
+    SaLaunch A = sa_record(g, coeffs, &smem);
+    if (spec_in) A.spec = spec_in;
+    if (aout) {
+        A.ahat = nullptr;
+        A.aout = aout;
+    }
     StageScope sc(g, SS_STAGE_SA_SI, st);
     if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
         if (aout) CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
@@ -543,19 +576,11 @@ static int32_t inv_sa(ss_grid *g, cudaStream_t st, int coeffs, const void *spec_
 
 template <typename P, typename T>
 static int32_t inv_rings(ss_grid *g, cudaStream_t st, int chunk) {
-    const ss_dims &d = g->d;
-    RingLaunch L{};
-    L.rings = g->d_rings;
-    L.ring_var_stride = g->rlz ? 0 : d.iDim;
-    L.plans = g->d_plans; L.pool = g->d_pool; L.phase = g->d_phase;
-    L.in = g->G;
-    L.out = g->rlz ? g->H : g->phys;
-    L.frows = g->frows; L.jDim = d.jDim; L.np = d.n_physical;
-    L.nitems = g->nitems; L.nvars = (int)d.nvars; L.bk = (int)d.b_kDim; L.rlz = g->rlz;
+    RingLaunch L = ring_record(g, true);
     StageScope sc(g, SS_STAGE_RING_INV, st);
     return for_ring_segments(g, chunk, [&](const int *list, int count, const RingBucket &bkt) -> int32_t {
         L.ring_list = list;
-        size_t sm = (sizeof(T) == 8) ? bkt.smem_inv_f64 : bkt.smem_inv_f64 / 2;
+        const size_t sm = ring_item_smem(g, bkt, true);
         L.ib = ring_batch(sm, g->nitems, count, 4 * g->sms, g->ring_threads_inv, bkt.max_buf);
         CUDA_TRY((launch_ring_inverse<P, T>(L, count, g->nitems, sm, g->ring_threads_inv, st)));
         g->launches[SS_STAGE_RING_INV]++;

@@ -25,6 +25,17 @@ using namespace ss;
     } while (0)
 
 // ====================================================================== batch
+// One launch of a fused batch: the CTAs of many grids' records of one stage
+// (one shared-memory class), each CTA running the record its work entry names.
+enum { FK_RING_FWD = 0, FK_SB = 1, FK_SA = 2, FK_SA_F32 = 3, FK_RING_INV = 4 };
+struct FusedLaunch {
+    int kind, tl;
+    size_t smem;
+    int threads, nwork;
+    const void *recs;       // RingLaunch / SbLaunch / SaLaunch records (device)
+    const BatchWork *work;  // one entry per CTA (device)
+};
+
 struct ss_batch {
     std::vector<ss_grid *> grids;
     int device = 0;
@@ -34,6 +45,13 @@ struct ss_batch {
     cudaGraph_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<uint64_t> gen[4];  // each grid's generation when graph[what] was captured
+    // fused mode: every RL grid's stages as a few launches over work lists
+    bool fused = false;
+    int ib_scale = 1;                   // items per ring CTA × this (autotuned)
+    std::vector<FusedLaunch> fwd, inv;  // in launch order
+    std::vector<ss_grid *> unfused;     // RLZ grids: their own launch sequences
+    std::vector<void *> fused_mem;
+    std::vector<uint64_t> fused_gen;    // generations the records were built from
 };
 
 // The grids' generation counters; a graph whose grids have changed since (ahat registered or cleared, filter set) is captured again,
@@ -85,6 +103,236 @@ static int32_t autotune_grid(ss_grid *g, cudaStream_t st) {
     return SS_OK;
 }
 
+// ---- fused plan
+// shared-memory classes of the fused ring and SA launches: a CTA's dynamic
+// shared memory is its class's largest, so records of similar size share a launch
+static const size_t kSmemClass[] = {12 << 10, 24 << 10, 48 << 10, 72 << 10, 100 << 10, 140 << 10, 227 << 10};
+static int smem_class(size_t b) {
+    for (int c = 0; c < (int)(sizeof kSmemClass / sizeof kSmemClass[0]); c++)
+        if (b <= kSmemClass[c]) return c;
+    return -1;
+}
+
+static void free_fused(ss_batch *bt) {
+    for (void *p : bt->fused_mem) cudaFree(p);
+    bt->fused_mem.clear();
+    bt->fwd.clear();
+    bt->inv.clear();
+    bt->unfused.clear();
+}
+
+template <typename R>
+static int32_t upload(ss_batch *bt, const std::vector<R> &v, const void **out) {
+    void *p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(R)));
+    bt->fused_mem.push_back(p);
+    CUDA_TRY(cudaMemcpy(p, v.data(), v.size() * sizeof(R), cudaMemcpyHostToDevice));
+    *out = p;
+    return SS_OK;
+}
+
+// ring stage of every grid of one compute layout: one record per (grid, bucket),
+// CTAs grouped by (shared-memory class, CTA size), largest rings first
+static int32_t plan_rings(ss_batch *bt, const std::vector<ss_grid *> &gs, int tl, bool inverse,
+                          std::vector<FusedLaunch> &out) {
+    struct Rec { RingLaunch L; size_t smem; int threads, nrings, nb, buf; };
+    std::vector<Rec> recs;
+    for (ss_grid *g : gs)
+        for (const RingBucket &bkt : g->buckets) {
+            Rec r;
+            r.L = ring_record(g, inverse);
+            r.L.ring_list = g->d_ring_list + bkt.offset;
+            r.threads = inverse ? g->ring_threads_inv : g->ring_threads_fwd;
+            const size_t per = ring_item_smem(g, bkt, inverse);
+            int ib = ring_batch(per, g->nitems, bkt.count, 1, r.threads, bkt.max_buf) * bt->ib_scale;
+            ib = std::max(1, std::min({ib, kRingBatchMax, g->nitems}));
+            while (ib > 1 && per * ib > kSmemClass[6]) ib--;
+            r.L.ib = ib;
+            r.smem = per * ib;
+            r.nrings = bkt.count;
+            r.nb = (g->nitems + ib - 1) / ib;
+            r.buf = bkt.max_buf;
+            if (smem_class(r.smem) < 0) {
+                set_error("a ring of the batch needs %zu bytes of shared memory", r.smem);
+                return SS_BAD_SHAPE;
+            }
+            recs.push_back(r);
+        }
+    std::vector<RingLaunch> L;
+    for (const Rec &r : recs) L.push_back(r.L);
+    const void *d_recs = nullptr;
+    int32_t rc = upload(bt, L, &d_recs);
+    if (rc) return rc;
+    std::vector<int> order(recs.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return recs[a].buf > recs[b].buf; });
+    for (int c = 0; c < 7; c++)
+        for (int threads : {64, 128, 256}) {
+            std::vector<BatchWork> work;
+            size_t smem = 0;
+            for (int i : order) {
+                const Rec &r = recs[i];
+                if (smem_class(r.smem) != c || r.threads != threads) continue;
+                smem = std::max(smem, r.smem);
+                for (int ring = 0; ring < r.nrings; ring++)
+                    for (int bx = 0; bx < r.nb; bx++) work.push_back({i, bx, ring, 0});
+            }
+            if (work.empty()) continue;
+            FusedLaunch f{inverse ? FK_RING_INV : FK_RING_FWD, tl, smem, threads, (int)work.size(), d_recs, nullptr};
+            const void *w = nullptr;
+            if ((rc = upload(bt, work, &w))) return rc;
+            f.work = (const BatchWork *)w;
+            out.push_back(f);
+        }
+    return SS_OK;
+}
+
+static int32_t plan_sb(ss_batch *bt, const std::vector<ss_grid *> &gs, int tl, std::vector<FusedLaunch> &out) {
+    std::vector<SbLaunch> L;
+    std::vector<BatchWork> work;
+    for (ss_grid *g : gs) {
+        const int i = (int)L.size();
+        L.push_back(sb_record(g));
+        const SbLaunch &S = L.back();
+        for (int bz = 0; bz < g->nitems; bz++)
+            for (int by = 0; by < (S.b + 63) / 64; by++)
+                for (int bx = 0; bx < (S.nslots_z + 31) / 32; bx++) work.push_back({i, bx, by, bz});
+    }
+    const void *d_recs = nullptr, *w = nullptr;
+    int32_t rc = upload(bt, L, &d_recs);
+    if (!rc) rc = upload(bt, work, &w);
+    if (rc) return rc;
+    out.push_back({FK_SB, tl, 0, 256, (int)work.size(), d_recs, (const BatchWork *)w});
+    return SS_OK;
+}
+
+static int32_t plan_sa(ss_batch *bt, const std::vector<ss_grid *> &gs, int tl, std::vector<FusedLaunch> &out) {
+    std::vector<SaLaunch> L;
+    std::vector<size_t> smem;
+    for (ss_grid *g : gs) {
+        size_t sm = 0;
+        L.push_back(sa_record(g, 0, &sm));
+        smem.push_back(sm);
+    }
+    const void *d_recs = nullptr;
+    int32_t rc = upload(bt, L, &d_recs);
+    if (rc) return rc;
+    if (tl == TL_F32) {  // slot-parallel binary32 solve: no dynamic shared memory
+        std::vector<BatchWork> work;
+        for (int i = 0; i < (int)gs.size(); i++)
+            for (int by = 0; by < gs[i]->nitems; by++)
+                for (int bx = 0; bx < (L[i].nslots_z + 127) / 128; bx++) work.push_back({i, bx, by, 0});
+        const void *w = nullptr;
+        if ((rc = upload(bt, work, &w))) return rc;
+        out.push_back({FK_SA_F32, tl, 0, 128, (int)work.size(), d_recs, (const BatchWork *)w});
+        return SS_OK;
+    }
+    for (int c = 0; c < 7; c++) {
+        std::vector<BatchWork> work;
+        size_t sm = 0;
+        for (int i = 0; i < (int)gs.size(); i++) {
+            if (smem_class(smem[i]) != c) continue;
+            sm = std::max(sm, smem[i]);
+            for (int by = 0; by < gs[i]->nitems; by++)
+                for (int bx = 0; bx < (L[i].nslots_z + 31) / 32; bx++) work.push_back({i, bx, by, 0});
+        }
+        if (work.empty()) continue;
+        const void *w = nullptr;
+        if ((rc = upload(bt, work, &w))) return rc;
+        out.push_back({FK_SA, tl, sm, 128, (int)work.size(), d_recs, (const BatchWork *)w});
+    }
+    for (size_t i = 0; i < smem.size(); i++)
+        if (smem_class(smem[i]) < 0) {
+            set_error("a spline solve of the batch needs %zu bytes of shared memory", smem[i]);
+            return SS_BAD_SHAPE;
+        }
+    return SS_OK;
+}
+
+static std::vector<uint64_t> generations(const ss_batch *bt);
+static int32_t build_fused(ss_batch *bt) {
+    free_fused(bt);
+    for (int tl : {TL_F64, TL_DF64, TL_F32}) {
+        std::vector<ss_grid *> gs;
+        for (ss_grid *g : bt->grids)
+            if (!g->rlz && g->tl == tl) gs.push_back(g);
+        if (gs.empty()) continue;
+        int32_t rc = plan_rings(bt, gs, tl, false, bt->fwd);
+        if (!rc) rc = plan_sb(bt, gs, tl, bt->fwd);
+        if (!rc) rc = plan_sa(bt, gs, tl, bt->inv);
+        if (!rc) rc = plan_rings(bt, gs, tl, true, bt->inv);
+        if (rc) { free_fused(bt); return rc; }
+    }
+    for (ss_grid *g : bt->grids)
+        if (g->rlz) bt->unfused.push_back(g);
+    bt->fused_gen = generations(bt);
+    return SS_OK;
+}
+
+template <typename P, typename T>
+static cudaError_t fused_launch(const FusedLaunch &f, cudaStream_t st) {
+    switch (f.kind) {
+    case FK_RING_FWD:
+        return launch_ring_forward_fused<P, T>((const RingLaunch *)f.recs, f.work, f.nwork, f.smem, f.threads, st);
+    case FK_RING_INV:
+        return launch_ring_inverse_fused<P, T>((const RingLaunch *)f.recs, f.work, f.nwork, f.smem, f.threads, st);
+    case FK_SB: return launch_sb_project_fused<P, T>((const SbLaunch *)f.recs, f.work, f.nwork, st);
+    case FK_SA: return launch_sa_si_fused<P, T>((const SaLaunch *)f.recs, f.work, f.nwork, f.smem, st);
+    default:
+        if constexpr (std::is_same<P, float>::value)
+            return launch_sa_si_f32_fused<P>((const SaLaunch *)f.recs, f.work, f.nwork, st);
+        return cudaErrorInvalidValue;
+    }
+}
+
+static int32_t enqueue_fused(ss_batch *bt, int what, cudaStream_t st) {
+    for (int dir = 1; dir <= 2; dir++) {
+        if (!(what & dir)) continue;
+        for (const FusedLaunch &f : dir == 1 ? bt->fwd : bt->inv) {
+            cudaError_t e = f.tl == TL_F64 ? fused_launch<double, double>(f, st)
+                            : f.tl == TL_DF64 ? fused_launch<double, df64>(f, st)
+                                              : fused_launch<float, float>(f, st);
+            CUDA_TRY(e);
+        }
+        for (ss_grid *g : bt->unfused) {
+            int32_t r = run_direction(g, dir, st);
+            if (r) return r;
+        }
+    }
+    return SS_OK;
+}
+
+// Autotuner of the fused plan: CTA size of the ring kernels and items per ring
+// CTA, timed on the batch's own data (both directions); the fastest is kept.
+static int32_t autotune_fused(ss_batch *bt, cudaStream_t st) {
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    float best = 1e30f;
+    int best_t = -1, best_s = 1;
+    for (int threads : {128, 256})
+        for (int scale : {1, 2}) {
+            for (ss_grid *g : bt->grids) g->ring_threads_fwd = g->ring_threads_inv = threads;
+            bt->ib_scale = scale;
+            int32_t r = build_fused(bt);
+            if (!r) r = enqueue_fused(bt, 3, st);  // warm-up
+            if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
+            CUDA_TRY(cudaEventRecord(a, st));
+            for (int rep = 0; rep < 2 && !r; rep++) r = enqueue_fused(bt, 3, st);
+            CUDA_TRY(cudaEventRecord(b, st));
+            CUDA_TRY(cudaEventSynchronize(b));
+            if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
+            float ms = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+            if (ms < best) { best = ms; best_t = threads; best_s = scale; }
+        }
+    for (ss_grid *g : bt->grids) g->ring_threads_fwd = g->ring_threads_inv = best_t;
+    bt->ib_scale = best_s;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return build_fused(bt);
+}
+
 extern "C" int32_t ss_batch_destroy(ss_batch *bt);
 extern "C" int32_t ss_batch_create(ss_grid *const *grids, int32_t n, int32_t flags, ss_batch **out) {
     if (!out || !grids || n < 1) { set_error("bad batch arguments"); return SS_BAD_ARG; }
@@ -112,7 +360,13 @@ extern "C" int32_t ss_batch_create(ss_grid *const *grids, int32_t n, int32_t fla
         cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         bt->ev.push_back(e);
     }
-    if (flags & 1) {
+    bt->fused = (flags & SS_BATCH_FUSED) != 0;
+    if (bt->fused) {
+        for (ss_grid *g : bt->grids)
+            if (g->profiling) { ss_batch_destroy(bt); set_error("disable stage profiling on batched grids"); return SS_BAD_ARG; }
+        int32_t r = (flags & SS_BATCH_AUTOTUNE) ? autotune_fused(bt, bt->stream) : build_fused(bt);
+        if (r) { ss_batch_destroy(bt); return r; }
+    } else if (flags & SS_BATCH_AUTOTUNE) {
         for (ss_grid *g : bt->grids) {
             int32_t r = autotune_grid(g, bt->stream);
             if (r) { ss_batch_destroy(bt); return r; }
@@ -132,6 +386,7 @@ extern "C" int32_t ss_batch_destroy(ss_batch *bt) {
     }
     for (cudaStream_t s : bt->side) cudaStreamDestroy(s);
     for (cudaEvent_t e : bt->ev) cudaEventDestroy(e);
+    free_fused(bt);
     cudaStreamDestroy(bt->stream);
     delete bt;
     return SS_OK;
@@ -160,7 +415,13 @@ extern "C" int32_t ss_batch_run(ss_batch *bt, int32_t what, int32_t use_graph, v
     cudaStream_t st = stream ? (cudaStream_t)stream : bt->stream;
     for (ss_grid *g : bt->grids)
         if (g->profiling) { set_error("disable stage profiling on batched grids"); return SS_BAD_ARG; }
-    if (!use_graph) return enqueue_batch(bt, what, st);
+    if (bt->fused && bt->fused_gen != generations(bt)) {  // records hold the old ahat pointer / filter flag
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(cudaStreamSynchronize(bt->stream));
+        int32_t r = build_fused(bt);
+        if (r) return r;
+    }
+    if (!use_graph) return bt->fused ? enqueue_fused(bt, what, st) : enqueue_batch(bt, what, st);
     if (bt->exec[what] && bt->gen[what] != generations(bt)) {
         CUDA_TRY(cudaStreamSynchronize(st));  // a replay in flight still uses the old graph
         cudaGraphExecDestroy(bt->exec[what]);
@@ -171,7 +432,7 @@ extern "C" int32_t ss_batch_run(ss_batch *bt, int32_t what, int32_t use_graph, v
     if (!bt->exec[what]) {
         // capture on the batch's own stream, then launch the graph on `st`
         CUDA_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeRelaxed));
-        int32_t r = enqueue_batch(bt, what, bt->stream);
+        int32_t r = bt->fused ? enqueue_fused(bt, what, bt->stream) : enqueue_batch(bt, what, bt->stream);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(bt->stream, &graph);
         if (r) { if (graph) cudaGraphDestroy(graph); return r; }
@@ -188,6 +449,12 @@ extern "C" int32_t ss_batch_synchronize(ss_batch *bt) {
     if (!bt) { set_error("null batch"); return SS_BAD_ARG; }
     cudaSetDevice(bt->device);
     CUDA_TRY(cudaStreamSynchronize(bt->stream));
+    return SS_OK;
+}
+
+extern "C" int32_t ss_batch_fused_launches(const ss_batch *bt, int32_t what, int32_t *launches) {
+    if (!bt || !launches || what < 1 || what > 3) { set_error("bad batch query"); return SS_BAD_ARG; }
+    *launches = (int32_t)(((what & 1) ? bt->fwd.size() : 0) + ((what & 2) ? bt->inv.size() : 0));
     return SS_OK;
 }
 

@@ -116,3 +116,15 @@ int32_t grid_inverse(ss_grid *g, cudaStream_t st);
 // SI + ring (+ column) stages only: the spectral array holds spline coefficients a
 int32_t grid_inverse_coeffs(ss_grid *g, cudaStream_t st);
 }  // namespace ss
+
+namespace ss {
+struct RingLaunch;
+struct SbLaunch;
+struct SaLaunch;
+// launch records of one grid's stages (ring_list and ib are set per launch;
+// the record types are defined in ss_kernels.h)
+RingLaunch ring_record(const ss_grid *g, bool inverse);
+size_t ring_item_smem(const ss_grid *g, const RingBucket &bkt, bool inverse);
+SbLaunch sb_record(const ss_grid *g);
+SaLaunch sa_record(const ss_grid *g, int coeffs, size_t *smem_generic);
+}  // namespace ss

@@ -77,11 +77,11 @@ constexpr int kSweepSeqs = 1;
 // for the binary32 400-cell grid, 4% for the binary64 200-cell grid).
 // ====================================================================
 template <typename P, typename T>
-__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(RingLaunch L) {
+__device__ __forceinline__ void ring_forward_body(const RingLaunch &L, const int bx, const int by) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int kmx[kRingBatchMax];
-    const int ring = L.ring_list[blockIdx.y];  // consecutive CTAs: item batches of one ring
-    const int item0 = blockIdx.x * L.ib;
+    const int ring = L.ring_list[by];  // consecutive CTAs: item batches of one ring
+    const int item0 = bx * L.ib;
     const int nb = min(L.ib, L.nitems - item0);
     const RingDesc rd = L.rings[(size_t)(L.rlz ? 0 : item0) * L.ring_var_stride + ring];
     const FftPlan &pl = L.plans[rd.plan];
@@ -149,6 +149,11 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(Ri
     }
 }
 
+template <typename P, typename T>
+__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(RingLaunch L) {
+    ring_forward_body<P, T>(L, blockIdx.x, blockIdx.y);
+}
+
 // ====================================================================
 // ring_inverse: one CTA per (ring, batch of items).  For d = 0 (value), 1 (∂r),
 // 2 (∂rr) read the ring's coefficient rows, undo the phase rotation
@@ -156,11 +161,11 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_kernel(Ri
 // d=2 → ∂rr.
 // ====================================================================
 template <typename P, typename T>
-__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(RingLaunch L) {
+__device__ __forceinline__ void ring_inverse_body(const RingLaunch &L, const int bx, const int by) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int kmx[kRingBatchMax];
-    const int ring = L.ring_list[blockIdx.y];  // consecutive CTAs: item batches of one ring
-    const int item0 = blockIdx.x * L.ib;
+    const int ring = L.ring_list[by];  // consecutive CTAs: item batches of one ring
+    const int item0 = bx * L.ib;
     const int nb = min(L.ib, L.nitems - item0);
     const RingDesc rd = L.rings[(size_t)(L.rlz ? 0 : item0) * L.ring_var_stride + ring];
     const FftPlan &pl = L.plans[rd.plan];
@@ -258,16 +263,21 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(Ri
     }
 }
 
+template <typename P, typename T>
+__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(RingLaunch L) {
+    ring_inverse_body<P, T>(L, blockIdx.x, blockIdx.y);
+}
+
 // ====================================================================
 // sb_project: spectral[(zb*(1+2K) + s)*b + mi] = Σ_taps w(mi,tap) F[row][s]
 // block (32 slots, 8 rows of outputs); 64 outputs per CTA in mi
 // ====================================================================
 template <typename P, typename T>
-__global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch S) {
+__device__ __forceinline__ void sb_project_body(const SbLaunch &S, const int bx, const int by, const int bz) {
     __shared__ T tile[32][65];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int s0 = blockIdx.x * 32, m0 = blockIdx.y * 64;
-    const int item = blockIdx.z;
+    const int s0 = bx * 32, m0 = by * 64;
+    const int item = bz;
     const int v = item / S.bk, zb = item % S.bk;
     const int s = s0 + tx;
     const SplineDev &sp = S.spl[v];
@@ -307,6 +317,11 @@ __global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch S) {
     }
 }
 
+template <typename P, typename T>
+__global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch S) {
+    sb_project_body<P, T>(S, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // ====================================================================
 // sa_si: per 32-slot tile, SAtransform! (src/CubicBSpline.jl:1368-1396)
 //   FP64 modes: Γ b → L⁻ᵀL⁻¹ → Γᵀ (+ahat) in binary64;
@@ -317,11 +332,11 @@ __global__ void __launch_bounds__(256) sb_project_kernel(SbLaunch S) {
 // then the 4-tap SI/SIx/SIxx at the mish points in the compute type.
 // ====================================================================
 template <typename P, typename T>
-__global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
+__device__ __forceinline__ void sa_si_body(const SaLaunch &A, const int bx, const int by) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr bool kF32 = std::is_same<T, float>::value;
     using S = typename std::conditional<kF32, float, double>::type;  // solve type
-    const int item = blockIdx.y;
+    const int item = by;
     const int v = item / A.bk, zb = item % A.bk;
     const SplineDev &sp = A.spl[v];
     const int b = A.b, ld = A.ld, n = sp.Min;
@@ -331,7 +346,7 @@ __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
     S *R = Di + n;                           // 32 × ld: FP32 residuals / df64 coefficients for SI
     constexpr bool kSameX = kF32 || std::is_same<T, double>::value;
     T *XT = kSameX ? reinterpret_cast<T *>(X) : reinterpret_cast<T *>(R);
-    const int s0 = blockIdx.x * 32;
+    const int s0 = bx * 32;
     const P *spec = (const P *)A.spec + (size_t)v * A.nspec + ((size_t)zb * A.nslots_z + s0) * b;
     const int nsl = min(32, A.nslots_z - s0);
     for (int e = threadIdx.x; e < nsl * b; e += blockDim.x) X[(e / b) * ld + (e % b)] = (S)spec[e];
@@ -426,6 +441,11 @@ __global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
             ((T *)A.G)[((size_t)d * A.nitems + item) * A.frows + orow] = u;
         }
     }
+}
+
+template <typename P, typename T>
+__global__ void __launch_bounds__(128) sa_si_kernel(SaLaunch A) {
+    sa_si_body<P, T>(A, blockIdx.x, blockIdx.y);
 }
 
 // ====================================================================
@@ -698,10 +718,248 @@ __global__ void __launch_bounds__(128) cheb_inverse_m_kernel(ChebLaunch C) {
     }
 }
 
+// TJ consecutive values from registers to global memory: 16-byte stores when the
+// run is 16-byte aligned (`vec`), else one store per value
+template <typename P, int TJ>
+__device__ __forceinline__ void store_run(P *dst, const P (&u)[TJ], bool vec) {
+    if constexpr ((TJ * sizeof(P)) % 16 == 0) {
+        if (vec) {
+#pragma unroll
+            for (int q = 0; q < TJ * (int)sizeof(P) / 16; q++) {
+                if constexpr (sizeof(P) == 4)
+                    reinterpret_cast<float4 *>(dst)[q] = make_float4(u[4 * q], u[4 * q + 1], u[4 * q + 2], u[4 * q + 3]);
+                else
+                    reinterpret_cast<double2 *>(dst)[q] = make_double2(u[2 * q], u[2 * q + 1]);
+            }
+            return;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < TJ; i++) dst[i] = u[i];
+}
+
+// ====================================================================
+// cheb_inverse, persistent: the same composed matrices u = M_d b as
+// cheb_inverse_m_kernel, with M_0, M_1, M_2 of both output halves resident in
+// shared memory for the CTA's life.  grid = (CTAs per variable, variables);
+// each CTA walks work items (64-column block, ring variant), variants fastest,
+// and gathers the next item's bk ring outputs (16-byte cp.async: four binary32
+// or two binary64 columns of one ring row per copy) into the second buffer
+// while it computes the current one.  The register tiles are TJ z-outputs ×
+// TC columns, consecutive threads on consecutive z, so each u[j] run and its
+// mirror u[N−1−j] leave registers as 16-byte stores covering whole sectors.
+// Summation order per output is that of cheb_inverse_m_kernel (bit-identical).
+// ====================================================================
+template <typename P, typename T>
+__global__ void __launch_bounds__(128) cheb_inverse_p_kernel(ChebLaunch C) {
+    // binary64 columns are short (kz = 32: JT = 4): 2-column tiles keep all 128
+    // threads busy; binary32 (kz = 64: JT = 8) takes 4-column tiles
+    constexpr int COLS = 64, TJ = 4, TC = std::is_same<T, float>::value ? 4 : 2, CT = COLS / TC;
+    constexpr int VEC = 16 / (int)sizeof(T);  // compute-type values per 16-byte copy
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int64_t col_base[COLS / VEC];
+    __shared__ int col_L[COLS / VEC];
+    const int v = blockIdx.y;
+    const ChebDev &cb = C.cheb[v];
+    const int N = cb.N, bk = cb.bk, half = cb.half;
+    const int JT = (half + TJ - 1) / TJ, JP = JT * TJ;
+    const int nr = cb.nrank, ke = (bk + 1) / 2, ko = bk / 2, Ke = ke + nr, Ko = ko + nr;
+    const int kcap = cb.kcap;
+    T *ms = reinterpret_cast<T *>(smem_raw);    // [d][pe][kcap][JP]
+    T *xbuf = ms + (size_t)6 * kcap * JP;       // 2 × [(Ke + Ko) × COLS]: even rows, then odd rows
+    const int XS = (Ke + Ko) * COLS;
+    const int64_t nblk = (C.col1 - C.col0 + COLS - 1) / COLS;
+    const int64_t nitem = ((nblk - blockIdx.x + gridDim.x - 1) / gridDim.x) * 5;  // this CTA's items
+    if (blockIdx.x >= nblk) return;
+    constexpr int VP = 16 / (int)sizeof(P);
+    const bool vec_ok = (N % VP) == 0 && (C.np % VP) == 0;
+    {
+        const int nm = 6 * kcap * JP;  // kcap·JP is a multiple of 4 entries: 16-byte rows
+        const T *src = (const T *)cb.inv_m_t;
+        for (int e = threadIdx.x * VEC; e < nm; e += blockDim.x * VEC) cp_async<16>(ms + e, src + e);
+    }
+    // column metadata of a block (one entry per VEC-column group: a group never
+    // straddles a ring, whose starts and lengths are multiples of 4)
+    auto meta = [&](int64_t blk) {
+        const int64_t c0 = C.col0 + blk * COLS;
+        for (int g = threadIdx.x; g < COLS / VEC; g += blockDim.x) {
+            const int64_t q = c0 + (int64_t)g * VEC;
+            if (q < C.col1) {
+                const RingDesc &rd = C.rings[C.col_ring[q]];
+                col_base[g] = (int64_t)C.bk * rd.jofs + (q - rd.jofs);
+                col_L[g] = rd.L;
+            }
+        }
+    };
+    auto gather = [&](int64_t blk, int var, T *xb) {
+        const int64_t c0 = C.col0 + blk * COLS;
+        const int ng = (int)(((C.col1 - c0) < COLS ? (C.col1 - c0) : COLS) / VEC);
+        const T *H = (const T *)C.in + ((size_t)var * C.nvars + v) * C.bk * C.jDim;
+        for (int e = threadIdx.x; e < bk * (COLS / VEC); e += blockDim.x) {
+            const int zb = e / (COLS / VEC), g = e % (COLS / VEC);
+            T *dst = xb + ((zb & 1) ? (size_t)(Ke + (zb >> 1)) * COLS : (size_t)(zb >> 1) * COLS) + g * VEC;
+            if (g < ng) {
+                cp_async<16>(dst, H + col_base[g] + (int64_t)zb * col_L[g]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < VEC; q++) dst[q] = T(0.0f);
+            }
+        }
+    };
+    meta(blockIdx.x);
+    __syncthreads();
+    gather(blockIdx.x, 0, xbuf);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    for (int64_t it = 0; it < nitem; it++) {
+        const int64_t blk = blockIdx.x + (it / 5) * gridDim.x;
+        const int var = (int)(it % 5);
+        T *xb = xbuf + (size_t)(it & 1) * XS;
+        T *xe = xb, *xo = xb + (size_t)Ke * COLS;
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();  // item it's inputs (and, at first, the matrices) are in; item it−1 is done
+        // s_p = Σ_i gu[p][i] b_i (the rank term of the Γ fold), appended to both input sets
+        for (int t = threadIdx.x; t < COLS * nr; t += blockDim.x) {
+            const int c = t % COLS, p = t / COLS;
+            const int64_t g0 = (int64_t)p * bk;
+            T se = T(0.0f), so = T(0.0f);
+            for (int i2 = 0; 2 * i2 < bk; i2++) {
+                se = se + ld_real<T>(cb.gu_t, g0 + 2 * i2) * xe[(size_t)i2 * COLS + c];
+                if (2 * i2 + 1 < bk) so = so + ld_real<T>(cb.gu_t, g0 + 2 * i2 + 1) * xo[(size_t)i2 * COLS + c];
+            }
+            const T acc = se + so;
+            xe[(size_t)(ke + p) * COLS + c] = acc;
+            xo[(size_t)(ko + p) * COLS + c] = acc;
+        }
+        const bool more = it + 1 < nitem;
+        const int64_t nblk_next = blockIdx.x + ((it + 1) / 5) * gridDim.x;
+        if (more && nblk_next != blk) meta(nblk_next);
+        __syncthreads();  // rank rows and the next block's metadata are visible
+        if (more) gather(nblk_next, (int)((it + 1) % 5), xbuf + (size_t)((it + 1) & 1) * XS);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+
+        const int64_t c0 = C.col0 + blk * COLS;
+        const int ncol = (int)((C.col1 - c0) < COLS ? (C.col1 - c0) : COLS);
+        const int nd = (var == 0) ? 3 : 1;
+        for (int dd = 0; dd < nd; dd++) {
+            const T *me = ms + (size_t)(2 * dd) * kcap * JP, *mo = me + (size_t)kcap * JP;
+            const T *ie = (dd & 1) ? xo : xe, *io = (dd & 1) ? xe : xo;
+            const int Kie = (dd & 1) ? Ko : Ke, Kio = (dd & 1) ? Ke : Ko;
+            int slot;
+            if (var == 0) slot = (dd == 0) ? 1 : (dd == 1 ? 6 : 7);
+            else slot = (var == 1) ? 4 : (var == 2 ? 5 : (var == 3 ? 2 : 3));
+            P *dst = (P *)C.out + ((size_t)(slot - 1) * C.nvars + v) * C.np + c0 * N;
+            for (int t = threadIdx.x; t < JT * CT; t += blockDim.x) {
+                const int jt = t % JT, ct = t / JT;
+                const int j0 = jt * TJ, cc = ct * TC;
+                if (cc >= ncol) continue;
+                T E[TJ][TC], O[TJ][TC];
+#pragma unroll
+                for (int i = 0; i < TJ; i++)
+#pragma unroll
+                    for (int c = 0; c < TC; c++) { E[i][c] = T(0.0f); O[i][c] = T(0.0f); }
+                for (int k = 0; k < Kie; k++) {
+                    T w[TJ], b[TC];
+                    load_row<T, TJ>(me + (size_t)k * JP + j0, w);
+                    load_row<T, TC>(ie + (size_t)k * COLS + cc, b);
+#pragma unroll
+                    for (int i = 0; i < TJ; i++)
+#pragma unroll
+                        for (int c = 0; c < TC; c++) E[i][c] = E[i][c] + w[i] * b[c];
+                }
+                for (int k = 0; k < Kio; k++) {
+                    T w[TJ], b[TC];
+                    load_row<T, TJ>(mo + (size_t)k * JP + j0, w);
+                    load_row<T, TC>(io + (size_t)k * COLS + cc, b);
+#pragma unroll
+                    for (int i = 0; i < TJ; i++)
+#pragma unroll
+                        for (int c = 0; c < TC; c++) O[i][c] = O[i][c] + w[i] * b[c];
+                }
+                // whole run below the middle: u[j0..j0+TJ) and its mirror as two runs
+                const bool full = j0 + TJ <= N - (j0 + TJ) && j0 + TJ <= half;
+#pragma unroll
+                for (int c = 0; c < TC; c++) {
+                    if (cc + c >= ncol) break;
+                    P *u = dst + (size_t)(cc + c) * N;
+                    if (full) {
+                        P lo[TJ], hi[TJ];
+#pragma unroll
+                        for (int i = 0; i < TJ; i++) {
+                            lo[i] = to_storage<P>(E[i][c] + O[i][c]);
+                            hi[TJ - 1 - i] = to_storage<P>(E[i][c] - O[i][c]);
+                        }
+                        store_run<P, TJ>(u + j0, lo, vec_ok);
+                        store_run<P, TJ>(u + (N - TJ - j0), hi, vec_ok);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < TJ; i++) {
+                            const int j = j0 + i;
+                            if (j >= half) break;
+                            u[j] = to_storage<P>(E[i][c] + O[i][c]);
+                            if (N - 1 - j != j) u[N - 1 - j] = to_storage<P>(E[i][c] - O[i][c]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+template <typename T>
+size_t cheb_inverse_p_smem(int N, int bk) {  // rank of the Γ fold ≤ 2
+    const size_t kcap = (size_t)(bk + 1) / 2 + 2, jp = (size_t)cheb_pad4((N + 1) / 2);
+    const size_t kk = (size_t)(bk + 1) / 2 + bk / 2 + 4;
+    return (6 * kcap * jp + 2 * kk * 64) * sizeof(T);
+}
+
 template <typename T>
 size_t cheb_inverse_m_smem(int N, int bk) {  // rank of the Γ fold ≤ 2: two s rows per input set
     const size_t kcap = (size_t)(bk + 1) / 2 + 2, jp = (size_t)cheb_pad4((N + 1) / 2);
     return ((size_t)(bk + 4) * 64 + (size_t)64 * (N | 1) + 2 * kcap * jp) * sizeof(T);
+}
+
+// ====================================================================
+// fused multi-grid launches: CTA blockIdx.x runs work[blockIdx.x], the launch
+// record it names staged in shared memory (one 4-byte word per thread)
+// ====================================================================
+template <typename R>
+__device__ __forceinline__ void load_record(R &dst, const R *src) {
+    static_assert(sizeof(R) % 4 == 0, "launch records are whole 4-byte words");
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x, nt = blockDim.x * blockDim.y;
+    for (int i = tid; i < (int)(sizeof(R) / 4); i += nt)
+        reinterpret_cast<int *>(&dst)[i] = __ldg(reinterpret_cast<const int *>(src) + i);
+    __syncthreads();
+}
+template <typename P, typename T>
+__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_forward_fused_kernel(const RingLaunch *recs,
+                                                                                    const BatchWork *work) {
+    __shared__ __align__(16) RingLaunch L;
+    const BatchWork w = work[blockIdx.x];
+    load_record(L, recs + w.rec);
+    ring_forward_body<P, T>(L, w.bx, w.by);
+}
+template <typename P, typename T>
+__global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_fused_kernel(const RingLaunch *recs,
+                                                                                    const BatchWork *work) {
+    __shared__ __align__(16) RingLaunch L;
+    const BatchWork w = work[blockIdx.x];
+    load_record(L, recs + w.rec);
+    ring_inverse_body<P, T>(L, w.bx, w.by);
+}
+template <typename P, typename T>
+__global__ void __launch_bounds__(256) sb_project_fused_kernel(const SbLaunch *recs, const BatchWork *work) {
+    __shared__ __align__(16) SbLaunch S;
+    const BatchWork w = work[blockIdx.x];
+    load_record(S, recs + w.rec);
+    sb_project_body<P, T>(S, w.bx, w.by, w.bz);
+}
+template <typename P, typename T>
+__global__ void __launch_bounds__(128) sa_si_fused_kernel(const SaLaunch *recs, const BatchWork *work) {
+    __shared__ __align__(16) SaLaunch A;
+    const BatchWork w = work[blockIdx.x];
+    load_record(A, recs + w.rec);
+    sa_si_body<P, T>(A, w.bx, w.by);
 }
 
 // ====================================================================
@@ -755,6 +1013,35 @@ cudaError_t launch_ring_inverse(const RingLaunch &L0, int nrings, int nitems, si
     return cudaGetLastError();
 }
 template <typename P, typename T>
+cudaError_t launch_ring_forward_fused(const RingLaunch *recs, const BatchWork *work, int nwork, size_t smem,
+                                      int threads, cudaStream_t st) {
+    if (nwork <= 0) return cudaSuccess;
+    set_smem(ring_forward_fused_kernel<P, T>, smem);
+    ring_forward_fused_kernel<P, T><<<nwork, threads, smem, st>>>(recs, work);
+    return cudaGetLastError();
+}
+template <typename P, typename T>
+cudaError_t launch_ring_inverse_fused(const RingLaunch *recs, const BatchWork *work, int nwork, size_t smem,
+                                      int threads, cudaStream_t st) {
+    if (nwork <= 0) return cudaSuccess;
+    set_smem(ring_inverse_fused_kernel<P, T>, smem);
+    ring_inverse_fused_kernel<P, T><<<nwork, threads, smem, st>>>(recs, work);
+    return cudaGetLastError();
+}
+template <typename P, typename T>
+cudaError_t launch_sb_project_fused(const SbLaunch *recs, const BatchWork *work, int nwork, cudaStream_t st) {
+    if (nwork <= 0) return cudaSuccess;
+    sb_project_fused_kernel<P, T><<<nwork, dim3(32, 8), 0, st>>>(recs, work);
+    return cudaGetLastError();
+}
+template <typename P, typename T>
+cudaError_t launch_sa_si_fused(const SaLaunch *recs, const BatchWork *work, int nwork, size_t smem, cudaStream_t st) {
+    if (nwork <= 0) return cudaSuccess;
+    set_smem(sa_si_fused_kernel<P, T>, smem);
+    sa_si_fused_kernel<P, T><<<nwork, 128, smem, st>>>(recs, work);
+    return cudaGetLastError();
+}
+template <typename P, typename T>
 cudaError_t launch_sb_project(const SbLaunch &S, int nitems, cudaStream_t st) {
     dim3 grid((S.nslots_z + 31) / 32, (S.b + 63) / 64, nitems);
     sb_project_kernel<P, T><<<grid, dim3(32, 8), 0, st>>>(S);
@@ -785,6 +1072,16 @@ cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t s
 template <typename P, typename T>
 cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t st, int N) {
     (void)smem;
+    if (C.col1 <= C.col0) return cudaSuccess;
+    const size_t sp = cheb_inverse_p_smem<T>(N, C.bk);
+    if (sp <= (size_t)227 * 1024) {  // the three matrices stay resident: persistent CTAs
+        set_smem(cheb_inverse_p_kernel<P, T>, sp);
+        const int64_t nblk = (C.col1 - C.col0 + 63) / 64;
+        const int64_t want = std::max<int64_t>(1, (int64_t)resident_ctas(sp, 128) / std::max(C.nvars, 1));
+        cheb_inverse_p_kernel<P, T><<<dim3((unsigned)std::min(nblk, want), C.nvars), 128, sp, st>>>(C);
+        return cudaGetLastError();
+    }
+    // long columns: one matrix at a time, one CTA per (block, variable, variant)
     const size_t sm = cheb_inverse_m_smem<T>(N, C.bk);
     set_smem(cheb_inverse_m_kernel<P, T>, sm);
     if (C.col1 <= C.col0) return cudaSuccess;
@@ -904,6 +1201,12 @@ template cudaError_t launch_tile_sum<double>(const TileLaunch &, cudaStream_t);
 template cudaError_t launch_tile_sum<float>(const TileLaunch &, cudaStream_t);
 
 #define SS_INSTANTIATE(P, T)                                                                                 \
+    template cudaError_t launch_ring_forward_fused<P, T>(const RingLaunch *, const BatchWork *, int, size_t, int, \
+                                                         cudaStream_t);                                          \
+    template cudaError_t launch_ring_inverse_fused<P, T>(const RingLaunch *, const BatchWork *, int, size_t, int, \
+                                                         cudaStream_t);                                          \
+    template cudaError_t launch_sb_project_fused<P, T>(const SbLaunch *, const BatchWork *, int, cudaStream_t);   \
+    template cudaError_t launch_sa_si_fused<P, T>(const SaLaunch *, const BatchWork *, int, size_t, cudaStream_t); \
     template cudaError_t launch_ring_forward<P, T>(const RingLaunch &, int, int, size_t, int, cudaStream_t); \
     template cudaError_t launch_ring_inverse<P, T>(const RingLaunch &, int, int, size_t, int, cudaStream_t); \
     template cudaError_t launch_sb_project<P, T>(const SbLaunch &, int, cudaStream_t);                      \

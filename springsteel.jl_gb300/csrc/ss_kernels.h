@@ -65,6 +65,7 @@ struct SaLaunch {
     int coeffs;                // 1: spectral holds spline coefficients a (skip SAtransform!)
     void *aout;                // non-null: write the coefficients a (storage type, spectral
                                // layout) here and skip SI (splineTransform!)
+    float *sx, *sy;            // binary32 grids: the slot-parallel solve's scratch arrays
 };
 
 struct ChebLaunch {
@@ -100,6 +101,14 @@ struct TileLaunch {
     int b_p, b_t, blocks_p, blocks_t, bk, nvars, offset, set;
 };
 
+// One CTA of a fused multi-grid launch: the launch record it runs (an index
+// into the launch's record array in device memory) and its block coordinates
+// in the grid of CTAs that record would have on its own.
+struct BatchWork {
+    int rec;
+    int bx, by, bz;
+};
+
 void fft_init_constants();
 
 template <typename P>
@@ -123,6 +132,19 @@ cudaError_t launch_sa_si(const SaLaunch &A, int nitems, size_t smem, cudaStream_
 // nitems × b × nslots_z floats (ss_sa_f32.cu)
 template <typename P>
 cudaError_t launch_sa_si_f32(const SaLaunch &A, int nitems, float *X, float *Y, cudaStream_t st);
+// fused launches over the CTAs of many grids' records (nwork CTAs)
+template <typename P, typename T>
+cudaError_t launch_ring_forward_fused(const RingLaunch *recs, const BatchWork *work, int nwork, size_t smem,
+                                      int threads, cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_ring_inverse_fused(const RingLaunch *recs, const BatchWork *work, int nwork, size_t smem,
+                                      int threads, cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_sb_project_fused(const SbLaunch *recs, const BatchWork *work, int nwork, cudaStream_t st);
+template <typename P, typename T>
+cudaError_t launch_sa_si_fused(const SaLaunch *recs, const BatchWork *work, int nwork, size_t smem, cudaStream_t st);
+template <typename P>
+cudaError_t launch_sa_si_f32_fused(const SaLaunch *recs, const BatchWork *work, int nwork, cudaStream_t st);
 template <typename P, typename T>
 cudaError_t launch_cheb_forward(const ChebLaunch &C, size_t smem, cudaStream_t st, int N);
 template <typename P, typename T>

@@ -38,13 +38,13 @@ constexpr int kSaChunk = 32;   // rows per shared-memory staging chunk
 constexpr int kSaBlk = 8;      // rows per prefetch block in the substitution sweeps
 
 template <typename P>
-__global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, float *X, float *Y) {
+__device__ __forceinline__ void sa_si_f32_body(const SaLaunch &A, float *X, float *Y, const int bx, const int by) {
     __shared__ float tile[kSaSlots][kSaChunk + 1];
-    const int item = blockIdx.y;
+    const int item = by;
     const int v = item / A.bk, zb = item % A.bk;
     const SplineDev &sp = A.spl[v];
     const int Md = A.b, n = sp.Min, rL = sp.rankL;
-    const int s0 = blockIdx.x * kSaSlots, t = threadIdx.x, s = s0 + t;
+    const int s0 = bx * kSaSlots, t = threadIdx.x, s = s0 + t;
     const int nsl = min(kSaSlots, A.nslots_z - s0);
     const bool act = t < nsl;
     const size_t ns = (size_t)A.nslots_z;
@@ -265,6 +265,31 @@ __global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, floa
         }
     }
 }
+
+template <typename P>
+__global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, float *X, float *Y) {
+    sa_si_f32_body<P>(A, X, Y, blockIdx.x, blockIdx.y);
+}
+
+// fused multi-grid launch: CTA blockIdx.x runs work[blockIdx.x]; the record
+// (with its own scratch arrays) is staged in shared memory
+template <typename P>
+__global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_fused_kernel(const SaLaunch *recs, const BatchWork *work) {
+    __shared__ __align__(16) SaLaunch A;
+    const BatchWork w = work[blockIdx.x];
+    for (int i = threadIdx.x; i < (int)(sizeof(SaLaunch) / 4); i += blockDim.x)
+        reinterpret_cast<int *>(&A)[i] = __ldg(reinterpret_cast<const int *>(recs + w.rec) + i);
+    __syncthreads();
+    sa_si_f32_body<P>(A, A.sx, A.sy, w.bx, w.by);
+}
+
+template <typename P>
+cudaError_t launch_sa_si_f32_fused(const SaLaunch *recs, const BatchWork *work, int nwork, cudaStream_t st) {
+    if (nwork <= 0) return cudaSuccess;
+    sa_si_f32_fused_kernel<P><<<nwork, kSaSlots, 0, st>>>(recs, work);
+    return cudaGetLastError();
+}
+template cudaError_t launch_sa_si_f32_fused<float>(const SaLaunch *, const BatchWork *, int, cudaStream_t);
 
 template <typename P>
 cudaError_t launch_sa_si_f32(const SaLaunch &A, int nitems, float *X, float *Y, cudaStream_t st) {

@@ -582,15 +582,22 @@ def getGridpoints(grid):
 
 # ----------------------------------------------------------------- batches
 class Batch:
-    """Many grids transformed by one launch sequence (optionally a CUDA graph)."""
+    """Many grids transformed together (optionally replayed as a CUDA graph).
+    fused=True (default): the RL grids' stages run as a few launches over all
+    grids (one launch per ring shared-memory class, one SB and one SA launch);
+    fused=False: every grid's own launch sequence on forked streams.
+    autotune=True times tile shapes (ring CTA size, items per ring CTA) on the
+    grids' own data at creation."""
 
-    def __init__(self, grids, autotune=False):
+    def __init__(self, grids, autotune=False, fused=True):
         self.grids = list(grids)
         lib = load_library()
         arr = (C.c_void_p * len(self.grids))(*[g.handle for g in self.grids])
         h = C.c_void_p()
-        _check(lib.ss_batch_create(arr, len(self.grids), 1 if autotune else 0, C.byref(h)))
+        flags = (abi.SS_BATCH_AUTOTUNE if autotune else 0) | (abi.SS_BATCH_FUSED if fused else 0)
+        _check(lib.ss_batch_create(arr, len(self.grids), flags, C.byref(h)))
         self._h = h
+        self.fused = fused
 
     def run(self, what=3, use_graph=True, stream=None):
         """what: 1 spectralTransform!, 2 gridTransform!, 3 both."""
@@ -598,6 +605,12 @@ class Batch:
 
     def synchronize(self):
         _check(load_library().ss_batch_synchronize(self._h))
+
+    def fused_launches(self, what=3):
+        """Kernel launches the fused batch enqueues for `what` (RL grids)."""
+        n = C.c_int32()
+        _check(load_library().ss_batch_fused_launches(self._h, int(what), C.byref(n)))
+        return n.value
 
     def ring_threads(self, i):
         f, v = C.c_int32(), C.c_int32()
@@ -861,3 +874,8 @@ def regularGridTransform(grid, *points, stream=None):
         grid.handle, rp.ctypes.data_as(C.c_void_p), len(r), lp.ctypes.data_as(C.c_void_p), len(lam),
         zp.ctypes.data_as(C.c_void_p) if zp is not None else None, nz, out.ctypes.data_as(C.c_void_p), stream))
     return out
+
+
+# ----------------------------------------------------------------- I/O (src/io.jl)
+from .io import (check_grid_dims, load_grid, read_netcdf, read_physical_grid, save_grid,  # noqa: E402,F401
+                 write_grid, write_netcdf)

@@ -41,6 +41,9 @@ SS_SBC_PERIODIC = 3
 SS_SBC_R3 = 4
 SS_SBC_R3X = 5
 
+SS_BATCH_AUTOTUNE = 1
+SS_BATCH_FUSED = 2
+
 SS_CBC_R0 = 0
 SS_CBC_R1T0 = 1
 SS_CBC_R1T1 = 2
@@ -158,7 +161,8 @@ EXPORTED = [
     "ss_grid_transform_to_host", "ss_grid_set_filter", "ss_grid_set_ahat",
     "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
     "ss_spectral_transform_noalloc", "ss_regular_grid_transform", "ss_spline_transform", "ss_tile_transform",
-    "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads",
+    "ss_grid_save", "ss_grid_load", "ss_grid_load_arrays", "ss_grid_archive_user",
+    "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads", "ss_batch_fused_launches",
     "ss_chain_create", "ss_chain_destroy", "ss_multi_grid_transform",
     "ss_tile_sum_spectral", "ss_tile_copy_physical", "ss_grid_zero_spectral",
     "ss_problem_create", "ss_problem_destroy", "ss_problem_dims", "ss_problem_operator_band",
@@ -220,9 +224,14 @@ def bind(lib):
         "ss_regular_grid_transform": ([vp, vp, i32, vp, i32, vp, i32, vp, vp], i32),
         "ss_spline_transform": ([vp, vp, vp], i32),
         "ss_tile_transform": ([vp, vp], i32),
+        "ss_grid_save": ([vp, C.c_char_p, vp, C.c_int64, vp], i32),
+        "ss_grid_load": ([C.c_char_p, C.POINTER(vp), vp], i32),
+        "ss_grid_load_arrays": ([vp, C.c_char_p, vp], i32),
+        "ss_grid_archive_user": ([C.c_char_p, vp, C.c_int64, C.POINTER(C.c_int64)], i32),
         "ss_batch_create": ([vp, i32, i32, C.POINTER(vp)], i32),
         "ss_batch_destroy": ([vp], i32),
         "ss_batch_run": ([vp, i32, i32, vp], i32),
+        "ss_batch_fused_launches": ([vp, i32, C.POINTER(i32)], i32),
         "ss_batch_synchronize": ([vp], i32),
         "ss_batch_ring_threads": ([vp, i32, C.POINTER(i32), C.POINTER(i32)], i32),
         "ss_chain_create": ([vp, i32, C.POINTER(vp)], i32),

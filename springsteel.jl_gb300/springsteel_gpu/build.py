@@ -19,7 +19,7 @@ LIB = os.path.join(OUT_DIR, "libspringsteel_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = ["ss_setup.cpp", "ss_kernels.cu", "ss_sa_f32.cu", "ss_api.cu", "ss_batch.cu", "ss_solver.cu", "ss_mlp.cu",
-           "ss_regular.cu"]
+           "ss_regular.cu", "ss_io.cpp"]
 
 
 def _nvcc():

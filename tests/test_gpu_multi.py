@@ -84,8 +84,9 @@ def test_two_patch_chain_linear_exactness():
     assert np.max(np.abs(gs[1].get_physical()[:, 0, 0] - (3 * pts2[:, 0] + 7))) < 1e-8
 
 
+@pytest.mark.parametrize("fused", [False, True])
 @pytest.mark.parametrize("use_graph,autotune", [(True, False), (False, True), (True, True)])
-def test_batch_matches_single_grid_calls(use_graph, autotune):
+def test_batch_matches_single_grid_calls(use_graph, autotune, fused):
     rng = np.random.default_rng(7)
     grids, refs, inputs = [], [], []
     for i in range(6):
@@ -99,7 +100,7 @@ def test_batch_matches_single_grid_calls(use_graph, autotune):
         S.gridTransform_b(g)
         refs.append(g.get_physical())
         grids.append(g)
-    batch = S.Batch(grids, autotune=autotune)
+    batch = S.Batch(grids, autotune=autotune, fused=fused)
     for _ in range(2):  # capture, then replay; gridTransform! overwrites the value slot
         for g, u in zip(grids, inputs):
             g.set_physical(u, slot=1)
@@ -111,7 +112,8 @@ def test_batch_matches_single_grid_calls(use_graph, autotune):
         assert all(t in (64, 128, 256) for i in range(6) for t in batch.ring_threads(i))
 
 
-def test_batch_graph_recaptured_after_filter_and_ahat_changes():
+@pytest.mark.parametrize("fused", [False, True])
+def test_batch_graph_recaptured_after_filter_and_ahat_changes(fused):
     """A batch graph holds each grid's launch arguments (filter flag, ahat
     pointer); changing them between runs re-captures it, so replays equal fresh
     single-grid calls with the new settings."""
@@ -126,7 +128,7 @@ def test_batch_graph_recaptured_after_filter_and_ahat_changes():
     b1 = grids[1].dims["b_iDim"]
     ahat = np.zeros(b1)
     ahat[:3] = (0.7, -0.2, 0.4)
-    batch = S.Batch(grids)
+    batch = S.Batch(grids, fused=fused)
 
     def run_batch():
         for g, u in zip(grids, inputs):
@@ -215,3 +217,48 @@ def test_rlz_tiles_halo_sum_matches_oracle():
     one = np.zeros_like(ref)
     _sum_spectral_tile(one, tile_specs[0], gp, tps[0])
     assert np.max(np.abs(patch.get_spectral() - one)) <= TOL64 * np.max(np.abs(one))
+
+
+# binary32 bulk with the FP64-refined spline solve (RL): f near 2e-7 of its scale,
+# the derivative slots amplify the binary32 rounding of the ring transforms
+F32_RL_BOUNDS = np.array([2e-6, 5e-5, 5e-5, 5e-5, 5e-5])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_fused_batch_config3_range_matches_oracle(precision):
+    """Uneven RL grids of the batched workload's ranges (50-400 cells, 1-4
+    variables) in one fused batch, against the oracle grid by grid; then the
+    same batch with per-grid launch sequences gives bit-identical results."""
+    rng = np.random.default_rng(11)
+    grids, oracles, params, inputs = [], [], [], []
+    for i in range(8):
+        nc = int(rng.integers(50, 401)) if i else 400
+        nv = int(rng.integers(1, 5))
+        gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=float(nc), num_cells=nc,
+                                         vars={"v%d" % k: k + 1 for k in range(nv)}, precision=precision)
+        g = S.createGrid(gp)
+        inputs.append(_fill(g, seed=40 + i))
+        grids.append(g)
+        oracles.append(O.OracleGrid(gp.to_abi()))
+        params.append(gp)
+    fused = S.Batch(grids, autotune=True, fused=True)  # the autotuner's timed runs overwrite slot 1
+    assert fused.fused_launches(3) <= 20  # a few launches per stage for all 8 grids
+    for g, u in zip(grids, inputs):
+        g.set_physical(u, slot=1)
+    fused.run(what=3, use_graph=True)
+    fused.synchronize()
+    outs = [g.get_physical() for g in grids]
+    for g, o, gp, u, out in zip(grids, oracles, params, inputs, outs):
+        ph = np.zeros(o.physical_shape, order="F")
+        ph[:, :, 0] = u.astype(np.float32).astype(np.float64) if precision == "f32" else u
+        ref = o.grid_transform(o.spectral_transform(ph))
+        errs = slot_errors(out, ref, gp)
+        bound = TOL64 if precision == "f64" else F32_RL_BOUNDS
+        assert np.all(errs <= bound), (gp.num_cells, errs.max(axis=0))
+    plain = S.Batch(grids, fused=False)
+    for g, u in zip(grids, inputs):
+        g.set_physical(u, slot=1)
+    plain.run(what=3, use_graph=False)
+    plain.synchronize()
+    for g, out in zip(grids, outs):
+        assert np.array_equal(g.get_physical(), out)
