@@ -71,7 +71,8 @@ enum {
     SS_SBC_R0 = 0,        /* NaturalBC                            */
     SS_SBC_RANK1 = 1,     /* α1, β1: R1T0 (-4,-1), R1T1 (0,1), R1T2 (2,-1), Robin */
     SS_SBC_RANK2 = 2,     /* α2, β2: R2T10 (1,-0.5), R2T20 (-1,0)  */
-    SS_SBC_PERIODIC = 3,  /* not supported by the GPU path (dense factor) */
+    SS_SBC_PERIODIC = 3,  /* PERIODIC: rankL 1 / rankR 2 wrap-around fold; dense LLᵀ factor
+                             (DenseSplineFactor), kept as band + last 3 rows */
     SS_SBC_R3 = 4,        /* ZerosBC                              */
     SS_SBC_R3X = 5        /* FixedBC: R3 fold plus background ahat */
 };

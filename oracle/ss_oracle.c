@@ -294,6 +294,8 @@ struct or_spline {
     int r3x;
     double *PQb;   /* full P+Q, band storage PQb[i*7 + (j-i+3)] (|i-j| ≤ 3) */
     double *L4;    /* banded Cholesky factor of Γ(P+Q)Γᵀ, L4[j*4+d] = L[j+d][j] */
+    int periodic;  /* PERIODIC on either side: dense factor (DenseSplineFactor) */
+    double *Ld;    /* periodic: dense lower Cholesky factor, Ld[i + j*n] = L[i][j] */
     double *mish;
 };
 
@@ -385,9 +387,7 @@ static int gamma_setup(or_spline *s, const ss_spline_bc *bcl, const ss_spline_bc
     case SS_SBC_R0: s->rankL = 0; s->lk = GBC_R0; s->aL = s->bL = 0.0; break;
     case SS_SBC_R3: case SS_SBC_R3X:
         s->rankL = 3; s->lk = GBC_R3; s->aL = s->bL = 0.0; if (bcl->kind == SS_SBC_R3X) s->r3x = 1; break;
-    case SS_SBC_PERIODIC:
-        set_err("PERIODIC spline BC needs the dense factor (src/banded_cholesky.jl:254-260); unsupported");
-        return SS_UNSUPPORTED_BC;
+    case SS_SBC_PERIODIC: s->rankL = 1; s->lk = GBC_PER; s->aL = s->bL = 0.0; break;  /* :395-397 */
     default: set_err("GammaBC: unrecognised BCL kind %d", bcl->kind); return SS_UNSUPPORTED_BC;
     }
     switch (bcr->kind) {
@@ -396,13 +396,12 @@ static int gamma_setup(or_spline *s, const ss_spline_bc *bcl, const ss_spline_bc
     case SS_SBC_R0: s->rankR = 0; s->rk = GBC_R0; s->aR = s->bR = 0.0; break;
     case SS_SBC_R3: case SS_SBC_R3X:
         s->rankR = 3; s->rk = GBC_R3; s->aR = s->bR = 0.0; if (bcr->kind == SS_SBC_R3X) s->r3x = 1; break;
-    case SS_SBC_PERIODIC:
-        set_err("PERIODIC spline BC needs the dense factor; unsupported");
-        return SS_UNSUPPORTED_BC;
+    case SS_SBC_PERIODIC: s->rankR = 2; s->rk = GBC_PER; s->aR = s->bR = 0.0; break;  /* :414-416 */
     default: set_err("GammaBC: unrecognised BCR kind %d", bcr->kind); return SS_UNSUPPORTED_BC;
     }
     s->Mdim = s->nc + 3;
     s->Min = s->Mdim - s->rankL - s->rankR;
+    s->periodic = (s->lk == GBC_PER || s->rk == GBC_PER);
     if (s->Min < 1) { set_err("no interior coefficients (num_cells too small for the BCs)"); return SS_BAD_SHAPE; }
     return SS_OK;
 }
@@ -415,12 +414,17 @@ static double gamma_at(const or_spline *g, int i, int j) {
     } else if (g->lk == GBC_A2) {
         if (j == 1 && i == 1) val += g->aL;
         else if (j == 2 && i == 1) val += g->bL;
+    } else if (g->lk == GBC_PER) {
+        if (j == 1 && i == g->Min) val += 1.0;
     }
     if (g->rk == GBC_A1) {
         if (j == g->Mdim) { if (i == g->Min) val += g->aR; if (i == g->Min - 1) val += g->bR; }
     } else if (g->rk == GBC_A2) {
         if (j == g->Mdim && i == g->Min) val += g->aR;
         else if (j == g->Mdim - 1 && i == g->Min) val += g->bR;
+    } else if (g->rk == GBC_PER) {  /* src/CubicBSpline.jl:366-369 */
+        if (j == g->Mdim - 1 && i == 1) val += 1.0;
+        if (j == g->Mdim && i == 2) val += 1.0;
     }
     return val;
 }
@@ -431,8 +435,10 @@ static void gamma_apply(const or_spline *g, const double *b, double *out) {
     for (int i = 0; i < Min; i++) out[i] = b[i + rL];
     if (g->lk == GBC_A1) { out[0] += g->aL * b[0]; out[1] += g->bL * b[0]; }
     else if (g->lk == GBC_A2) { out[0] += g->aL * b[0] + g->bL * b[1]; }
+    else if (g->lk == GBC_PER) { out[Min - 1] += b[0]; }
     if (g->rk == GBC_A1) { out[Min - 1] += g->aR * b[Mdim - 1]; out[Min - 2] += g->bR * b[Mdim - 1]; }
     else if (g->rk == GBC_A2) { out[Min - 1] += g->aR * b[Mdim - 1] + g->bR * b[Mdim - 2]; }
+    else if (g->rk == GBC_PER) { out[0] += b[Mdim - 2]; out[1] += b[Mdim - 1]; }
 }
 
 /* out (Mdim) ← Γᵀ x (Min), src/CubicBSpline.jl:461-500 */
@@ -443,8 +449,43 @@ static void gamma_adjoint(const or_spline *g, const double *x, double *out) {
     for (int i = 0; i < Min; i++) out[i + rL] = x[i];
     if (g->lk == GBC_A1) out[0] = g->aL * x[0] + g->bL * x[1];
     else if (g->lk == GBC_A2) { out[0] = g->aL * x[0]; out[1] = g->bL * x[0]; }
+    else if (g->lk == GBC_PER) out[0] = x[Min - 1];
     if (g->rk == GBC_A1) out[Mdim - 1] = g->aR * x[Min - 1] + g->bR * x[Min - 2];
     else if (g->rk == GBC_A2) { out[Mdim - 2] = g->bR * x[Min - 1]; out[Mdim - 1] = g->aR * x[Min - 1]; }
+    else if (g->rk == GBC_PER) { out[Mdim - 2] = x[0]; out[Mdim - 1] = x[1]; }
+}
+
+/* cholesky_dense_factor / DenseSplineFactor (src/banded_cholesky.jl:70, 250-260;
+ * LAPACK potrf's A = L Lᵀ, lower): the periodic case, whose Γ wrap-around
+ * couples the first and last interior coefficients.  A column-major n × n,
+ * overwritten by L in its lower triangle. */
+static int dense_chol(double *A, int n) {
+    for (int j = 0; j < n; j++) {
+        double d = A[j + (size_t)j * n];
+        for (int k = 0; k < j; k++) d -= A[j + (size_t)k * n] * A[j + (size_t)k * n];
+        if (d <= 0.0) { set_err("PosDefException(%d)", j + 1); return SS_NOT_SPD; }
+        const double ljj = sqrt(d);
+        A[j + (size_t)j * n] = ljj;
+        for (int i = j + 1; i < n; i++) {
+            double t = A[i + (size_t)j * n];
+            for (int k = 0; k < j; k++) t -= A[i + (size_t)k * n] * A[j + (size_t)k * n];
+            A[i + (size_t)j * n] = t / ljj;
+        }
+        for (int i = 0; i < j; i++) A[i + (size_t)j * n] = 0.0;
+    }
+    return SS_OK;
+}
+static void dense_solve(const double *L, int n, const double *b, double *x) {
+    for (int i = 0; i < n; i++) {
+        double t = b[i];
+        for (int k = 0; k < i; k++) t -= L[i + (size_t)k * n] * x[k];
+        x[i] = t / L[i + (size_t)i * n];
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        double t = x[i];
+        for (int k = i + 1; k < n; k++) t -= L[k + (size_t)i * n] * x[k];
+        x[i] = t / L[i + (size_t)i * n];
+    }
 }
 
 /* _band_factor3!, src/banded_cholesky.jl:166-197 (0-based; L4[j*4+d] = L[j+d][j]) */
@@ -529,11 +570,13 @@ static int pq_setup(or_spline *s) {
     }
     s->PQb = (double *)calloc((size_t)Mdim * 7, sizeof(double));
     for (int i = 0; i < Mdim * 7; i++) s->PQb[i] = P[i] + Q[i];
-    /* PQopen = Γ P Γᵀ + Γ Q Γᵀ, computed on the ±6 band (Γ rows have ≤ 3 entries) */
+    /* PQopen = Γ P Γᵀ + Γ Q Γᵀ, computed on the ±6 band (Γ rows have ≤ 3 entries);
+     * periodic: every entry (the wrap-around couples the two ends) */
     int n = s->Min;
     double *A = (double *)calloc((size_t)n * n, sizeof(double));
     for (int i = 1; i <= n; i++) {
-        for (int j = (i - 6 > 1 ? i - 6 : 1); j <= (i + 6 < n ? i + 6 : n); j++) {
+        const int jlo = s->periodic ? 1 : (i - 6 > 1 ? i - 6 : 1), jhi = s->periodic ? n : (i + 6 < n ? i + 6 : n);
+        for (int j = jlo; j <= jhi; j++) {
             double accP = 0.0, accQ = 0.0;
             for (int a = 1; a <= Mdim; a++) {
                 double ga = gamma_at(s, i, a);
@@ -550,7 +593,15 @@ static int pq_setup(or_spline *s) {
     }
     free(P); free(Q);
     s->L4 = (double *)calloc((size_t)n * 4, sizeof(double));
-    int st = or_band_chol(A, n, s->L4);
+    int st;
+    if (s->periodic) {  /* calcPQfactor: is_periodic → cholesky_dense_factor (:777-781) */
+        st = dense_chol(A, n);
+        s->Ld = A;
+        for (int j = 0; j < n; j++)
+            for (int d = 0; d < 4 && j + d < n; d++) s->L4[j * 4 + d] = A[(j + d) + (size_t)j * n];
+        return st;
+    }
+    st = or_band_chol(A, n, s->L4);
     free(A);
     return st;
 }
@@ -585,7 +636,7 @@ int32_t or_spline_create(double xmin, double xmax, int32_t nc, int32_t mubar, in
 }
 void or_spline_destroy(or_spline *s) {
     if (!s) return;
-    free(s->PQb); free(s->L4); free(s->mish); free(s);
+    free(s->PQb); free(s->L4); free(s->Ld); free(s->mish); free(s);
 }
 int32_t or_spline_info(const or_spline *s, int32_t *bDim, int32_t *mishDim, int32_t *Min) {
     *bDim = s->bDim; *mishDim = s->mishDim; *Min = s->Min;
@@ -627,7 +678,8 @@ static void spline_sa(const or_spline *s, const double *b, const double *ahat, d
         bb = t1;
     }
     gamma_apply(s, bb, t2);
-    band_solve3(s->L4, s->Min, t2, t3);
+    if (s->periodic) dense_solve(s->Ld, s->Min, t2, t3);
+    else band_solve3(s->L4, s->Min, t2, t3);
     gamma_adjoint(s, t3, a);
     if (s->r3x && ahat)
         for (int i = 0; i < Mdim; i++) a[i] += ahat[i];

@@ -165,7 +165,7 @@ static int32_t build_grid(ss_grid *g) {
         SplineDev &sd = sdev[v];
         std::memset(&sd, 0, sizeof sd);
         sd.bDim = sh.bDim; sd.Min = sh.Min; sd.rankL = sh.rankL; sd.rankR = sh.rankR;
-        sd.lk = sh.lk; sd.rk = sh.rk; sd.r3x = sh.r3x;
+        sd.lk = sh.lk; sd.rk = sh.rk; sd.r3x = sh.r3x; sd.periodic = sh.periodic;
         sd.aL = sh.aL; sd.bL = sh.bL; sd.aR = sh.aR; sd.bR = sh.bR;
         std::vector<double> dinv(sh.Min);
         for (int i = 0; i < sh.Min; i++) dinv[i] = 1.0 / sh.L4[size_t(i) * 4];
@@ -178,6 +178,13 @@ static int32_t build_grid(ss_grid *g) {
         if ((st = upload_vec(g, &sd.L4f, l4f))) return st;
         if ((st = upload_vec(g, &sd.dinvf, dinvf))) return st;
         if ((st = upload_vec(g, &sd.Aband, sh.Aopen))) return st;
+        if (sh.periodic) {  // the dense factor's last three rows and A's corners
+            std::vector<float> tf(sh.tail.size());
+            for (size_t i = 0; i < tf.size(); i++) tf[i] = (float)sh.tail[i];
+            if ((st = upload_vec(g, &sd.tail, sh.tail))) return st;
+            if ((st = upload_vec(g, &sd.tailf, tf))) return st;
+            if ((st = upload_vec(g, &sd.acorner, sh.acorner))) return st;
+        }
         if ((st = upload_bytes(g, &sd.sbw_t, real_layout(sh.sbw, g->tl)))) return st;
         if ((st = upload_bytes(g, &sd.siw_t, real_layout(sh.siw, g->tl)))) return st;
         if ((st = upload_vec(g, &sd.si_m0, sh.si_m0))) return st;
@@ -564,8 +571,12 @@ static int32_t inv_sa(ss_grid *g, cudaStream_t st, int coeffs, const void *spec_
         A.aout = aout;
     }
     StageScope sc(g, SS_STAGE_SA_SI, st);
+    bool periodic = false;
+    for (auto &sh : g->spl_host) periodic |= sh.periodic != 0;
     if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
-        if (aout) CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
+        // the slot-parallel binary32 kernel has no dense-tail solve: periodic splines
+        // (and the coefficient output of splineTransform!) take the tiled kernel
+        if (aout || periodic) CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));
         else CUDA_TRY((launch_sa_si_f32<P>(A, g->nitems, (float *)g->sa_x, (float *)g->sa_y, st)));
     } else {
         CUDA_TRY((launch_sa_si<P, T>(A, g->nitems, smem, st)));

@@ -217,20 +217,30 @@ static int32_t plan_sa(ss_batch *bt, const std::vector<ss_grid *> &gs, int tl, s
     const void *d_recs = nullptr;
     int32_t rc = upload(bt, L, &d_recs);
     if (rc) return rc;
-    if (tl == TL_F32) {  // slot-parallel binary32 solve: no dynamic shared memory
+    // binary32 grids: the slot-parallel solve (no dynamic shared memory), except
+    // grids with a periodic spline, whose dense-tail solve runs on the tiled kernel
+    auto periodic = [&](int i) {
+        for (auto &sh : gs[i]->spl_host)
+            if (sh.periodic) return true;
+        return false;
+    };
+    if (tl == TL_F32) {
         std::vector<BatchWork> work;
         for (int i = 0; i < (int)gs.size(); i++)
-            for (int by = 0; by < gs[i]->nitems; by++)
-                for (int bx = 0; bx < (L[i].nslots_z + 127) / 128; bx++) work.push_back({i, bx, by, 0});
-        const void *w = nullptr;
-        if ((rc = upload(bt, work, &w))) return rc;
-        out.push_back({FK_SA_F32, tl, 0, 128, (int)work.size(), d_recs, (const BatchWork *)w});
-        return SS_OK;
+            if (!periodic(i))
+                for (int by = 0; by < gs[i]->nitems; by++)
+                    for (int bx = 0; bx < (L[i].nslots_z + 127) / 128; bx++) work.push_back({i, bx, by, 0});
+        if (!work.empty()) {
+            const void *w = nullptr;
+            if ((rc = upload(bt, work, &w))) return rc;
+            out.push_back({FK_SA_F32, tl, 0, 128, (int)work.size(), d_recs, (const BatchWork *)w});
+        }
     }
     for (int c = 0; c < 7; c++) {
         std::vector<BatchWork> work;
         size_t sm = 0;
         for (int i = 0; i < (int)gs.size(); i++) {
+            if (tl == TL_F32 && !periodic(i)) continue;
             if (smem_class(smem[i]) != c) continue;
             sm = std::max(sm, smem[i]);
             for (int by = 0; by < gs[i]->nitems; by++)
@@ -495,6 +505,11 @@ extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **
             set_error("the chain supports RL or RLZ patches with equal variable counts (and Chebyshev modes)");
             return SS_BAD_ARG;
         }
+        for (auto &sh : grids[i]->spl_host)
+            if (sh.periodic) {
+                set_error("a patch of a chain cannot have a PERIODIC spline (patches couple at their ends)");
+                return SS_UNSUPPORTED_BC;
+            }
     }
     ss_chain *c = new ss_chain();
     c->device = grids[0]->device;

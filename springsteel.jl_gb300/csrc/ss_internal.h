@@ -78,7 +78,8 @@ enum { TL_F64 = 0, TL_DF64 = 1, TL_F32 = 2 };
 
 // Per-variable spline template on the device (FP64 factor, B-spline weights).
 struct SplineDev {
-    int bDim, Min, rankL, rankR, lk, rk, r3x, _pad;
+    int bDim, Min, rankL, rankR, lk, rk, r3x;
+    int periodic;       // PERIODIC on a side: L has 3 dense bottom rows (tail), A has corners
     double aL, bL, aR, bR;
     double *L4;         // Min*4: L[j+d][j] at j*4+d   (FP64 banded Cholesky factor)
     double *dinv;       // Min: 1/L[j][j]
@@ -86,6 +87,9 @@ struct SplineDev {
     float *L4f;         // FP32-rounded factor (FP32 mode)
     float *dinvf;
     double *Aband;      // FP64 open-form Γ(P+Q)Γᵀ band, Aband[j*4+d] = A[j+d][j] (FP32 refinement residual)
+    double *tail;       // periodic: rows n-3..n-1 of L, tail[r*n + j] = L[n-3+r][j] (j ≤ n-3+r); else null
+    float *tailf;       // the same, FP32-rounded
+    double *acorner;    // periodic: A[n-3+r][c] for c < 3 where |n-3+r-c| > 3 (else 0), 3 × 3
     const void *sbw_t;  // bDim*(4 mubar) SB weights (row mi, tap), compute layout
     const void *siw_t;  // 3*mishDim*4 SI weights (derivative, point, tap), compute layout
     int *si_m0;         // mishDim: first coefficient index of the 4-tap window
@@ -127,6 +131,8 @@ struct SplineHost {
     double aL, bL, aR, bR;
     std::vector<double> PQb, L4, Aopen, sbw, siw;  // Aopen: open-form band before factoring
     std::vector<int> si_m0;
+    int periodic = 0;
+    std::vector<double> tail, acorner;  // periodic factor rows n-3..n-1 and out-of-band corners of A
 };
 int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, double l_q,
                      const ss_spline_bc &bcl, const ss_spline_bc &bcr, SplineHost &out);

@@ -378,35 +378,49 @@ __device__ __forceinline__ void sa_si_body(const SaLaunch &A, const int bx, cons
         if constexpr (kF32) {
             S *r = R + threadIdx.x * ld;
             for (int i = 0; i < n; i++) r[i] = x[i];  // keep Γb
-            band_solve(Ls, Di, x, n);
+            band_solve(Ls, Di, x, n, sp.periodic ? sp.tailf : nullptr);
             // one refinement step in FP64: residual r = Γb − A x against the FP64
-            // open-form band, correction L Lᵀ c = r with the FP64 factor
-            // (forward sweep into r, rounded to binary32 between the sweeps),
-            // x ← x + c rounded once
+            // open-form band (and, periodic, its corners), correction L Lᵀ c = r
+            // with the FP64 factor (forward sweep into r, rounded to binary32
+            // between the sweeps), x ← x + c rounded once
+            const int r0 = sp.periodic ? n - 3 : n;
             double y1 = 0.0, y2 = 0.0, y3 = 0.0;
             for (int i = 0; i < n; i++) {
                 double acc = (double)r[i];
                 for (int j = max(0, i - 3); j <= min(n - 1, i + 3); j++)
                     acc -= __ldg(sp.Aband + min(i, j) * 4 + abs(i - j)) * (double)x[j];
-                if (i >= 3) acc -= __ldg(sp.L4 + (i - 3) * 4 + 3) * y3;
-                if (i >= 2) acc -= __ldg(sp.L4 + (i - 2) * 4 + 2) * y2;
-                if (i >= 1) acc -= __ldg(sp.L4 + (i - 1) * 4 + 1) * y1;
+                if (sp.periodic) {  // A[n−3+q][c] and its transpose, beyond the band
+                    for (int c = 0; c < 3; c++) {
+                        if (i >= r0) acc -= __ldg(sp.acorner + (i - r0) * 3 + c) * (double)x[c];
+                        if (i < 3) acc -= __ldg(sp.acorner + c * 3 + i) * (double)x[r0 + c];
+                    }
+                }
+                if (i >= r0) {
+                    for (int j = 0; j < i; j++) acc -= __ldg(sp.tail + (size_t)(i - r0) * n + j) * (double)r[j];
+                } else {
+                    if (i >= 3) acc -= __ldg(sp.L4 + (i - 3) * 4 + 3) * y3;
+                    if (i >= 2) acc -= __ldg(sp.L4 + (i - 2) * 4 + 2) * y2;
+                    if (i >= 1) acc -= __ldg(sp.L4 + (i - 1) * 4 + 1) * y1;
+                }
                 const double yi = acc * __ldg(sp.dinv + i);
                 r[i] = (S)yi;
                 y3 = y2; y2 = y1; y1 = yi;
             }
-            double c1 = 0.0, c2 = 0.0, c3 = 0.0;
+            double c1 = 0.0, c2 = 0.0, c3 = 0.0, ct[3] = {0.0, 0.0, 0.0};  // ct: the tail rows' c
             for (int i = n - 1; i >= 0; i--) {
                 double acc = (double)r[i];
                 if (i + 1 < n) acc -= __ldg(sp.L4 + i * 4 + 1) * c1;
                 if (i + 2 < n) acc -= __ldg(sp.L4 + i * 4 + 2) * c2;
                 if (i + 3 < n) acc -= __ldg(sp.L4 + i * 4 + 3) * c3;
+                if (sp.periodic)
+                    for (int q = max(r0, i + 4); q < n; q++) acc -= __ldg(sp.tail + (size_t)(q - r0) * n + i) * ct[q - r0];
                 const double ci = acc * __ldg(sp.dinv + i);
+                if (i >= r0) ct[i - r0] = ci;
                 c3 = c2; c2 = c1; c1 = ci;
                 x[i] = (S)((double)x[i] + ci);
             }
         } else {
-            band_solve(Ls, Di, x, n);
+            band_solve(Ls, Di, x, n, sp.periodic ? sp.tail : nullptr);
         }
         gamma_unfold(sp, x, Md, n);
         if (ah)
@@ -1114,7 +1128,7 @@ __global__ void __launch_bounds__(32) chain_couple_kernel(ChainLaunch C) {
     if (threadIdx.x < nsl) {
         double *x = X + threadIdx.x * ld;
         gamma_fold(sp, x, b, n);
-        band_solve(Ls, Di, x, n);
+        band_solve(Ls, Di, x, n, sp.periodic ? sp.tail : nullptr);
         gamma_unfold(sp, x, b, n);
         const double e0 = x[C.node[0]], e1 = x[C.node[1]], e2 = x[C.node[2]];
         double *out = C.coupled + ((size_t)item * C.nq + q0 + threadIdx.x) * 3;

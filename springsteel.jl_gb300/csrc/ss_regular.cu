@@ -60,7 +60,7 @@ __global__ void reg_sa_kernel(const P *spec, const SplineDev *spl, double *coef,
     if (threadIdx.x < nsl) {
         double *x = X + threadIdx.x * ld;
         gamma_fold(sp, x, b, n);
-        band_solve(Ls, Di, x, n);
+        band_solve(Ls, Di, x, n, sp.periodic ? sp.tail : nullptr);
         gamma_unfold(sp, x, b, n);
     }
     __syncthreads();

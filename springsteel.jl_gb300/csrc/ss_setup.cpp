@@ -101,11 +101,15 @@ static double gamma_at(const SplineHost &g, int i, int j) {
         if (j == 1 && i == 1) val += g.aL;
         else if (j == 2 && i == 1) val += g.bL;
     }
+    else if (g.lk == BC_PER && j == 1 && i == g.Min) val += 1.0;
     if (g.rk == BC_A1) {
         if (j == g.Mdim) { if (i == g.Min) val += g.aR; if (i == g.Min - 1) val += g.bR; }
     } else if (g.rk == BC_A2) {
         if (j == g.Mdim && i == g.Min) val += g.aR;
         else if (j == g.Mdim - 1 && i == g.Min) val += g.bR;
+    } else if (g.rk == BC_PER) {  // wrap-around rows (src/CubicBSpline.jl:366-369)
+        if (j == g.Mdim - 1 && i == 1) val += 1.0;
+        if (j == g.Mdim && i == 2) val += 1.0;
     }
     return val;
 }
@@ -117,12 +121,76 @@ static int side_bc(const ss_spline_bc &bc, int right, int &rank, int &kind, doub
     case SS_SBC_RANK2: rank = 2; kind = BC_A2; a = bc.alpha; b = bc.beta; return SS_OK;
     case SS_SBC_R3: rank = 3; kind = BC_R3; a = b = 0.0; return SS_OK;
     case SS_SBC_R3X: rank = 3; kind = BC_R3; a = b = 0.0; r3x = 1; return SS_OK;
-    case SS_SBC_PERIODIC:
-        set_error("PERIODIC spline BC (%s) needs a dense factor; not supported by the GPU path",
-                  right ? "BCR" : "BCL");
-        return SS_UNSUPPORTED_BC;
+    case SS_SBC_PERIODIC:  // GammaBC: rankL 1 / rankR 2 (src/CubicBSpline.jl:395-397, 414-416)
+        rank = right ? 2 : 1; kind = BC_PER; a = b = 0.0; return SS_OK;
     default: set_error("unrecognised spline BC kind %d", bc.kind); return SS_UNSUPPORTED_BC;
     }
+}
+
+static int32_t finish_weights(SplineHost &s);
+
+// PERIODIC: the wrap-around rows of Γ couple the first and the last interior
+// coefficients, so Γ(P+Q)Γᵀ is banded plus corner entries and the reference
+// factors it densely (cholesky_dense_factor, src/banded_cholesky.jl:70, 250-260,
+// chosen by calcPQfactor, src/CubicBSpline.jl:777-781).  The corners sit in the
+// last three rows (and columns), so the dense LLᵀ factor is banded except for
+// its last three rows; it is kept as the (4, n) band plus those rows (`tail`),
+// and the corners of A beyond the band for the binary32 refinement residual.
+static int32_t periodic_factor(SplineHost &s, const std::vector<double> &P, const std::vector<double> &Q) {
+    const int n = s.Min, Md = s.Mdim;
+    if (n < 4) { set_error("PERIODIC spline BC needs at least 4 interior coefficients"); return SS_BAD_SHAPE; }
+    std::vector<std::vector<std::pair<int, double>>> rows(n + 1);  // Γ row i (1-based): (column, value)
+    for (int i = 1; i <= n; i++)
+        for (int a : {i + s.rankL, 1, 2, Md - 1, Md}) {
+            bool seen = false;
+            for (auto &e : rows[i]) seen |= e.first == a;
+            const double ga = (a >= 1 && a <= Md && !seen) ? gamma_at(s, i, a) : 0.0;
+            if (ga != 0.0) rows[i].push_back({a, ga});
+        }
+    std::vector<double> A(size_t(n) * n, 0.0);  // column-major, A[i + j n]
+    for (int i = 1; i <= n; i++)
+        for (int j = 1; j <= n; j++) {
+            double acc = 0.0;
+            for (auto &ea : rows[i])
+                for (auto &eb : rows[j]) {
+                    const int d = eb.first - ea.first;
+                    if (d < -3 || d > 3) continue;
+                    const size_t k = size_t(ea.first - 1) * 7 + (d + 3);
+                    acc += ea.second * (P[k] + Q[k]) * eb.second;
+                }
+            A[size_t(i - 1) + size_t(j - 1) * n] = acc;
+        }
+    s.Aopen.assign(size_t(n) * 4, 0.0);
+    s.acorner.assign(9, 0.0);
+    const int r0 = n - 3;
+    for (int j = 0; j < n; j++)
+        for (int d = 0; d < 4 && j + d < n; d++) s.Aopen[size_t(j) * 4 + d] = A[size_t(j + d) + size_t(j) * n];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            if (r0 + r - c > 3) s.acorner[r * 3 + c] = A[size_t(r0 + r) + size_t(c) * n];
+    // dense LLᵀ, lower triangle in place (potrf's factor)
+    for (int j = 0; j < n; j++) {
+        double d = A[size_t(j) + size_t(j) * n];
+        for (int k = 0; k < j; k++) d -= A[size_t(j) + size_t(k) * n] * A[size_t(j) + size_t(k) * n];
+        if (d <= 0.0) { set_error("P+Q not positive definite (PosDefException at %d)", j + 1); return SS_NOT_SPD; }
+        const double ljj = std::sqrt(d);
+        A[size_t(j) + size_t(j) * n] = ljj;
+        for (int i = j + 1; i < n; i++) {
+            double t = A[size_t(i) + size_t(j) * n];
+            for (int k = 0; k < j; k++) t -= A[size_t(i) + size_t(k) * n] * A[size_t(j) + size_t(k) * n];
+            A[size_t(i) + size_t(j) * n] = t / ljj;
+        }
+    }
+    for (int i = 0; i < r0; i++)  // rows above the tail keep the band: no fill-in below j = i − 3
+        for (int j = 0; j < i - 3; j++)
+            if (A[size_t(i) + size_t(j) * n] != 0.0) { set_error("periodic factor fills outside its band"); return SS_BAD_ARG; }
+    s.L4.assign(size_t(n) * 4, 0.0);
+    for (int j = 0; j < n; j++)
+        for (int d = 0; d < 4 && j + d < n; d++) s.L4[size_t(j) * 4 + d] = A[size_t(j + d) + size_t(j) * n];
+    s.tail.assign(size_t(3) * n, 0.0);
+    for (int r = 0; r < 3; r++)
+        for (int j = 0; j <= r0 + r; j++) s.tail[size_t(r) * n + j] = A[size_t(r0 + r) + size_t(j) * n];
+    return SS_OK;
 }
 
 int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, double l_q,
@@ -169,8 +237,13 @@ int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, doub
     s.PQb.assign(Md * 7, 0.0);
     for (int i = 0; i < Md * 7; i++) s.PQb[i] = P[i] + Q[i];
 
-    // open form Γ P Γᵀ + Γ Q Γᵀ on the band, then the banded LLᵀ factor
     const int n = s.Min;
+    s.periodic = (s.lk == BC_PER || s.rk == BC_PER);
+    if (s.periodic) {
+        const int32_t st = periodic_factor(s, P, Q);
+        return st ? st : finish_weights(s);
+    }
+    // open form Γ P Γᵀ + Γ Q Γᵀ on the band, then the banded LLᵀ factor
     std::vector<double> A(size_t(n) * 4, 0.0);  // A[j*4+d] = Aopen[j+d][j]
     for (int j = 1; j <= n; j++)
         for (int i = j; i <= std::min(n, j + 6); i++) {
@@ -208,7 +281,13 @@ int32_t build_spline(double xmin, double xmax, int nc, int mubar, int quad, doub
         }
     }
     s.L4 = A;
+    return finish_weights(s);
+}
 
+// SB weights and SI weights of a spline (shared by the banded and periodic setups)
+static int32_t finish_weights(SplineHost &s) {
+    const int Md = s.Mdim, nc = s.nc, mubar = s.mubar;
+    const double xmin = s.xmin;
     // SB weights: row mi (0-based), tap t = c*mubar + mu over cells mc = mi-3+c
     const int taps = 4 * mubar;
     s.sbw.assign(size_t(Md) * taps, 0.0);

@@ -227,10 +227,10 @@ def test_fp32_kz64_error_vs_fp64_oracle():
 def test_bad_shapes_rejected():
     with pytest.raises(S.SpringsteelError):
         S.createGrid(S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=1.0, num_cells=0))
-    with pytest.raises(S.SpringsteelError) as e:
-        S.createGrid(S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=1.0, num_cells=4,
+    with pytest.raises(S.SpringsteelError) as e:  # a periodic spline needs 4 interior coefficients
+        S.createGrid(S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=1.0, num_cells=3,
                                                  BCL={"default": S.PeriodicBC()}, BCR={"default": S.PeriodicBC()}))
-    assert e.value.status == S.abi.SS_UNSUPPORTED_BC
+    assert e.value.status == S.abi.SS_BAD_SHAPE
 
 
 def _host_case(geometry, precision):
@@ -302,3 +302,29 @@ def test_rlz_unequal_max_wavenumber():
     u = fields.rlz_blob_fields(pts, 3, zmax=20000.0)
     _, o, sg, so, pg, po = _run_both(gp, u)
     _assert_parity(sg, so, pg, po, gp)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f64_fast", "f32"])
+@pytest.mark.parametrize("geometry", ["RL", "RLZ"])
+def test_periodic_spline_bc_parity(geometry, precision):
+    """PERIODIC radial splines (DenseSplineFactor, src/banded_cholesky.jl:70, 250-260):
+    the wrap-around Γ fold and the dense factor's tail rows against the oracle's
+    dense solve; a second variable keeps a banded BC in the same grid."""
+    kw = dict(vars={"u": 1, "w": 2}, BCL={"u": S.PeriodicBC(), "w": S.DirichletBC()},
+              BCR={"u": S.PeriodicBC(), "w": S.NaturalBC()}, precision=precision)
+    if geometry == "RL":
+        gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=30.0, num_cells=15, **kw)
+    else:
+        gp = S.SpringsteelGridParameters(geometry="RLZ", iMin=0.0, iMax=24.0, num_cells=12, kMin=0.0, kMax=500.0,
+                                         kDim=10, BCB={"default": S.DirichletBC()}, **kw)
+    pts = S.getGridpoints(S.createGrid(gp))
+    u = np.column_stack([fields.blob_sum(pts, seed=31 + v, nblobs=5, wmin=3.0, wmax=9.0,
+                                         zmax=max(gp.kMax, 1.0)) for v in range(2)])
+    if precision == "f32":
+        u = u.astype(np.float32).astype(np.float64)
+    g, o, spec_g, spec_o, phys_g, phys_o = _run_both(gp, u)
+    if precision == "f32":
+        errs = slot_errors(phys_g, phys_o, gp)
+        assert np.all(errs.max(axis=0)[:5] <= [2e-6, 5e-5, 5e-5, 5e-5, 5e-5]), errs
+    else:
+        _assert_parity(spec_g, spec_o, phys_g, phys_o, gp, TOL64 if precision == "f64" else TOL_FAST)

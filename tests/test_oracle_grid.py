@@ -137,10 +137,10 @@ def test_dirichlet_bc_in_z():
     assert np.max(np.abs(out[kz - 1::kz, 0, 0])) < 1e-12
 
 
-def test_unsupported_spline_periodic():
-    with pytest.raises(O.OracleError) as e:
-        _rl(4, 10.0, BCL=[(abi.SS_SBC_PERIODIC, 0, 0)], BCR=[(abi.SS_SBC_PERIODIC, 0, 0)])
-    assert e.value.status == abi.SS_UNSUPPORTED_BC
+def test_periodic_spline_grid_builds():
+    # PERIODIC is a GammaBC kind with a dense factor (src/banded_cholesky.jl:70, 250-260)
+    g = _rl(4, 10.0, BCL=[(abi.SS_SBC_PERIODIC, 0, 0)], BCR=[(abi.SS_SBC_PERIODIC, 0, 0)])
+    assert g.dims["b_iDim"] == 7
 
 
 def _rlz_spectral_wavenumber_norms(gp):
