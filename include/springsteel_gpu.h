@@ -319,6 +319,12 @@ int32_t ss_batch_fused_launches(const ss_batch *batch, int32_t what, int32_t *la
  * (NaturalBC side), the finer secondary (FixedBC side); DX ratio 1:1 or 2:1. */
 typedef struct ss_chain ss_chain;
 int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **out);
+/* PatchEmbedded(grids) (src/multipatch.jl:891-925): grids nested outermost
+ * first, each inner grid 2:1 finer than its parent and FixedBC (R3X) at both
+ * ends; multiGridTransform! feeds each inner grid R3X data from its parent
+ * at both ends (stacked interfaces at the parent's nodes under the inner
+ * boundaries).  Destroyed and run like a chain. */
+int32_t ss_chain_create_embedded(ss_grid *const *grids, int32_t n, ss_chain **out);
 int32_t ss_chain_destroy(ss_chain *chain);
 int32_t ss_multi_grid_transform(ss_chain *chain, void *stream);
 

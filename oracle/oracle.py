@@ -372,10 +372,12 @@ def cheb_mish(zDim, zmin, zmax):
 class OracleChain:
     """PatchChain + multiGridTransform! on the oracle (src/multipatch.jl)."""
 
-    def __init__(self, grids):
+    def __init__(self, grids, embedded=False):
+        """embedded=True: PatchEmbedded (src/multipatch.jl:891-925), grids outermost first."""
         L = lib()
-        L.or_chain_create.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]
-        L.or_chain_create.restype = C.c_int32
+        for fn in (L.or_chain_create, L.or_chain_create_embedded):
+            fn.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]
+            fn.restype = C.c_int32
         L.or_chain_destroy.argtypes = [C.c_void_p]
         L.or_chain_destroy.restype = None
         L.or_multi_grid_transform.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -383,7 +385,7 @@ class OracleChain:
         self.grids = list(grids)
         arr = (C.c_void_p * len(self.grids))(*[g.h.value for g in self.grids])
         h = C.c_void_p()
-        _check(L.or_chain_create(arr, len(self.grids), C.byref(h)))
+        _check((L.or_chain_create_embedded if embedded else L.or_chain_create)(arr, len(self.grids), C.byref(h)))
         self.h = h
 
     def multi_grid_transform(self, spectrals):

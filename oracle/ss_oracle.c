@@ -1539,6 +1539,68 @@ int32_t or_chain_create(or_grid **grids, int32_t n, or_chain **out) {
     return SS_OK;
 }
 
+/* PatchEmbedded (src/multipatch.jl:891-925): grids nested outermost first; each
+ * inner grid takes R3X data from its parent at both ends through stacked
+ * interfaces (the parent's node at the inner boundary, :190-207, 270-276),
+ * pushed right-of-inner-left first, then its right end. */
+int32_t or_chain_create_embedded(or_grid **grids, int32_t n, or_chain **out) {
+    *out = NULL;
+    if (n < 2) { set_err("PatchEmbedded requires at least 2 grids, got %d", n); return SS_BAD_ARG; }
+    for (int k = 0; k < n; k++)
+        if (grids[k]->geom != grids[0]->geom || grids[k]->nvars != grids[0]->nvars ||
+            (grids[0]->geom == SS_GEOM_RLZ && grids[k]->bk != grids[0]->bk)) {
+            set_err("embedded patches must share geometry, variable count (and Chebyshev modes)");
+            return SS_BAD_ARG;
+        }
+    or_chain *c = (or_chain *)calloc(1, sizeof *c);
+    c->n = n;
+    c->g = (or_grid **)malloc(sizeof(or_grid *) * (size_t)n);
+    memcpy(c->g, grids, sizeof(or_grid *) * (size_t)n);
+    c->nif = 2 * (n - 1);
+    c->ifs = (or_iface *)calloc((size_t)c->nif, sizeof(or_iface));
+    for (int k = 1; k < n; k++) {
+        const or_spline *P = grids[k - 1]->spl[0], *S = grids[k]->spl[0];
+        if (fabs(P->DX / S->DX - 1.0) < 1e-12 * (P->DX > S->DX ? P->DX : S->DX)) {
+            set_err("PatchEmbedded requires refinement at each level (grids %d and %d have DX=%g)", k, k + 1, P->DX);
+            free(c->ifs); free(c->g); free(c);
+            return SS_BAD_ARG;
+        }
+        for (int side = 0; side < 2; side++) {
+            or_iface *f = &c->ifs[2 * (k - 1) + side];
+            f->primary = k - 1;
+            f->secondary = k;
+            f->pside = side == 0 ? 1 : 0;  /* (outer, inner, :right, :left), then (:left, :right) */
+            f->sside = side == 0 ? 0 : 1;
+            int st = coupling_matrix(P->DX, S->DX, f->C);
+            if (st) { free(c->ifs); free(c->g); free(c); return st; }
+            for (int v = 0; v < grids[0]->nvars; v++)
+                if (!grids[k]->spl[v]->r3x) {
+                    set_err("embedded grid %d needs R3X (FixedBC) at both ends", k + 1);
+                    free(c->ifs); free(c->g); free(c);
+                    return SS_UNSUPPORTED_BC;
+                }
+            const double xb = f->sside == 0 ? S->xmin : S->xmax;
+            const long m = lround((xb - P->xmin) / P->DX);
+            const double xn = P->xmin + (double)m * P->DX;
+            if (fabs(xn - xb) > 1e-12 * P->DX || m + 1 < 1 || m + 1 > P->bDim - 2) {
+                set_err("inner boundary %g does not align with a node of its parent", xb);
+                free(c->ifs); free(c->g); free(c);
+                return SS_BAD_ARG;
+            }
+            /* node index m + 2 (1-based) and its neighbours, 0-based */
+            f->node[0] = (int)m; f->node[1] = (int)m + 1; f->node[2] = (int)m + 2;
+        }
+    }
+    c->layer_of = (int *)calloc((size_t)n, sizeof(int));
+    for (int i = 0; i < n; i++) c->layer_of[i] = i;  /* outer → inner */
+    c->nlayers = n;
+    c->state = (double **)calloc((size_t)n, sizeof(double *));
+    for (int i = 0; i < n; i++)
+        c->state[i] = (double *)calloc((size_t)grids[i]->nvars * 3 * grids[i]->b, sizeof(double));
+    *out = c;
+    return SS_OK;
+}
+
 void or_chain_destroy(or_chain *c) {
     if (!c) return;
     for (int i = 0; i < c->n; i++) free(c->state[i]);
@@ -1564,7 +1626,10 @@ static void chain_update_interface(or_chain *c, const or_iface *f, const double 
             for (int q = 0; q <= 2 * Kc; q++) {
                 /* q: 0 = k0, odd = real k=(q+1)/2, even = imag */
                 int obj = (q == 0) ? 0 : ((q & 1) ? 1 : 2);
-                spline_sa(P->spl[v], sp + ((size_t)zb * (1 + 2 * Kp) + q) * bp, NULL, a, t, t + bp, t + 2 * bp);
+                /* SAtransform!(primary spline object): an R3X primary (an inner grid of an
+                 * embedded multigrid) solves with that object's current background */
+                const double *pah = P->spl[v]->r3x ? c->state[f->primary] + ((size_t)v * 3 + obj) * bp : NULL;
+                spline_sa(P->spl[v], sp + ((size_t)zb * (1 + 2 * Kp) + q) * bp, pah, a, t, t + bp, t + 2 * bp);
                 double ex[3] = {a[f->node[0]], a[f->node[1]], a[f->node[2]]};
                 double *st = c->state[f->secondary] + ((size_t)v * 3 + obj) * bs;
                 double *dst = (f->sside == 0) ? st : st + bs - 3;

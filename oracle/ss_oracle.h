@@ -46,6 +46,7 @@ int32_t or_grid_factor(const or_grid *g, int32_t var, double *L4, int32_t *n_out
 /* RL multi-patch chain (PatchChain + multiGridTransform!, src/multipatch.jl) */
 typedef struct or_chain or_chain;
 int32_t or_chain_create(or_grid **grids, int32_t n, or_chain **out);
+int32_t or_chain_create_embedded(or_grid **grids, int32_t n, or_chain **out);
 void or_chain_destroy(or_chain *c);
 /* spectral[i] / physical[i]: arrays of patch i (layouts as or_grid_transform) */
 int32_t or_multi_grid_transform(or_chain *c, const double **spectral, double **physical);

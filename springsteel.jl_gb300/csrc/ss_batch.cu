@@ -496,8 +496,12 @@ struct ss_chain {
 
 static double grid_DX(const ss_grid *g) { return (g->p.iMax - g->p.iMin) / g->p.num_cells; }
 
-extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **out) {
-    if (!out || !grids || n < 2) { set_error("PatchChain requires at least 2 grids, got %d", n); return SS_BAD_ARG; }
+// PatchChain (embedded = false) or PatchEmbedded (embedded = true)
+static int32_t chain_build(ss_grid *const *grids, int32_t n, bool embedded, ss_chain **out) {
+    if (!out || !grids || n < 2) {
+        set_error("%s requires at least 2 grids, got %d", embedded ? "PatchEmbedded" : "PatchChain", n);
+        return SS_BAD_ARG;
+    }
     *out = nullptr;
     for (int i = 0; i < n; i++) {
         if (!grids[i] || grids[i]->rlz != grids[0]->rlz || grids[i]->d.nvars != grids[0]->d.nvars ||
@@ -516,7 +520,49 @@ extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **
     cudaSetDevice(c->device);
     for (int i = 0; i < n; i++) c->g.push_back(grids[i]);
     const int nv = (int)grids[0]->d.nvars;
-    for (int k = 0; k < n - 1; k++) {
+    for (int k = 0; embedded && k < n - 1; k++) {
+        // PatchEmbedded (src/multipatch.jl:891-925): the inner grid k+1 takes R3X data
+        // from grid k at both ends through stacked interfaces whose primary nodes sit
+        // at the inner boundary (_compute_primary_node_index, :190-207, 270-276)
+        const ss_grid *P = grids[k], *S = grids[k + 1];
+        const double pDX = grid_DX(P), sDX = grid_DX(S), ratio = pDX / sDX;
+        if (std::fabs(ratio - 1.0) < 1e-12 * std::max(pDX, sDX)) {
+            delete c;
+            set_error("PatchEmbedded requires refinement at each level (grids %d and %d have DX=%g)", k + 1, k + 2, pDX);
+            return SS_BAD_ARG;
+        }
+        if (std::fabs(ratio - 2.0) >= 1e-12 * std::max(pDX, sDX)) {
+            delete c;
+            set_error("Only 1:1 and 2:1 coarse-to-fine ratios are supported, got %g:1", ratio);
+            return SS_BAD_ARG;
+        }
+        for (int v = 0; v < nv; v++)
+            if (!S->spl_host[v].r3x) {
+                delete c;
+                set_error("embedded grid %d needs R3X (FixedBC) at both ends", k + 2);
+                return SS_UNSUPPORTED_BC;
+            }
+        for (int side = 0; side < 2; side++) {  // (outer, inner, :right, :left), then (:left, :right)
+            IfaceDev f{};
+            f.primary = k;
+            f.secondary = k + 1;
+            f.pside = side == 0 ? 1 : 0;
+            f.sside = side == 0 ? 0 : 1;
+            static const double M2[9] = {0.5, 0.5, 0.0, 0.125, 0.75, 0.125, 0.0, 0.5, 0.5};
+            std::memcpy(f.C, M2, sizeof M2);
+            const double xb = f.sside == 0 ? S->p.iMin : S->p.iMax;
+            const long m = std::lround((xb - P->p.iMin) / pDX);
+            const double xn = P->p.iMin + (double)m * pDX;
+            if (std::fabs(xn - xb) > 1e-12 * pDX || m < 0 || m + 2 > (long)P->d.b_iDim - 1) {
+                delete c;
+                set_error("inner boundary %g does not align with a node of its parent", xb);
+                return SS_BAD_ARG;
+            }
+            f.node[0] = (int)m; f.node[1] = (int)m + 1; f.node[2] = (int)m + 2;
+            c->ifs.push_back(f);
+        }
+    }
+    for (int k = 0; !embedded && k < n - 1; k++) {
         IfaceDev f{};
         // PatchChain (src/multipatch.jl:825-848): the coarser side is primary
         if (grid_DX(grids[k]) >= grid_DX(grids[k + 1])) { f.primary = k; f.secondary = k + 1; f.pside = 1; f.sside = 0; }
@@ -589,6 +635,14 @@ extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **
     return SS_OK;
 }
 
+extern "C" int32_t ss_chain_create(ss_grid *const *grids, int32_t n, ss_chain **out) {
+    return chain_build(grids, n, false, out);
+}
+
+extern "C" int32_t ss_chain_create_embedded(ss_grid *const *grids, int32_t n, ss_chain **out) {
+    return chain_build(grids, n, true, out);
+}
+
 extern "C" int32_t ss_chain_destroy(ss_chain *c) {
     if (!c) return SS_OK;
     cudaSetDevice(c->device);
@@ -622,6 +676,7 @@ static int32_t update_interface(ss_chain *c, const IfaceDev &f, cudaStream_t st)
     L.zblk_p = 1 + 2 * (int)P->d.kDim_wn;
     L.zblk_s = 1 + 2 * (int)S->d.kDim_wn;
     L.side = f.sside;
+    L.pstate = c->state[f.primary];
     for (int i = 0; i < 3; i++) L.node[i] = f.node[i];
     std::memcpy(L.C, f.C, sizeof L.C);
     int nmax = 0;

@@ -1127,9 +1127,22 @@ __global__ void __launch_bounds__(32) chain_couple_kernel(ChainLaunch C) {
     __syncthreads();
     if (threadIdx.x < nsl) {
         double *x = X + threadIdx.x * ld;
+        // an R3X primary solves with its spline object's background, as
+        // SAtransform!(spline) does: k0 / real / imag objects by slot parity
+        const int q = q0 + threadIdx.x;
+        const double *ah = (sp.r3x && C.pstate) ? C.pstate + ((size_t)v * 3 + (q == 0 ? 0 : ((q & 1) ? 1 : 2))) * b
+                                                : nullptr;
+        if (ah)  // b̃ = b − PQ·ahat (full P+Q band)
+            for (int i = 0; i < b; i++) {
+                double acc = 0.0;
+                for (int j = max(0, i - 3); j <= min(b - 1, i + 3); j++) acc += sp.PQb[i * 7 + (j - i + 3)] * ah[j];
+                x[i] -= acc;
+            }
         gamma_fold(sp, x, b, n);
         band_solve(Ls, Di, x, n, sp.periodic ? sp.tail : nullptr);
         gamma_unfold(sp, x, b, n);
+        if (ah)
+            for (int i = 0; i < b; i++) x[i] += ah[i];
         const double e0 = x[C.node[0]], e1 = x[C.node[1]], e2 = x[C.node[2]];
         double *out = C.coupled + ((size_t)item * C.nq + q0 + threadIdx.x) * 3;
         for (int r = 0; r < 3; r++) out[r] = C.C[r * 3] * e0 + C.C[r * 3 + 1] * e1 + C.C[r * 3 + 2] * e2;

@@ -85,6 +85,8 @@ struct ChainLaunch {
     const SplineDev *spl;      // primary splines (per variable)
     double *coupled;           // [v][q][3] coupled border coefficients
     double *state;             // secondary spline-object ahat: [v][3][b_s] (k0, real, imag)
+    const double *pstate;      // the primary's spline-object ahat [v][3][b_p] (used when the primary is
+                               // itself R3X, an inner grid of an embedded multigrid)
     double *reg;               // secondary per-wavenumber registry: [v][nblocks_s][b_s]
     int64_t nspec_p, nblocks_s;
     int b_p, b_s, ld, nq, nvars, side;  // side of the secondary: 0 left, 1 right

@@ -657,6 +657,46 @@ class PatchChain:
             pass
 
 
+class PatchEmbedded(PatchChain):
+    """PatchEmbedded(grids) (src/multipatch.jl:891-925) on the device: grids nested
+    outermost first; each inner grid receives R3X data from its parent at both ends."""
+
+    def __init__(self, grids):
+        self.patches = list(grids)
+        lib = load_library()
+        arr = (C.c_void_p * len(self.patches))(*[g.handle for g in self.patches])
+        h = C.c_void_p()
+        _check(lib.ss_chain_create_embedded(arr, len(self.patches), C.byref(h)))
+        self._h = h
+
+
+def embedded_grid_params(domains, cells, vars=None, BCL=None, BCR=None, mubar=3, l_q=None, precision="f64",
+                         geometry="RL", **column):
+    """Per-grid parameters of an embedded multigrid (_create_embedded,
+    src/multipatch.jl:1113-1190): domains outermost first, each contained in its
+    parent and strictly finer; the outer grid keeps BCL/BCR, inner grids get
+    FixedBC (R3X) at both ends; patch offsets from the domain starts."""
+    n = len(domains)
+    cells = [cells] * n if isinstance(cells, int) else list(cells)
+    vars = vars or {"u": 1}
+    for k in range(1, n):
+        if not (domains[k][0] >= domains[k - 1][0] and domains[k][1] <= domains[k - 1][1]):
+            raise ValueError("Domain %d %s not contained in domain %d %s" % (k + 1, domains[k], k, domains[k - 1]))
+    dx = [(domains[k][1] - domains[k][0]) / cells[k] for k in range(n)]
+    for k in range(1, n):
+        if abs(dx[k - 1] / dx[k] - 1.0) < 1e-10 * max(dx[k - 1], dx[k]):
+            raise ValueError("Embedded requires strict refinement. Domains %d and %d have same DX=%g" % (k, k + 1, dx[k]))
+    offs = compute_patch_offsets([d[0] for d in domains] + [domains[-1][1]], cells, mubar)
+    out = []
+    for k in range(n):
+        bl = (BCL or {"default": NaturalBC()}) if k == 0 else {"default": FixedBC()}
+        br = (BCR or {"default": NaturalBC()}) if k == 0 else {"default": FixedBC()}
+        out.append(SpringsteelGridParameters(geometry=geometry, iMin=domains[k][0], iMax=domains[k][1],
+                                             num_cells=cells[k], mubar=mubar, vars=vars, BCL=bl, BCR=br, l_q=l_q,
+                                             patchOffsetL=offs[k], precision=precision, **column))
+    return out
+
+
 def compute_patch_offsets(boundaries, cells, mubar=3):
     """_compute_patch_offsets (src/multipatch.jl:998-1014) for cylindrical grids."""
     offsets, cumulative = [], 0

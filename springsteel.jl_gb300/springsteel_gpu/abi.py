@@ -163,7 +163,7 @@ EXPORTED = [
     "ss_spectral_transform_noalloc", "ss_regular_grid_transform", "ss_spline_transform", "ss_tile_transform",
     "ss_grid_save", "ss_grid_load", "ss_grid_load_arrays", "ss_grid_archive_user",
     "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads", "ss_batch_fused_launches",
-    "ss_chain_create", "ss_chain_destroy", "ss_multi_grid_transform",
+    "ss_chain_create", "ss_chain_create_embedded", "ss_chain_destroy", "ss_multi_grid_transform",
     "ss_tile_sum_spectral", "ss_tile_copy_physical", "ss_grid_zero_spectral",
     "ss_problem_create", "ss_problem_destroy", "ss_problem_dims", "ss_problem_operator_band",
     "ss_problem_set_mlp", "ss_solve", "ss_problem_export", "ss_problem_collect_training",
@@ -235,6 +235,7 @@ def bind(lib):
         "ss_batch_synchronize": ([vp], i32),
         "ss_batch_ring_threads": ([vp, i32, C.POINTER(i32), C.POINTER(i32)], i32),
         "ss_chain_create": ([vp, i32, C.POINTER(vp)], i32),
+        "ss_chain_create_embedded": ([vp, i32, C.POINTER(vp)], i32),
         "ss_chain_destroy": ([vp], i32),
         "ss_multi_grid_transform": ([vp, vp], i32),
         "ss_tile_sum_spectral": ([vp, vp, i32, vp], i32),

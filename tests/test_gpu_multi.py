@@ -262,3 +262,47 @@ def test_fused_batch_config3_range_matches_oracle(precision):
     plain.synchronize()
     for g, out in zip(grids, outs):
         assert np.array_equal(g.get_physical(), out)
+
+
+def test_embedded_three_level_linear_exactness():
+    """PatchEmbedded (src/multipatch.jl:891-925; test/multipatch.jl:1121-1164): radial
+    splines nested [0, 30] ⊃ [10, 20] ⊃ [13, 17] (DX 1, 0.5, 0.25), l_q = 0; f = 2r + 1
+    is reproduced to 1e-10 on every level, the inner grids through R3X data at both ends."""
+    ps = S.embedded_grid_params([(0.0, 30.0), (10.0, 20.0), (13.0, 17.0)], [30, 20, 16], l_q={"default": 0.0},
+                                BCL={"default": S.R0}, BCR={"default": S.R0})
+    gs = [S.createGrid(p) for p in ps]
+    for g in gs:
+        pts = S.getGridpoints(g)
+        g.set_physical((2 * pts[:, 0] + 1)[:, None], slot=1)
+        S.spectralTransform_b(g)
+    S.PatchEmbedded(gs).multiGridTransform()
+    for g in gs:
+        pts = S.getGridpoints(g)
+        assert np.max(np.abs(g.get_physical()[:, 0, 0] - (2 * pts[:, 0] + 1))) < 1e-10
+
+
+@pytest.mark.parametrize("geometry", ["RL", "RLZ"])
+def test_embedded_parity(geometry):
+    """Embedded multigrid against the oracle's (two levels, two variables), twice in
+    a row: the second run sees the spline-object backgrounds the first left."""
+    col = {} if geometry == "RL" else dict(kMin=0.0, kMax=2000.0, kDim=12, BCB={"default": S.DirichletBC()},
+                                           BCT={"default": S.NeumannBC()})
+    ps = S.embedded_grid_params([(0.0, 36.0), (12.0, 24.0), (15.0, 21.0)], [18, 12, 12], vars={"u": 1, "w": 2},
+                                geometry=geometry, **col)
+    gs = [S.createGrid(p) for p in ps]
+    os_ = [O.OracleGrid(p.to_abi()) for p in ps]
+    specs = []
+    for i, (g, o) in enumerate(zip(gs, os_)):
+        u = _fill(g, seed=60 + i)
+        ph = np.zeros(o.physical_shape, order="F")
+        ph[:, :, 0] = u
+        specs.append(o.spectral_transform(ph))
+        S.spectralTransform_b(g)
+    emb = S.PatchEmbedded(gs)
+    och = O.OracleChain(os_, embedded=True)
+    for _ in range(2):
+        emb.multiGridTransform()
+        ref = och.multi_grid_transform(specs)
+        for p, g, r in zip(ps, gs, ref):
+            errs = slot_errors(g.get_physical(), r, p)
+            assert np.all(errs <= TOL64), errs

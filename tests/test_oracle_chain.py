@@ -104,3 +104,31 @@ def test_oracle_tiles_sum_to_patch_spectral():
                 acc[p0:p0 + bt, 0] += st[t0:t0 + bt, 0]
     assert row == og.dims["n_physical"]
     assert np.max(np.abs(acc - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_embedded_three_level_linear_exactness():
+    # test/multipatch.jl:1121-1164 (R geometry there; radial splines of an RL grid
+    # here): outer [0, 30] 30 cells, mid [10, 20] 20 cells, inner [13, 17] 16 cells,
+    # l_q = 0, f = 2r + 1 reproduced to 1e-10 on every level
+    ps = S.embedded_grid_params([(0.0, 30.0), (10.0, 20.0), (13.0, 17.0)], [30, 20, 16], l_q={"default": 0.0},
+                                BCL={"default": S.R0}, BCR={"default": S.R0})
+    gs = [O.OracleGrid(p.to_abi()) for p in ps]
+    sp = []
+    for g in gs:
+        pts = g.gridpoints()
+        ph = np.zeros(g.physical_shape, order="F")
+        ph[:, 0, 0] = 2 * pts[:, 0] + 1
+        sp.append(g.spectral_transform(ph))
+    out = O.OracleChain(gs, embedded=True).multi_grid_transform(sp)
+    for g, o in zip(gs, out):
+        pts = g.gridpoints()
+        assert np.max(np.abs(o[:, 0, 0] - (2 * pts[:, 0] + 1))) < 1e-10
+
+
+def test_embedded_rejects_equal_resolution_and_misalignment():
+    # test/multipatch.jl:1108-1118, 429-443
+    with pytest.raises(ValueError):
+        S.embedded_grid_params([(0.0, 30.0), (10.0, 20.0)], [30, 10])
+    ps = S.embedded_grid_params([(0.0, 30.0), (10.25, 20.25)], [30, 20])
+    with pytest.raises(O.OracleError):
+        O.OracleChain([O.OracleGrid(p.to_abi()) for p in ps], embedded=True)
