@@ -268,6 +268,32 @@ int32_t ss_tile_transform(ss_grid *grid, void *stream);
 int32_t ss_regular_grid_transform(ss_grid *grid, const double *r_pts, int32_t n_r, const double *lam_pts,
                                   int32_t n_lam, const double *z_pts, int32_t n_z, double *out, void *stream);
 
+/* evaluate_unstructured(grid, pts; out_of_bounds) (src/interpolation.jl:1735-1850;
+ * RL :1628-1656, RLZ :1670-1718): the device-resident spectral array evaluated at
+ * npts arbitrary points.  `pts` is column-major npts × 2 (r, λ) or npts × 3
+ * (r, λ, z); `out` a host array npts × nvars (column-major).  Per point:
+ * SAtransform! of every block (FP64, no R3X background, as regularGridTransform),
+ * the 4-tap spline value at r, the Fourier series at λ with the factor 2 for
+ * k ≥ 1, and for RLZ CAtransform! plus the Chebyshev series at z (clamped to the
+ * column).  Points with r outside [iMin, iMax] (or z outside [kMin, kMax]) get
+ * NaN (out_of_bounds 0), make the call fail with SS_BAD_ARG (1), or get `fill` (2).
+ * Returns once `out` holds the result. */
+int32_t ss_evaluate_unstructured(ss_grid *grid, const double *pts, int64_t npts, double *out,
+                                 int32_t out_of_bounds, double fill, void *stream);
+/* relocate_grid(grid, (dx, dy); boundary, taper_width) fast path
+ * (src/relocation.jl:144-439): every gridpoint (r, λ[, z]) of `target` takes the
+ * source's value at the shifted position x = r cos λ + dx, y = r sin λ + dy; then
+ * spectralTransform! and gridTransform! of the target.  Points mapped beyond
+ * [iMin, iMax] take NaN (boundary 0), the value at the clamped radius (1, :nearest)
+ * or the azimuthal mean there (2, :azimuthal_mean); taper_width > 0 blends the
+ * last taper_width cells toward the azimuthal mean with a cosine weight.
+ * `target` has the source's parameters; target == source relocates in place
+ * (relocate_grid!: the source is read before the target is written).  The work
+ * is queued on `stream` (NULL: the target's stream) once the source's stream
+ * has drained. */
+int32_t ss_relocate_grid(ss_grid *target, ss_grid *source, double dx, double dy, int32_t boundary,
+                         int32_t taper_width, void *stream);
+
 /* ---- stage timing (the library's own instrumentation; no reference
  * counterpart: the reference times whole calls with BenchmarkTools,
  * bench/bench_grids.jl:20-38).  With profiling on, CUDA events bracket every

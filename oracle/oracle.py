@@ -555,3 +555,113 @@ def regular_grid_transform(params, spectral, r_pts, lam_pts, z_pts=None):
                 s = slot if i == 0 else 4 + i
                 out[:, v, s] = np.einsum("zn,rln->rlz", M, coef).reshape(-1)
     return out
+
+
+# ---------------------------------------------------------------- unstructured points, relocation
+def _cheb_value_rows(N, zmin, zmax, z):
+    """_cheb_eval_single (src/interpolation.jl:1271-1285): weights of the A-coefficients
+    for the value at z, ξ clamped to [−1, 1]."""
+    scale, offset = -0.5 * (zmax - zmin), 0.5 * (zmin + zmax)
+    t = np.arccos(np.clip((np.asarray(z, np.float64) - offset) / scale, -1.0, 1.0))
+    E = 2.0 * np.cos(np.outer(t, np.arange(N, dtype=np.float64)))
+    E[:, 0] = 1.0
+    E[:, N - 1] = np.cos((N - 1) * t)
+    return E
+
+
+def _point_values(p, sp, spec_v, r, lam, mean_only=None):
+    """Per Chebyshev mode, the Fourier series of the SI values at each point's own
+    (r, λ) (src/interpolation.jl:1628-1656, 1670-1702): (n_pts, bk) values; rows
+    flagged in mean_only keep the k = 0 term."""
+    nc, mubar = p.num_cells, p.mubar
+    b = nc + 3
+    kdim = nc * mubar + p.patchOffsetL
+    nslot = 1 + 2 * kdim
+    bk = 1 if p.geometry == abi.SS_GEOM_RL else (p.b_kDim if p.b_kDim > 0 else min(p.kDim, (2 * p.kDim - 1) // 3 + 1))
+    k = np.arange(1, kdim + 1, dtype=np.float64)
+    c, s = np.cos(np.outer(lam, k)), np.sin(np.outer(lam, k))
+    out = np.zeros((len(r), bk))
+    for zb in range(bk):
+        sv = np.zeros((len(r), nslot))
+        for q in range(nslot):
+            a = sp.sa(spec_v[(zb * nslot + q) * b:(zb * nslot + q + 1) * b])
+            sv[:, q] = sp.si(a, 0, r)
+        full = sv[:, 0] + 2.0 * np.sum(sv[:, 1::2] * c + sv[:, 2::2] * s, axis=1)
+        out[:, zb] = np.where(mean_only, sv[:, 0], full) if mean_only is not None else full
+    return out
+
+
+def evaluate_unstructured(params, spectral, pts, out_of_bounds="nan"):
+    """evaluate_unstructured (src/interpolation.jl:1735-1850) for RL / RLZ grids: (N, nvars)."""
+    p = params.params
+    pts = np.asarray(pts, np.float64)
+    spec = np.asarray(spectral, np.float64)
+    mask = (pts[:, 0] >= p.iMin) & (pts[:, 0] <= p.iMax)
+    if p.geometry == abi.SS_GEOM_RLZ:
+        mask &= (pts[:, 2] >= p.kMin) & (pts[:, 2] <= p.kMax)
+    if out_of_bounds == "error" and not mask.all():
+        raise ValueError("%d points are outside the source domain" % int((~mask).sum()))
+    out = np.full((pts.shape[0], p.nvars), np.nan)
+    ib = np.nonzero(mask)[0]
+    for v, sp in enumerate(_grid_splines(p)):
+        if len(ib):
+            f = _point_values(p, sp, spec[:, v], pts[ib, 0], pts[ib, 1])
+            if p.geometry == abi.SS_GEOM_RL:
+                out[ib, v] = f[:, 0]
+            else:
+                N = p.kDim
+                bk = f.shape[1]
+                CA = np.column_stack([cheb_ca(np.eye(bk)[i], N, int(p.BCB[v]) if p.BCB else 0,
+                                              int(p.BCT[v]) if p.BCT else 0) for i in range(bk)])
+                A = f @ CA.T  # (n, N) A-coefficients per point
+                out[ib, v] = np.sum(_cheb_value_rows(N, p.kMin, p.kMax, pts[ib, 2]) * A, axis=1)
+        if out_of_bounds not in ("nan", "error"):
+            out[~mask, v] = float(out_of_bounds)
+    return out
+
+
+def relocated_slot1(params, spectral, gridpoints, dx, dy, boundary="azimuthal_mean", taper_width=0):
+    """Physical slot 1 of the relocated grid before its transforms (_relocate_rl_fast! /
+    _relocate_rlz_fast!, src/relocation.jl:144-439): each gridpoint takes the source's
+    value at (r cos λ + dx, r sin λ + dy); out-of-range radii per `boundary`
+    ("nan", "nearest", "azimuthal_mean"), cosine taper toward the mean over the last
+    `taper_width` cells."""
+    p = params.params
+    spec = np.asarray(spectral, np.float64)
+    gp = np.asarray(gridpoints, np.float64)
+    rlz = p.geometry == abi.SS_GEOM_RLZ
+    kz = p.kDim if rlz else 1
+    ring = gp[::kz]  # one row per ring point
+    xo = ring[:, 0] * np.cos(ring[:, 1]) + dx
+    yo = ring[:, 0] * np.sin(ring[:, 1]) + dy
+    ro = np.hypot(xo, yo)
+    lo = np.arctan2(yo, xo)
+    oob = (ro > p.iMax) | (ro < p.iMin)
+    rs = np.where(oob, np.clip(ro, p.iMin + 1e-10, p.iMax - 1e-10), ro)
+    DX = (p.iMax - p.iMin) / p.num_cells
+    start = p.iMax - taper_width * DX if taper_width > 0 else p.iMax
+    w = np.ones(len(rs))
+    tap = (~oob) & (taper_width > 0) & (rs > start)
+    w[tap] = 0.5 * (1.0 + np.cos(np.pi * (rs[tap] - start) / (p.iMax - start)))
+    out = np.zeros((gp.shape[0], p.nvars))
+    for v, sp in enumerate(_grid_splines(p)):
+        full = _point_values(p, sp, spec[:, v], rs, lo, mean_only=oob & (boundary == "azimuthal_mean"))
+        mean = _point_values(p, sp, spec[:, v], rs, lo, mean_only=np.ones(len(rs), bool))
+        if not rlz:
+            val = w * full[:, 0] + (1.0 - w) * mean[:, 0]
+            val[oob] = full[oob, 0]
+            if boundary == "nan":
+                val[oob] = np.nan
+            out[:, v] = val
+            continue
+        N, bk = p.kDim, full.shape[1]
+        CA = np.column_stack([cheb_ca(np.eye(bk)[i], N, int(p.BCB[v]) if p.BCB else 0,
+                                      int(p.BCT[v]) if p.BCT else 0) for i in range(bk)])
+        E = _cheb_value_rows(N, p.kMin, p.kMax, gp[:kz, 2])  # (kz, N): the column's levels
+        vf = (full @ CA.T) @ E.T  # (n_ring, kz)
+        vm = (mean @ CA.T) @ E.T
+        val = np.where(tap[:, None], w[:, None] * vf + (1.0 - w[:, None]) * vm, vf)
+        if boundary == "nan":
+            val[oob] = np.nan
+        out[:, v] = val.reshape(-1)
+    return out

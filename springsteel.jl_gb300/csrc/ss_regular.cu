@@ -153,6 +153,100 @@ __global__ void reg_cheb_kernel(const double *fb, const double *mats, double *ou
     (void)n_r;
 }
 
+// Value of the spectral fields at arbitrary points: one warp per (point, variable).
+// Per Chebyshev mode z_b the warp sums the Fourier series of the SI values at the
+// point's radius (4-tap window m0, weights w):
+//   f_zb = S_0 + 2 Σ_k (S_{2k−1} cos kλ + S_{2k} sin kλ),  S_q = Σ_tap w_tap a_q[m0 + tap]
+// (src/interpolation.jl:1628-1656 RL, 1670-1718 RLZ).  mode 1 keeps the k = 0
+// term only (the azimuthal mean), mode 2 writes NaN; taper t blends
+// t·full + (1 − t)·mean (src/relocation.jl:252-258).  RL: one value per point.
+// RLZ: CAtransform! of f_zb (the composed matrix CA, N × bk) and the Chebyshev
+// series at z (_cheb_eval_single, src/interpolation.jl:1271-1285) — at the
+// point's own z (zcol = nullptr) or at the n_z column levels zcol (relocation).
+struct PointArgs {
+    const double *coef;   // [item][slot][b] spline coefficients (FP64)
+    const double *lam, *z, *w, *taper;  // per point; z RLZ only; w[p][4]
+    const int *m0, *mode;
+    const double *ca;     // RLZ: per variable N × bk
+    const double *zcol;   // RLZ relocation: n_z column levels, else null
+    void *out;            // P storage
+    int64_t npts, ostride_v;  // rows between variables of out
+    int b, nslots, K, bk, nvars, N, n_z, rlz, out_f32;
+    double zmin, zmax;
+    int first_var, nvar_eval;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(128) point_eval_kernel(PointArgs A) {
+    extern __shared__ __align__(16) double fz[];  // per warp: bk values
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    const int64_t p = gw / A.nvar_eval;
+    if (p >= A.npts) return;  // whole warps leave together (no block barrier below)
+    const int v = A.first_var + (int)(gw - p * A.nvar_eval);
+    double *f = fz + (size_t)wib * A.bk;
+    const int mode = A.mode ? A.mode[p] : 0;
+    auto store = [&](int64_t row, double val) {
+        if (A.out_f32) ((float *)A.out)[(size_t)v * A.ostride_v + row] = (float)val;
+        else ((double *)A.out)[(size_t)v * A.ostride_v + row] = val;
+    };
+    const int nout = A.rlz && A.zcol ? A.n_z : 1;
+    const int64_t row0 = A.rlz && A.zcol ? p * A.n_z : p;
+    if (mode == 2) {
+        if (lane < nout) store(row0 + lane, __longlong_as_double(0x7ff8000000000000LL));
+        for (int q = lane + 32; q < nout; q += 32) store(row0 + q, __longlong_as_double(0x7ff8000000000000LL));
+        return;
+    }
+    const double lam = A.lam[p], t = A.taper ? A.taper[p] : 1.0;
+    const double w0 = A.w[p * 4], w1 = A.w[p * 4 + 1], w2 = A.w[p * 4 + 2], w3 = A.w[p * 4 + 3];
+    const int m0 = A.m0[p];
+    for (int zb = 0; zb < A.bk; zb++) {
+        const double *a = A.coef + ((size_t)(v * A.bk + zb) * A.nslots) * A.b + m0;
+        auto si = [&](int q) {
+            const double *c = a + (size_t)q * A.b;
+            return w0 * c[0] + w1 * c[1] + w2 * c[2] + w3 * c[3];
+        };
+        double full = 0.0;
+        if (mode == 0)
+            for (int k = 1 + lane; k <= A.K; k += 32) {
+                double sk, ck;
+                sincos((double)k * lam, &sk, &ck);
+                full += 2.0 * (si(2 * k - 1) * ck + si(2 * k) * sk);
+            }
+        full = warp_sum(full);
+        const double mean = si(0);
+        const double val = (mode == 1) ? mean : (t * (mean + full) + (1.0 - t) * mean);
+        if (lane == 0) f[zb] = val;
+    }
+    __syncwarp();
+    if (!A.rlz) {
+        if (lane == 0) store(p, f[0]);
+        return;
+    }
+    // CAtransform! then the Chebyshev series (clamped to [−1, 1]) at each level
+    const double scale = -0.5 * (A.zmax - A.zmin), offset = 0.5 * (A.zmin + A.zmax);
+    const double *ca = A.ca + (size_t)v * A.N * A.bk;
+    for (int zi = 0; zi < nout; zi++) {
+        const double z = A.zcol ? A.zcol[zi] : A.z[p];
+        const double xi = fmin(fmax((z - offset) / scale, -1.0), 1.0);
+        const double th = acos(xi);
+        double acc = 0.0;
+        for (int n = lane; n < A.N; n += 32) {
+            double an = 0.0;
+            for (int i = 0; i < A.bk; i++) an += ca[(size_t)n * A.bk + i] * f[i];
+            const double e = (n == 0) ? 1.0 : (n == A.N - 1 ? cos((double)n * th) : 2.0 * cos((double)n * th));
+            acc += e * an;
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) store(row0 + zi, acc);
+    }
+}
+
 // E (value), Dz, Dzz of the DCT-I series at z (n_z × N, row-major) with the
 // reference's clamps (_cheb_eval_pts!, _cheb_dz_pts!, _cheb_dzz_pts!,
 // src/transforms_cylindrical.jl:1030-1094)
@@ -313,6 +407,193 @@ int32_t regular(ss_grid *g, const double *r_pts, int n_r, const double *lam_pts,
     return rc;
 }
 
+// Spline coefficients of every spectral block of `src` (FP64, [item][slot][b]) into a
+// fresh device buffer (the caller frees it)
+template <typename P>
+int32_t block_coefficients(ss_grid *src, double **d_coef, cudaStream_t st) {
+    const ss_dims &d = src->d;
+    const int b = (int)d.b_iDim, ns = src->nslots_z, bk = (int)d.b_kDim;
+    int nmax = 0;
+    for (auto &sh : src->spl_host) nmax = std::max(nmax, sh.Min);
+    const int ld = (b % 2) ? b : b + 1;
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, src->device);
+    int per = 32;
+    auto sa_smem = [&](int q) { return (size_t(q) * ld + size_t(5) * nmax) * 8; };
+    while (per > 1 && sa_smem(per) > (size_t)optin) per /= 2;
+    if (sa_smem(per) > (size_t)optin) {
+        set_error("%d radial coefficients exceed shared memory", b);
+        return SS_BAD_SHAPE;
+    }
+    CUDA_TRY(cudaMalloc(d_coef, size_t(src->nitems) * ns * b * 8));
+    CUDA_TRY(cudaFuncSetAttribute(reg_sa_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa_smem(per)));
+    reg_sa_kernel<P><<<dim3((ns + per - 1) / per, src->nitems), per, sa_smem(per), st>>>(
+        (const P *)src->spec, src->d_spl, *d_coef, d.n_spectral, b, ld, ns, bk);
+    CUDA_TRY(cudaGetLastError());
+    return SS_OK;
+}
+
+// The point kernel over host-described points: radii r (SI windows built here),
+// angles, optional z, modes and taper weights; `out` is device memory
+int32_t eval_points(ss_grid *g, const double *coef, const std::vector<double> &r, const std::vector<double> &lam,
+                    const std::vector<double> &z, const std::vector<int> &mode, const std::vector<double> &taper,
+                    const std::vector<double> &zcol, void *out, int64_t ostride_v, int out_f32, cudaStream_t st) {
+    const ss_dims &d = g->d;
+    const int64_t npts = (int64_t)r.size();
+    if (npts == 0) return SS_OK;
+    std::vector<int> m0;
+    std::vector<double> w3;
+    spline_point_weights(g->spl_host[0], r.data(), (int)npts, m0, w3);  // every variable shares the knots
+    std::vector<double> w(size_t(npts) * 4);
+    std::copy(w3.begin(), w3.begin() + w.size(), w.begin());  // d = 0: the value weights
+    std::vector<double> ca;
+    const int N = (int)d.kDim, bk = (int)d.b_kDim, nv = (int)d.nvars;
+    if (g->rlz) {
+        ca.assign(size_t(nv) * N * bk, 0.0);
+        for (int v = 0; v < nv; v++) {
+            ChebHost ch;
+            int32_t rc = build_cheb(N, bk, g->bcb[v], g->bct[v], g->p.kMin, g->p.kMax, ch);
+            if (rc) return rc;
+            for (int n = 0; n < N; n++)  // CA[n][i] = δ_ni + Σ_p v_p[n] u_p[i]
+                for (int i = 0; i < bk; i++) {
+                    double a = (n == i) ? 1.0 : 0.0;
+                    for (int q = 0; q < ch.nrank; q++) a += ch.gv[size_t(q) * N + n] * ch.gu[size_t(q) * bk + i];
+                    ca[(size_t(v) * N + n) * bk + i] = a;
+                }
+        }
+    }
+    std::vector<void *> bufs;
+    auto up = [&](const void *h, size_t bytes, void **dptr) -> cudaError_t {
+        if (!bytes) { *dptr = nullptr; return cudaSuccess; }
+        cudaError_t e = cudaMalloc(dptr, bytes);
+        if (e != cudaSuccess) return e;
+        bufs.push_back(*dptr);
+        return cudaMemcpyAsync(*dptr, h, bytes, cudaMemcpyHostToDevice, st);
+    };
+    PointArgs A{};
+    cudaError_t e = cudaSuccess;
+    void *p_lam, *p_z, *p_w, *p_t, *p_m0, *p_mode, *p_ca, *p_zc;
+    if ((e = up(lam.data(), lam.size() * 8, &p_lam)) || (e = up(z.data(), z.size() * 8, &p_z)) ||
+        (e = up(w.data(), w.size() * 8, &p_w)) || (e = up(taper.data(), taper.size() * 8, &p_t)) ||
+        (e = up(m0.data(), m0.size() * 4, &p_m0)) || (e = up(mode.data(), mode.size() * 4, &p_mode)) ||
+        (e = up(ca.data(), ca.size() * 8, &p_ca)) || (e = up(zcol.data(), zcol.size() * 8, &p_zc))) {
+        cudaStreamSynchronize(st);
+        for (void *q : bufs) cudaFree(q);
+        set_error("point evaluation buffers: %s", cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? SS_OUT_OF_MEMORY : SS_CUDA_ERROR;
+    }
+    A.coef = coef; A.lam = (const double *)p_lam; A.z = (const double *)p_z; A.w = (const double *)p_w;
+    A.taper = (const double *)p_t; A.m0 = (const int *)p_m0; A.mode = (const int *)p_mode;
+    A.ca = (const double *)p_ca; A.zcol = (const double *)p_zc; A.out = out;
+    A.npts = npts; A.ostride_v = ostride_v; A.b = (int)d.b_iDim; A.nslots = g->nslots_z; A.K = (int)d.kDim_wn;
+    A.bk = bk; A.nvars = nv; A.N = N; A.n_z = (int)zcol.size(); A.rlz = g->rlz; A.out_f32 = out_f32;
+    A.zmin = g->p.kMin; A.zmax = g->p.kMax; A.first_var = 0; A.nvar_eval = nv;
+    const int64_t warps = npts * nv;
+    point_eval_kernel<<<(unsigned)((warps + 3) / 4), 128, size_t(4) * bk * 8, st>>>(A);
+    e = cudaGetLastError();
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    for (void *q : bufs) cudaFree(q);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        set_error("point evaluation: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+        return SS_CUDA_ERROR;
+    }
+    return SS_OK;
+}
+
+template <typename P>
+int32_t unstructured(ss_grid *g, const double *pts, int64_t npts, double *out, int oob, double fill,
+                     cudaStream_t st) {
+    const double rmin = g->p.iMin, rmax = g->p.iMax, zmin = g->p.kMin, zmax = g->p.kMax;
+    std::vector<double> r(npts), lam(npts), z(g->rlz ? npts : 0), taper;
+    std::vector<int> mode(npts, 0);
+    int64_t n_oob = 0;
+    for (int64_t i = 0; i < npts; i++) {
+        r[i] = pts[i];
+        lam[i] = pts[npts + i];
+        bool in = r[i] >= rmin && r[i] <= rmax;  // _check_bounds_nd: Fourier λ is always in bounds
+        if (g->rlz) {
+            z[i] = pts[2 * npts + i];
+            in = in && z[i] >= zmin && z[i] <= zmax;
+        }
+        if (!in) {
+            mode[i] = 2;
+            r[i] = std::min(std::max(r[i], rmin), rmax);
+            n_oob++;
+        }
+    }
+    if (oob == 1 && n_oob) {
+        set_error("%lld points are outside the source domain", (long long)n_oob);
+        return SS_BAD_ARG;
+    }
+    const int nv = (int)g->d.nvars;
+    double *d_coef = nullptr, *d_out = nullptr;
+    int32_t rc = block_coefficients<P>(g, &d_coef, st);
+    if (rc) return rc;
+    if (cudaMalloc((void **)&d_out, size_t(npts) * nv * 8) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamSynchronize(st);
+        cudaFree(d_coef);
+        set_error("out of device memory");
+        return SS_OUT_OF_MEMORY;
+    }
+    rc = eval_points(g, d_coef, r, lam, z, mode, taper, {}, d_out, npts, 0, st);
+    if (!rc && cudaMemcpy(out, d_out, size_t(npts) * nv * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        set_error("point evaluation download: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = SS_CUDA_ERROR;
+    }
+    cudaFree(d_coef);
+    cudaFree(d_out);
+    if (!rc && oob == 2)
+        for (int64_t i = 0; i < npts; i++)
+            if (mode[i] == 2)
+                for (int v = 0; v < nv; v++) out[size_t(v) * npts + i] = fill;
+    return rc;
+}
+
+// relocate_grid / relocate_grid! fast path (src/relocation.jl:144-439): every
+// gridpoint of the target evaluates the source at its shifted position
+template <typename P>
+int32_t relocate(ss_grid *t, ss_grid *s, double dx, double dy, int boundary, int taper_width, cudaStream_t st) {
+    const ss_dims &d = s->d;
+    const double rmin = s->p.iMin, rmax = s->p.iMax;
+    const double DX = (rmax - rmin) / s->p.num_cells;
+    const double r_start = taper_width > 0 ? rmax - taper_width * DX : rmax;
+    const int64_t nring_pts = d.jDim;
+    std::vector<double> r(nring_pts), lam(nring_pts), taper(nring_pts, 1.0), zcol;
+    std::vector<int> mode(nring_pts, 0);
+    const double twopi = 2 * 3.14159265358979323846;
+    int64_t q = 0;
+    for (int ri0 = 0; ri0 < (int)d.iDim; ri0++) {
+        const int ri = ri0 + 1 + s->pOL, L = 4 + 4 * ri;
+        const double ymin = 0.5 * (twopi / L) * (ri - 1), rm = s->spl_host[0].mish[ri0];
+        for (int l = 0; l < L; l++, q++) {
+            const double ln = ymin + twopi * l / L;
+            const double xo = rm * std::cos(ln) + dx, yo = rm * std::sin(ln) + dy;
+            const double ro = std::sqrt(xo * xo + yo * yo);
+            lam[q] = std::atan2(yo, xo);
+            const bool oob = ro > rmax || ro < rmin;
+            r[q] = oob ? std::min(std::max(ro, rmin + 1e-10), rmax - 1e-10) : ro;
+            if (oob) mode[q] = boundary == 0 ? 2 : (boundary == 2 ? 1 : 0);  // nan / nearest / azimuthal mean
+            else if (taper_width > 0 && r[q] > r_start)
+                taper[q] = 0.5 * (1.0 + std::cos(3.14159265358979323846 * (r[q] - r_start) / (rmax - r_start)));
+        }
+    }
+    if (s->rlz) {
+        ChebHost ch;
+        int32_t rc = build_cheb((int)d.kDim, (int)d.b_kDim, s->bcb[0], s->bct[0], s->p.kMin, s->p.kMax, ch);
+        if (rc) return rc;
+        zcol = ch.mish;  // the column's Chebyshev points, zmin → zmax
+    }
+    double *d_coef = nullptr;
+    int32_t rc = block_coefficients<P>(s, &d_coef, st);
+    if (rc) return rc;
+    rc = eval_points(s, d_coef, r, lam, {}, mode, taper, zcol, t->phys, d.n_physical, t->esz == 4, st);
+    cudaFree(d_coef);
+    if (rc) return rc;
+    if ((rc = grid_forward(t, st))) return rc;  // spectralTransform!(target); gridTransform!(target)
+    return grid_inverse(t, st);
+}
+
 }  // namespace
 
 extern "C" int32_t ss_regular_grid_transform(ss_grid *g, const double *r_pts, int32_t n_r, const double *lam_pts,
@@ -330,4 +611,38 @@ extern "C" int32_t ss_regular_grid_transform(ss_grid *g, const double *r_pts, in
     cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
     if (g->esz == 4) return regular<float>(g, r_pts, n_r, lam_pts, n_lam, z_pts, n_z, out, st);
     return regular<double>(g, r_pts, n_r, lam_pts, n_lam, z_pts, n_z, out, st);
+}
+
+extern "C" int32_t ss_evaluate_unstructured(ss_grid *g, const double *pts, int64_t npts, double *out,
+                                            int32_t out_of_bounds, double fill, void *stream) {
+    if (!g || !pts || !out || npts < 0 || out_of_bounds < 0 || out_of_bounds > 2) {
+        set_error("evaluate_unstructured: bad arguments");
+        return SS_BAD_ARG;
+    }
+    if (npts == 0) return SS_OK;
+    CUDA_TRY(cudaSetDevice(g->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+    if (g->esz == 4) return unstructured<float>(g, pts, npts, out, out_of_bounds, fill, st);
+    return unstructured<double>(g, pts, npts, out, out_of_bounds, fill, st);
+}
+
+extern "C" int32_t ss_relocate_grid(ss_grid *target, ss_grid *source, double dx, double dy, int32_t boundary,
+                                    int32_t taper_width, void *stream) {
+    if (!target || !source || boundary < 0 || boundary > 2 || taper_width < 0) {
+        set_error("relocate_grid: bad arguments");
+        return SS_BAD_ARG;
+    }
+    if (target->rlz != source->rlz || target->d.n_physical != source->d.n_physical ||
+        target->d.nvars != source->d.nvars || target->esz != source->esz || target->device != source->device ||
+        target->d.n_spectral != source->d.n_spectral) {
+        set_error("relocate_grid: target must be a grid with the source's parameters");
+        return SS_BAD_SHAPE;
+    }
+    CUDA_TRY(cudaSetDevice(source->device));
+    // queued on the target's stream (where the caller's later work on the target
+    // goes), after the source's queued work has finished
+    cudaStream_t st = stream ? (cudaStream_t)stream : target->stream;
+    CUDA_TRY(cudaStreamSynchronize(source->stream));
+    if (source->esz == 4) return relocate<float>(target, source, dx, dy, boundary, taper_width, st);
+    return relocate<double>(target, source, dx, dy, boundary, taper_width, st);
 }

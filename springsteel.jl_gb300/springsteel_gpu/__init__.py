@@ -919,3 +919,64 @@ def regularGridTransform(grid, *points, stream=None):
 # ----------------------------------------------------------------- I/O (src/io.jl)
 from .io import (check_grid_dims, load_grid, read_netcdf, read_physical_grid, save_grid,  # noqa: E402,F401
                  write_grid, write_netcdf)
+
+
+# ----------------------------------------------------------------- unstructured points, relocation
+def evaluate_unstructured(source, pts, vars=None, out_of_bounds="nan", stream=None):
+    """evaluate_unstructured(source, pts; vars, out_of_bounds) (src/interpolation.jl:1735-1850)
+    from the device-resident spectral array: pts (N, 2) (r, λ) for RL or (N, 3)
+    (r, λ, z) for RLZ; returns (N, nvars) values, NaN for variables not in `vars`.
+    out_of_bounds: "nan", "error" (raises), or a number to fill."""
+    p = np.asfortranarray(np.asarray(pts, np.float64))
+    d = source.dims
+    if p.ndim != 2 or p.shape[1] != (3 if source.params.geometry == "RLZ" else 2):
+        raise ValueError("pts must be (N, 2) for RL and (N, 3) for RLZ grids")
+    mode, fill = (0, 0.0) if out_of_bounds == "nan" else ((1, 0.0) if out_of_bounds == "error"
+                                                          else (2, float(out_of_bounds)))
+    out = np.empty((p.shape[0], d["nvars"]), order="F")
+    st = load_library().ss_evaluate_unstructured(source.handle, p.ctypes.data_as(C.c_void_p), p.shape[0],
+                                                 out.ctypes.data_as(C.c_void_p), mode, fill, stream)
+    if st == abi.SS_BAD_ARG and mode == 1:
+        raise ValueError(load_library().ss_last_error_string().decode())
+    _check(st)
+    if vars is not None:
+        keep = {source.params.vars[v] - 1 for v in vars if v in source.params.vars}
+        for j in range(d["nvars"]):
+            if j not in keep:
+                out[:, j] = np.nan
+    return out
+
+
+_BOUNDARY = {"nan": 0, "nearest": 1, "azimuthal_mean": 2}
+
+
+def grid_center(grid):
+    """grid_center (src/relocation.jl:25-27): cumulative shift of relocate_grid_b calls
+    (kept on the grid object)."""
+    return getattr(grid, "_center", (0.0, 0.0))
+
+
+def _relocate(target, source, new_center, boundary, taper_width, stream):
+    if boundary not in _BOUNDARY:
+        raise ValueError("Unknown boundary strategy: %s. Fast path supports nan, nearest, azimuthal_mean." % boundary)
+    dx, dy = float(new_center[0]), float(new_center[1])
+    _check(load_library().ss_relocate_grid(target.handle, source.handle, dx, dy, _BOUNDARY[boundary],
+                                           int(taper_width), stream))
+
+
+def relocate_grid(grid, new_center, boundary="azimuthal_mean", taper_width=0, stream=None):
+    """relocate_grid(grid, (dx, dy); boundary, taper_width) (src/relocation.jl:56-98): a new
+    grid whose fields are the source's reprojected to the shifted center."""
+    new = createGrid(grid.params)
+    grid.synchronize()
+    _relocate(new, grid, new_center, boundary, taper_width, stream)
+    return new
+
+
+def relocate_grid_b(grid, new_center, boundary="azimuthal_mean", taper_width=0, stream=None):
+    """relocate_grid!(grid, (dx, dy); ...) (src/relocation.jl:99-128): in place, and the
+    grid's cumulative center moves by (dx, dy)."""
+    _relocate(grid, grid, new_center, boundary, taper_width, stream)
+    old = grid_center(grid)
+    grid._center = (old[0] + float(new_center[0]), old[1] + float(new_center[1]))
+    return grid

@@ -160,7 +160,7 @@ EXPORTED = [
     "ss_spectral_transform", "ss_grid_transform", "ss_spectral_transform_from_host",
     "ss_grid_transform_to_host", "ss_grid_set_filter", "ss_grid_set_ahat",
     "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
-    "ss_spectral_transform_noalloc", "ss_regular_grid_transform", "ss_spline_transform", "ss_tile_transform",
+    "ss_spectral_transform_noalloc", "ss_regular_grid_transform", "ss_evaluate_unstructured", "ss_relocate_grid", "ss_spline_transform", "ss_tile_transform",
     "ss_grid_save", "ss_grid_load", "ss_grid_load_arrays", "ss_grid_archive_user",
     "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads", "ss_batch_fused_launches",
     "ss_chain_create", "ss_chain_create_embedded", "ss_chain_destroy", "ss_multi_grid_transform",
@@ -223,6 +223,8 @@ def bind(lib):
         "ss_spectral_transform_noalloc": ([vp, vp, vp, vp], i32),
         "ss_regular_grid_transform": ([vp, vp, i32, vp, i32, vp, i32, vp, vp], i32),
         "ss_spline_transform": ([vp, vp, vp], i32),
+        "ss_evaluate_unstructured": ([vp, vp, C.c_int64, vp, i32, C.c_double, vp], i32),
+        "ss_relocate_grid": ([vp, vp, C.c_double, C.c_double, i32, i32, vp], i32),
         "ss_tile_transform": ([vp, vp], i32),
         "ss_grid_save": ([vp, C.c_char_p, vp, C.c_int64, vp], i32),
         "ss_grid_load": ([C.c_char_p, C.POINTER(vp), vp], i32),
