@@ -48,6 +48,15 @@ for _p in (os.path.join(ROOT, "springsteel.jl_gb300"), os.path.join(ROOT, "oracl
 
 import numpy as np  # noqa: E402
 
+# Per-slot bound of the output check [f, ∂r, ∂rr, ∂λ, ∂λλ, ∂z, ∂zz], relative to the slot's
+# scale: FP64 to round-off; double-float bulk to its 48-bit significand; binary32 storage
+# with the FP64-refined spline solve to the binary32 floor of each derivative.
+CHECK_TOLERANCE = {
+    "f64": 1e-12,
+    "f64_fast": 2e-11,
+    "f32": [2e-6, 5e-5, 5e-5, 5e-5, 5e-5, 5e-6, 5e-6],
+}
+
 WORKLOADS = {
     "rlz200-f64": dict(num_cells=200, kDim=32, nvars=5, precision="f64"),
     "rlz200-f64fast": dict(num_cells=200, kDim=32, nvars=5, precision="f64_fast"),
@@ -720,13 +729,14 @@ def measure(wl, args, lib, ws, rank, local, cpu_baseline=True):
                        "(oracle), %.2f s; value = 1/%d round trip over that time" % (nv, dt, nv)) if one_var else
                       ("every variable of the same grid and inputs, one round trip (forward+inverse), FP64 C port "
                        "(oracle), %.2f s" % dt)}
-        tol = 1e-12 if gp.precision == "f64" else None
+        tol = np.broadcast_to(np.asarray(CHECK_TOLERANCE[gp.precision], np.float64), (dims["nslots"],))
+        worst = errs.max(axis=0)
         res["check"] = {
             "against": "FP64 oracle on the same inputs, one round trip",
             "variables": [0] if one_var else list(range(nv)),
-            "max_rel_err_per_slot": [float(x) for x in errs.max(axis=0)],
-            "max_rel_err": float(errs.max()), "tolerance": tol,
-            "pass": bool(tol is None or errs.max() <= tol)}
+            "max_rel_err_per_slot": [float(x) for x in worst],
+            "max_rel_err": float(errs.max()), "tolerance_per_slot": [float(x) for x in tol],
+            "pass": bool(np.all(worst <= tol))}
     grid.close()
     return res
 
