@@ -184,9 +184,28 @@ __device__ __forceinline__ const void *tab_at(const void *pool, int64_t off) {
 // the R × R DFT matrix product.
 template <typename T> constexpr int kPrimeOut = sizeof(T) == 4 ? 2 : 4;  // output pairs per unit
 template <typename T> constexpr int kPrimeSeqs = 1;                      // sequences per unit
+
+// kPrimeTile consecutive entries of one row of a prime pass's DFT matrix
+// (prime_matrix_width); binary32 rows load two entries per 16-byte access.
+template <typename T>
+__device__ __forceinline__ void ld_prime_row(const typename Tab<T>::cplx_t *__restrict__ row, cpx<T> *w) {
+    if constexpr (std::is_same<T, float>::value) {
+        const float4 *r4 = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+        for (int u = 0; u < kPrimeTile / 2; u++) {
+            const float4 v = __ldg(r4 + u);
+            w[2 * u] = {v.x, v.y};
+            w[2 * u + 1] = {v.z, v.w};
+        }
+    } else {
+#pragma unroll
+        for (int u = 0; u < kPrimeTile; u++) w[u] = ld_cplx<T>(row, u);
+    }
+}
+
 template <int SIGN, typename T>
 __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N, int Ns, int R,
-                           const void *__restrict__ tw, int ns, int ss) {
+                           const void *__restrict__ tw, const void *__restrict__ mat, int ns, int ss) {
     const int NR = N / R, H = (R - 1) / 2;
     const int tstride = N / (Ns * R), rstep = N / R;
     const float inv_ns = 1.0f / (float)Ns;
@@ -223,6 +242,62 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
             }
         }
         __syncthreads();
+    }
+    if (mat) {
+        // Matrix form: unit (butterfly j, output tile s0..s0+kPrimeTile−1) of one
+        // sequence walks q with running pointers; row q of the matrix gives the
+        // tile's (cos, −sin)(2πqs/R) in kPrimeTile/2 (binary32) or kPrimeTile loads.
+        constexpr int S = kPrimeTile;
+        const int SW = prime_matrix_width(R), Gs = SW / S;
+        const float inv_gs = 1.0f / (float)Gs;
+        using CT = typename Tab<T>::cplx_t;
+        for (UnitWalk uw_(NR * Gs); uw_.g < ns; uw_.next()) {
+            const int u = uw_.n, sq = uw_.g;
+            const int j = div_small(u, Gs, inv_gs), s0 = (u - j * Gs) * S;
+            const int jq = div_small(j, Ns, inv_ns), k = j - jq * Ns;
+            const cpx<T> *sv = src + (size_t)sq * ss + j;
+            const cpx<T> x0 = sv[0];
+            cpx<T> re[S], im[S];
+#pragma unroll
+            for (int i = 0; i < S; i++) { re[i] = x0; im[i] = c_zero<T>(); }
+            const cpx<T> *pa = sv + NR, *pb = sv + (R - 1) * NR;
+            const CT *row = reinterpret_cast<const CT *>(mat) + s0;
+#pragma unroll 2
+            for (int q = 1; q <= H; q++) {
+                const cpx<T> a = *pa, b = *pb;
+                pa += NR;
+                pb -= NR;
+                cpx<T> w[S];
+                ld_prime_row<T>(row, w);
+                row += SW;
+#pragma unroll
+                for (int i = 0; i < S; i++) {
+                    re[i].x = re[i].x + a.x * w[i].x;
+                    re[i].y = re[i].y + a.y * w[i].x;
+                    im[i].x = im[i].x - b.x * w[i].y;
+                    im[i].y = im[i].y - b.y * w[i].y;
+                }
+            }
+            cpx<T> *d = dst + (size_t)sq * ss + jq * Ns * R + k;
+#pragma unroll
+            for (int i = 0; i < S; i++) {
+                const int s = s0 + i;
+                if (s > H) break;
+                if (s == 0) {
+                    d[0] = re[i];
+                    continue;
+                }
+                const cpx<T> iim = {-im[i].y, im[i].x};
+                if (SIGN < 0) {
+                    d[s * Ns] = c_sub(re[i], iim);
+                    d[(R - s) * Ns] = c_add(re[i], iim);
+                } else {
+                    d[s * Ns] = c_add(re[i], iim);
+                    d[(R - s) * Ns] = c_sub(re[i], iim);
+                }
+            }
+        }
+        return;
     }
     // s = 0 gives X_0 = v_0 + Σ a_q through the unit twiddle; entries with s > H
     // are computed and dropped
@@ -296,9 +371,10 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
 
 // Stockham passes rad[s_begin..nrad) over ping-pong buffers, Ns0 = product of the
 // radices already applied; returns the buffer holding the result.
+// pm: pool offsets of the prime passes' DFT matrices, parallel to rad (null: none).
 template <int SIGN, typename T>
 __device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int ns,
-                                  int ss, int s_begin = 0, int Ns0 = 1) {
+                                  int ss, const void *pool, const int64_t *pm, int s_begin = 0, int Ns0 = 1) {
     int Ns = Ns0;
     for (int s = s_begin; s < nrad; s++) {
         const int R = rad[s];
@@ -310,7 +386,11 @@ __device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, i
         case 7: stockham_pass<7, SIGN>(a, b, N, Ns, tw, ns, ss); break;
         case 11: stockham_pass<11, SIGN>(a, b, N, Ns, tw, ns, ss); break;
         case 13: stockham_pass<13, SIGN>(a, b, N, Ns, tw, ns, ss); break;
-        default: prime_pass<SIGN, T>(a, b, N, Ns, R, tw, ns, ss); break;
+        default: {
+            const int64_t mo = pm ? pm[s] : -1;
+            prime_pass<SIGN, T>(a, b, N, Ns, R, tw, mo >= 0 ? tab_at<T>(pool, mo) : nullptr, ns, ss);
+            break;
+        }
         }
         __syncthreads();
         cpx<T> *t = a;
@@ -348,7 +428,7 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
     }
     __syncthreads();
     const int ni = nb * NR;  // inner sequences
-    cpx<T> *r1 = stockham_plain<-1, T>(dst, src, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1);
+    cpx<T> *r1 = stockham_plain<-1, T>(dst, src, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm);
     for (UnitWalk uw_(P1); uw_.g < (ni); uw_.next()) {
         const int k = uw_.n, sq = uw_.g;
         cpx<T> *u = r1 + (size_t)sq * P1 + k;
@@ -358,7 +438,7 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
     }
     __syncthreads();
     cpx<T> *other = (r1 == dst) ? src : dst;
-    cpx<T> *r2 = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1);
+    cpx<T> *r2 = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm);
     cpx<T> *out = (r2 == dst) ? src : dst;
     for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
         const int e = uw_.n, b = uw_.g;  // scatter: (j, b'), b' = p−1 → X_0
@@ -387,9 +467,9 @@ __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nra
     if (pl && pl->rp) {
         cpx<T> *o = rader_pass<SIGN, T>(a, b, N, *pl, pool, ns, ss, tail);
         if (o != a) { b = a; a = o; }
-        return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, 1, pl->rp);
+        return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, pool, pl->pm, 1, pl->rp);
     }
-    return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss);
+    return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, pool, pl ? pl->pm : nullptr);
 }
 
 // Sequence stride of a plan inside a CTA's ping-pong buffers: N, or M for
@@ -422,7 +502,7 @@ __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool,
         ab[k] = v;
     }
     __syncthreads();
-    cpx<T> *r = stockham_plain<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M);
+    cpx<T> *r = stockham_plain<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M, pool, nullptr);
     for (UnitWalk uw_(M); uw_.g < (nb); uw_.next()) {
         const int k = uw_.n, bi = uw_.g;
         cpx<T> *rb = r + (size_t)bi * M;
@@ -430,7 +510,7 @@ __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool,
     }
     __syncthreads();
     cpx<T> *other = (r == a) ? b : a;
-    cpx<T> *q = stockham_plain<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M);
+    cpx<T> *q = stockham_plain<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M, pool, nullptr);
     for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
         const int k = uw_.n, bi = uw_.g;
         cpx<T> *qb = q + (size_t)bi * M;

@@ -58,7 +58,20 @@ struct FftPlan {
     int64_t rtw;     // pool offset of W_{p−1}^t, t < p−1
     int64_t rH;      // pool offset of H, p−1 entries
     int64_t rperm;   // pool offset of (g^a mod p, g^{−a} mod p), a < p−1, as exact reals
+    // pool offsets of the DFT matrices of the direct prime passes (radix > 13) in
+    // rad[] and rrad[]; −1 for every other radix (prime_matrix_width)
+    int64_t pm[kMaxRadices];
+    int64_t rpm[kMaxRadices];
 };
+
+// Output pairs (s, R−s) one work unit of a direct prime pass computes: one row
+// load of the pass's DFT matrix feeds kPrimeTile outputs.
+constexpr int kPrimeTile = 4;
+// Columns of a radix-R prime matrix: s = 0..(R−1)/2, rounded up to whole tiles.
+// Entry (q, s), q = 1..(R−1)/2, at (q − 1)·width + s holds
+// (cos 2πqs/R, −sin 2πqs/R); the columns beyond (R−1)/2 hold the same formula
+// and their outputs are dropped.
+SS_HD inline int prime_matrix_width(int R) { return ((R - 1) / 2 + kPrimeTile) / kPrimeTile * kPrimeTile; }
 
 // One Fourier ring (src/factory.jl:608-624): L = 4+4ri points, kmax, bDim = 2ri+1.
 struct RingDesc {
@@ -159,11 +172,13 @@ struct PlanSet {
     std::vector<int> plan_of_N;     // index by N (−1 if absent)
     std::vector<int64_t> utw_of_L;  // by L
     std::vector<int64_t> mtw_of_M;  // by M
+    std::vector<int64_t> pm_of_R;   // by prime radix R
     int max_smem_cplx = 0;          // largest complex buffer (N or M)
     int max_prime = kMaxPrimeRadix; // direct prime passes up to here, Rader or Bluestein above
     bool rader = true;              // Rader passes for larger primes (else Bluestein)
     int plan_for(int N, TwiddlePool &pool);
     int64_t unpack_for(int L, TwiddlePool &pool);
+    int64_t prime_matrix(int R, TwiddlePool &pool);
 };
 // complex entries of one ping-pong buffer of a plan
 // complex entries of one ping-pong buffer: M (Bluestein), N + N/p (Rader: a tail

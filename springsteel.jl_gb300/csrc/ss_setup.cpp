@@ -642,10 +642,34 @@ int PlanSet::plan_for(int N, TwiddlePool &pool) {
         for (int k = 0; k < M; k++) { fi[2 * k] = f[k].real() / M; fi[2 * k + 1] = f[k].imag() / M; }
         p.filt = pool.push(fi);
     }
+    for (int i = 0; i < kMaxRadices; i++) {
+        const bool direct = i < p.nrad && p.rad[i] > 13 && !(p.rp && i == 0);
+        p.pm[i] = direct ? prime_matrix(p.rad[i], pool) : -1;
+        p.rpm[i] = (p.rp && i < p.rnrad && p.rrad[i] > 13) ? prime_matrix(p.rrad[i], pool) : -1;
+    }
     plans.push_back(p);
     plan_of_N[N] = (int)plans.size() - 1;
     max_smem_cplx = std::max(max_smem_cplx, fft_buffer_len(p));
     return plan_of_N[N];
+}
+
+// DFT matrix of a direct radix-R prime pass (layout at prime_matrix_width),
+// shared by every plan of the set.  Its offset is even, so that a binary32 row
+// segment of two entries is one aligned 16-byte load.
+int64_t PlanSet::prime_matrix(int R, TwiddlePool &pool) {
+    if ((int)pm_of_R.size() <= R) pm_of_R.resize(R + 1, -1);
+    if (pm_of_R[R] >= 0) return pm_of_R[R];
+    if (pool.size() % 2) pool.v.insert(pool.v.end(), {0.0, 0.0});
+    const int H = (R - 1) / 2, W = prime_matrix_width(R);
+    std::vector<double> m(size_t(2) * H * W);
+    for (int q = 1; q <= H; q++)
+        for (int s = 0; s < W; s++) {
+            const std::complex<double> w = unit_root((long)q * s, R, -1);
+            m[2 * ((size_t)(q - 1) * W + s)] = w.real();
+            m[2 * ((size_t)(q - 1) * W + s) + 1] = w.imag();
+        }
+    pm_of_R[R] = pool.push(m);
+    return pm_of_R[R];
 }
 
 int64_t PlanSet::unpack_for(int L, TwiddlePool &pool) {
