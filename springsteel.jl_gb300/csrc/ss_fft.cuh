@@ -115,54 +115,78 @@ struct UnitWalk {
     }
 };
 
-// Sequences a work unit of a radix-R pass carries.  One: the ring kernels are
-// bound by latency and barrier waits, not by instruction issue, so a pass
-// needs as many independent units per barrier as possible (measured on GB300:
-// four sequences per unit at half the occupancy ran ring_inverse 15% slower).
-template <int R, typename T>
-constexpr int kUnitSeqs = 1;
+// n consecutive complex entries of a twiddle table row (n even for binary32:
+// the row starts 16-byte aligned and loads two entries per access).
+template <typename T, int n>
+__device__ __forceinline__ void ld_cplx_row(const typename Tab<T>::cplx_t *__restrict__ row, cpx<T> *w) {
+    if constexpr (std::is_same<T, float>::value) {
+        static_assert(n % 2 == 0, "binary32 rows are whole 16-byte loads");
+        const float4 *r4 = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+        for (int u = 0; u < n / 2; u++) {
+            const float4 v = __ldg(r4 + u);
+            w[2 * u] = {v.x, v.y};
+            w[2 * u + 1] = {v.z, v.w};
+        }
+    } else {
+#pragma unroll
+        for (int u = 0; u < n; u++) w[u] = ld_cplx<T>(row, u);
+    }
+}
 
-// One Stockham pass over ns sequences: Ns = product of the radices already applied.
+// One Stockham pass over ns sequences: Ns = product of the radices already
+// applied.  Work unit (k, jq, g): butterfly j = jq·Ns + k of sequence g, in
+// the order j fastest, then g (unit threadIdx.x + i·blockDim.x); the thread's
+// coordinates advance by the CTA stride, pre-split into (k, jq, g) steps, with
+// two carries.  Inputs at j + r·N/R, outputs at jq·Ns·R + k + r·Ns.  ptab: the
+// pass's twiddle rows (pass_row_width), null when Ns = 1.
 template <int R, int SIGN, typename T>
 __device__ __forceinline__ void stockham_pass(const cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, int N,
-                                              int Ns, const void *__restrict__ tw, int ns, int ss) {
-    constexpr int IT = kUnitSeqs<R, T>;
-    const int NR = N / R;
-    const int tstride = N / (Ns * R);
-    const float inv_ns = 1.0f / (float)Ns;
-    const int G = (ns + IT - 1) / IT;
-    for (UnitWalk uw_(NR); uw_.g < (G); uw_.next()) {
-        const int j = uw_.n, g = uw_.g;
-        const int jq = div_small(j, Ns, inv_ns);
-        const int k = j - jq * Ns;
-        cpx<T> w[R];  // every entry set: a partly uninitialised array is placed in local memory
+                                              int Ns, const void *__restrict__ ptab, int ns, int ss) {
+    constexpr int RW = pass_row_width(R);
+    using CT = typename Tab<T>::cplx_t;
+    const int NR = N / R, NJ = NR / Ns;
+    const float inv_nr = __frcp_rn((float)NR), inv_ns = __frcp_rn((float)Ns);
+    const int TB = blockDim.x;
+    int g = div_small(threadIdx.x, NR, inv_nr);
+    const int j0 = threadIdx.x - g * NR;
+    int jq = div_small(j0, Ns, inv_ns);
+    int k = j0 - jq * Ns;
+    const int dg = div_small(TB, NR, inv_nr);
+    const int dj = TB - dg * NR;
+    const int dq = div_small(dj, Ns, inv_ns);
+    const int dk = dj - dq * Ns;
+    const CT *tab = reinterpret_cast<const CT *>(ptab);
+    while (g < ns) {
+        const int j = jq * Ns + k;
+        const cpx<T> *sp = src + (g * ss + j);
+        cpx<T> *dp = dst + (g * ss + j + jq * Ns * (R - 1));
+        cpx<T> v[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) w[r] = {T(1.0f), T(0.0f)};
-        if (k > 0) {
-            const int step = tstride * k;
+        for (int r = 0; r < R; r++) v[r] = sp[r * NR];
+        if (tab) {
+            cpx<T> w[RW];
+            ld_cplx_row<T, RW>(tab + k * RW, w);
 #pragma unroll
             for (int r = 1; r < R; r++) {
-                w[r] = ld_cplx<T>(tw, (int64_t)r * step);
-                if (SIGN > 0) w[r].y = -w[r].y;
+                const cpx<T> a = v[r], b = w[r - 1];
+                if (SIGN < 0) v[r] = {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+                else v[r] = {a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};  // a · conj(b)
             }
         }
-        const int idxD = jq * Ns * R + k;
+        dft_small<R, SIGN>(v);
 #pragma unroll
-        for (int t = 0; t < IT; t++) {
-            const int sq = g * IT + t;
-            if (sq >= ns) break;
-            const cpx<T> *s = src + (size_t)sq * ss + j;
-            cpx<T> *d = dst + (size_t)sq * ss + idxD;
-            cpx<T> v[R];
-#pragma unroll
-            for (int r = 0; r < R; r++) v[r] = s[r * NR];
-            if (k > 0) {
-#pragma unroll
-                for (int r = 1; r < R; r++) v[r] = c_mul(v[r], w[r]);
-            }
-            dft_small<R, SIGN>(v);
-#pragma unroll
-            for (int r = 0; r < R; r++) d[r * Ns] = v[r];
+        for (int r = 0; r < R; r++) dp[r * Ns] = v[r];
+        k += dk;
+        jq += dq;
+        g += dg;
+        if (k >= Ns) {
+            k -= Ns;
+            jq++;
+        }
+        if (jq >= NJ) {
+            jq -= NJ;
+            g++;
         }
     }
 }
@@ -372,20 +396,23 @@ __device__ void prime_pass(cpx<T> *__restrict__ src, cpx<T> *__restrict__ dst, i
 // Stockham passes rad[s_begin..nrad) over ping-pong buffers, Ns0 = product of the
 // radices already applied; returns the buffer holding the result.
 // pm: pool offsets of the prime passes' DFT matrices, parallel to rad (null: none).
+// pt: pool offsets of the radix passes' twiddle rows, parallel to rad.
 template <int SIGN, typename T>
 __device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nrad, const void *tw, int ns,
-                                  int ss, const void *pool, const int64_t *pm, int s_begin = 0, int Ns0 = 1) {
+                                  int ss, const void *pool, const int64_t *pm, const int64_t *pt, int s_begin = 0,
+                                  int Ns0 = 1) {
     int Ns = Ns0;
     for (int s = s_begin; s < nrad; s++) {
         const int R = rad[s];
+        const void *pst = (Ns > 1 && pt[s] >= 0) ? tab_at<T>(pool, pt[s]) : nullptr;
         switch (R) {
-        case 4: stockham_pass<4, SIGN>(a, b, N, Ns, tw, ns, ss); break;
-        case 2: stockham_pass<2, SIGN>(a, b, N, Ns, tw, ns, ss); break;
-        case 3: stockham_pass<3, SIGN>(a, b, N, Ns, tw, ns, ss); break;
-        case 5: stockham_pass<5, SIGN>(a, b, N, Ns, tw, ns, ss); break;
-        case 7: stockham_pass<7, SIGN>(a, b, N, Ns, tw, ns, ss); break;
-        case 11: stockham_pass<11, SIGN>(a, b, N, Ns, tw, ns, ss); break;
-        case 13: stockham_pass<13, SIGN>(a, b, N, Ns, tw, ns, ss); break;
+        case 4: stockham_pass<4, SIGN>(a, b, N, Ns, pst, ns, ss); break;
+        case 2: stockham_pass<2, SIGN>(a, b, N, Ns, pst, ns, ss); break;
+        case 3: stockham_pass<3, SIGN>(a, b, N, Ns, pst, ns, ss); break;
+        case 5: stockham_pass<5, SIGN>(a, b, N, Ns, pst, ns, ss); break;
+        case 7: stockham_pass<7, SIGN>(a, b, N, Ns, pst, ns, ss); break;
+        case 11: stockham_pass<11, SIGN>(a, b, N, Ns, pst, ns, ss); break;
+        case 13: stockham_pass<13, SIGN>(a, b, N, Ns, pst, ns, ss); break;
         default: {
             const int64_t mo = pm ? pm[s] : -1;
             prime_pass<SIGN, T>(a, b, N, Ns, R, tw, mo >= 0 ? tab_at<T>(pool, mo) : nullptr, ns, ss);
@@ -428,7 +455,7 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
     }
     __syncthreads();
     const int ni = nb * NR;  // inner sequences
-    cpx<T> *r1 = stockham_plain<-1, T>(dst, src, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm);
+    cpx<T> *r1 = stockham_plain<-1, T>(dst, src, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm, pl.rpt);
     for (UnitWalk uw_(P1); uw_.g < (ni); uw_.next()) {
         const int k = uw_.n, sq = uw_.g;
         cpx<T> *u = r1 + (size_t)sq * P1 + k;
@@ -438,7 +465,7 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
     }
     __syncthreads();
     cpx<T> *other = (r1 == dst) ? src : dst;
-    cpx<T> *r2 = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm);
+    cpx<T> *r2 = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm, pl.rpt);
     cpx<T> *out = (r2 == dst) ? src : dst;
     for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
         const int e = uw_.n, b = uw_.g;  // scatter: (j, b'), b' = p−1 → X_0
@@ -467,9 +494,9 @@ __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nra
     if (pl && pl->rp) {
         cpx<T> *o = rader_pass<SIGN, T>(a, b, N, *pl, pool, ns, ss, tail);
         if (o != a) { b = a; a = o; }
-        return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, pool, pl->pm, 1, pl->rp);
+        return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, pool, pl->pm, pl->pt, 1, pl->rp);
     }
-    return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, pool, pl ? pl->pm : nullptr);
+    return stockham_plain<SIGN, T>(a, b, N, rad, nrad, tw, ns, ss, pool, pl->pm, pl->pt);
 }
 
 // Sequence stride of a plan inside a CTA's ping-pong buffers: N, or M for
@@ -502,7 +529,7 @@ __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool,
         ab[k] = v;
     }
     __syncthreads();
-    cpx<T> *r = stockham_plain<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M, pool, nullptr);
+    cpx<T> *r = stockham_plain<-1, T>(a, b, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M, pool, nullptr, p.mpt);
     for (UnitWalk uw_(M); uw_.g < (nb); uw_.next()) {
         const int k = uw_.n, bi = uw_.g;
         cpx<T> *rb = r + (size_t)bi * M;
@@ -510,7 +537,7 @@ __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool,
     }
     __syncthreads();
     cpx<T> *other = (r == a) ? b : a;
-    cpx<T> *q = stockham_plain<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M, pool, nullptr);
+    cpx<T> *q = stockham_plain<1, T>(r, other, M, p.mrad, p.mnrad, tab_at<T>(pool, p.mtw), nb, M, pool, nullptr, p.mpt);
     for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
         const int k = uw_.n, bi = uw_.g;
         cpx<T> *qb = q + (size_t)bi * M;

@@ -8,6 +8,8 @@
 
 #include <cstdint>
 #include <string>
+#include <array>
+#include <map>
 #include <vector>
 
 #include <vector_types.h>
@@ -62,7 +64,18 @@ struct FftPlan {
     // rad[] and rrad[]; −1 for every other radix (prime_matrix_width)
     int64_t pm[kMaxRadices];
     int64_t rpm[kMaxRadices];
+    // pool offsets of the per-pass twiddle rows of the radix passes (R ≤ 13,
+    // Ns > 1) of rad[], rrad[] and mrad[]; −1 for every other pass
+    // (pass_row_width)
+    int64_t pt[kMaxRadices];
+    int64_t rpt[kMaxRadices];
+    int64_t mpt[kMaxRadices];
 };
+
+// Entries per twiddle row of a radix-R pass: R − 1 rounded up to even, so that
+// binary32 rows are whole 16-byte loads.  Row k (k < Ns) of the pass holds
+// W_N^{r·k·N/(Ns·R)} for r = 1..R−1 at entry r − 1, then (1, 0) padding.
+SS_HD constexpr int pass_row_width(int R) { return (R - 1 + 1) / 2 * 2; }
 
 // Output pairs (s, R−s) one work unit of a direct prime pass computes: one row
 // load of the pass's DFT matrix feeds kPrimeTile outputs.
@@ -179,6 +192,9 @@ struct PlanSet {
     int plan_for(int N, TwiddlePool &pool);
     int64_t unpack_for(int L, TwiddlePool &pool);
     int64_t prime_matrix(int R, TwiddlePool &pool);
+    std::map<std::array<int, 3>, int64_t> pt_of;  // by (N, Ns, R)
+    int64_t pass_table(int N, int Ns, int R, TwiddlePool &pool);
+    void pass_tables(int n, const int *rad, int nrad, int s0, int Ns0, int64_t *pt, TwiddlePool &pool);
 };
 // complex entries of one ping-pong buffer of a plan
 // complex entries of one ping-pong buffer: M (Bluestein), N + N/p (Rader: a tail

@@ -642,6 +642,19 @@ int PlanSet::plan_for(int N, TwiddlePool &pool) {
         for (int k = 0; k < M; k++) { fi[2 * k] = f[k].real() / M; fi[2 * k + 1] = f[k].imag() / M; }
         p.filt = pool.push(fi);
     }
+    if (p.blu) {
+        pass_tables(p.M, p.mrad, p.mnrad, 0, 1, p.mpt, pool);
+        pass_tables(0, nullptr, 0, 0, 1, p.pt, pool);
+        pass_tables(0, nullptr, 0, 0, 1, p.rpt, pool);
+    } else if (p.rp) {
+        pass_tables(N, p.rad, p.nrad, 1, p.rp, p.pt, pool);
+        pass_tables(p.rp - 1, p.rrad, p.rnrad, 0, 1, p.rpt, pool);
+        pass_tables(0, nullptr, 0, 0, 1, p.mpt, pool);
+    } else {
+        pass_tables(N, p.rad, p.nrad, 0, 1, p.pt, pool);
+        pass_tables(0, nullptr, 0, 0, 1, p.rpt, pool);
+        pass_tables(0, nullptr, 0, 0, 1, p.mpt, pool);
+    }
     for (int i = 0; i < kMaxRadices; i++) {
         const bool direct = i < p.nrad && p.rad[i] > 13 && !(p.rp && i == 0);
         p.pm[i] = direct ? prime_matrix(p.rad[i], pool) : -1;
@@ -670,6 +683,40 @@ int64_t PlanSet::prime_matrix(int R, TwiddlePool &pool) {
         }
     pm_of_R[R] = pool.push(m);
     return pm_of_R[R];
+}
+
+// Twiddle rows of one radix-R pass of an n-point DFT after Ns points are
+// combined (layout at pass_row_width); shared by the plans that have it.
+int64_t PlanSet::pass_table(int n, int Ns, int R, TwiddlePool &pool) {
+    const std::array<int, 3> key{n, Ns, R};
+    auto it = pt_of.find(key);
+    if (it != pt_of.end()) return it->second;
+    if (pool.size() % 2) pool.v.insert(pool.v.end(), {0.0, 0.0});
+    const int W = pass_row_width(R);
+    const long tstride = n / ((long)Ns * R);
+    std::vector<double> t(size_t(2) * Ns * W);
+    for (int k = 0; k < Ns; k++)
+        for (int r = 1; r <= W; r++) {
+            const std::complex<double> w = r < R ? unit_root((long)r * k * tstride, n, -1) : std::complex<double>(1.0, 0.0);
+            t[2 * ((size_t)k * W + r - 1)] = w.real();
+            t[2 * ((size_t)k * W + r - 1) + 1] = w.imag();
+        }
+    const int64_t off = pool.push(t);
+    pt_of[key] = off;
+    return off;
+}
+
+// Per-pass twiddle rows of the radix passes s0..nrad−1 of an n-point plan
+// whose first Ns0 points are already combined; −1 for prime passes and for
+// passes with Ns = 1 (no input twiddles).
+void PlanSet::pass_tables(int n, const int *rad, int nrad, int s0, int Ns0, int64_t *pt, TwiddlePool &pool) {
+    for (int i = 0; i < kMaxRadices; i++) pt[i] = -1;
+    int Ns = Ns0;
+    for (int s = s0; s < nrad; s++) {
+        const int R = rad[s];
+        if (R <= 13 && Ns > 1) pt[s] = pass_table(n, Ns, R, pool);
+        Ns *= R;
+    }
 }
 
 int64_t PlanSet::unpack_for(int L, TwiddlePool &pool) {
