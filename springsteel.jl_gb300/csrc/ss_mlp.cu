@@ -265,14 +265,19 @@ __device__ __forceinline__ uint32_t cm_offset(int row, int col) {
     return (uint32_t)((((row >> 3) * 32 + (col >> 3)) * 128) + (row & 7) * 16 + (col & 7) * 2);
 }
 
-__device__ __forceinline__ void stage_full(uint8_t *dst, const __nv_bfloat16 *src, int64_t row0, int rows) {
+// rows × 256 bf16 into the core-matrix layout by 16-byte cp.async pieces, every
+// piece of the thread in flight at once (completed by cp_async_wait_all)
+__device__ __forceinline__ void stage_full_async(uint8_t *dst, const __nv_bfloat16 *src, int64_t row0, int rows) {
     const int pieces = rows * 32;
     for (int p = threadIdx.x; p < pieces; p += kInferThreads) {
         const int row = p >> 5, kg = p & 31;
-        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src + (row0 + row) * kMlpWidth + kg * 8));
-        *reinterpret_cast<uint4 *>(dst + cm_offset(row, kg * 8)) = v;
+        const __nv_bfloat16 *g = src + (row0 + row) * kMlpWidth + kg * 8;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst + cm_offset(row, kg * 8))), "l"(g)
+                     : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 __global__ void __launch_bounds__(kInferThreads) mlp_infer_kernel(const __nv_bfloat16 *in, const __nv_bfloat16 *Wb,
                                                                   const float *bias, float *out, int *err) {
@@ -297,15 +302,19 @@ __global__ void __launch_bounds__(kInferThreads) mlp_infer_kernel(const __nv_bfl
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
-    stage_full(sX, in, m0, kMlpTileM);
+    stage_full_async(sX, in, m0, kMlpTileM);
+    stage_full_async(sW, Wb, 0, kMlpWidth);
     bool ok = true;
     uint32_t phase = 0u;
     const int row = (warp & 3) * 32 + lane, cbase = (warp >> 2) * (kMlpWidth / 2);
     for (int l = 0; l < kMlpLayers; l++) {
-        stage_full(sW, Wb + (size_t)l * kMlpWidth * kMlpWidth, 0, kMlpWidth);
+        // this layer's weights (and, first, the input rows) have landed; the
+        // generic-proxy writes (cp.async, the previous epilogue's activations)
+        // are made visible to the tensor core's async proxy
+        cp_async_wait_all();
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a0 = smem_u32(sX), b0 = smem_u32(sW);
 #pragma unroll
@@ -328,6 +337,8 @@ __global__ void __launch_bounds__(kInferThreads) mlp_infer_kernel(const __nv_bfl
         ok = ok && done;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // the MMAs have read sW: the next layer's weights stream in under the epilogue
+        if (ok && l + 1 < kMlpLayers) stage_full_async(sW, Wb + (size_t)(l + 1) * kMlpWidth * kMlpWidth, 0, kMlpWidth);
         const float *bl = bias + l * kMlpWidth;
         for (int cc = 0; cc < kMlpWidth / 64; cc++) {
             const int c0 = cbase + cc * 32;
