@@ -195,11 +195,12 @@ static int32_t build_grid(ss_grid *g) {
     // ---- rings (src/factory.jl:608-624) and FFT plans
     TwiddlePool pool;
     PlanSet plans;
-    // direct prime passes up to 67 and one Rader pass above, in every precision
-    // (measured: 200-cell FP64 RLZ ring_inverse 43.4 ms at 67, 44.4 at 41; 400-cell
-    // FP32 ring_inverse 84.1 ms with Rader above 67, 86.2 above 127, 91.9 with
-    // Bluestein above 127)
-    plans.max_prime = 67;
+    // direct prime passes up to 67 (FP64, double-float) or 127 (binary32) and one
+    // Rader pass above.  Measured with the DFT-matrix prime passes: 200-cell FP64
+    // RLZ ring_inverse 40.6 ms at 31, 40.0 at 67, 40.9 at 127, 43.8 at 199;
+    // 400-cell binary32 ring_inverse + ring_forward 88.1 ms at 31, 83.9 at 67,
+    // 82.4 at 127, 83.6 at 199.
+    plans.max_prime = (g->tl == TL_F32) ? 127 : 67;
     plans.rader = true;
     // tuning override of the direct-pass limit (odd, 13 ≤ limit ≤ 199)
     if (const char *e = std::getenv("SS_FFT_MAX_PRIME")) {
