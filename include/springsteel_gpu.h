@@ -374,7 +374,8 @@ int32_t ss_grid_zero_spectral(ss_grid *grid, void *stream);
  * caller's device arrays; the ring-coefficient scratch is a fixed 8 MiB static
  * device array (1,048,576 FP64 values, reserved on every GPU that loads the
  * library until exit), so grids needing more (nvars × Σ(1+2ri) > 1,048,576)
- * get SS_BAD_SHAPE.  The first call on a device resolves the array's device
+ * get SS_BAD_SHAPE.  d_physical_slot1 must be 16-byte aligned (cudaMalloc
+ * pointers are), else SS_BAD_ARG.  The first call on a device resolves the array's device
  * address; make that call before any stream capture.  Calls share the array:
  * calls that overlap on the GPU race.  Asynchronous on `stream`. */
 int32_t ss_spectral_transform_noalloc(const ss_grid *grid, const double *d_physical_slot1,

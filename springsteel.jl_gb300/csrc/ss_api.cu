@@ -1067,6 +1067,8 @@ static double *g_static_scratch_ptr[kMaxDevices] = {nullptr};
 extern "C" int32_t ss_spectral_transform_noalloc(const ss_grid *g, const double *d_physical_slot1,
                                                  double *d_spectral, void *stream) {
     if (!g || !d_physical_slot1 || !d_spectral) { set_error("null argument"); return SS_BAD_ARG; }
+    // the ring kernel reads each ring's points in aligned (2n, 2n+1) pairs
+    if ((uintptr_t)d_physical_slot1 % 16) { set_error("d_physical_slot1 must be 16-byte aligned"); return SS_BAD_ARG; }
     if (g->rlz || g->esz != 8) {
         set_error("ss_spectral_transform_noalloc supports RL grids with SS_PREC_F64 only");
         return SS_BAD_ARG;

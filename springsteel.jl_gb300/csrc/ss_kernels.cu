@@ -100,12 +100,12 @@ __device__ __forceinline__ void ring_forward_body(const RingLaunch &L, const int
     __syncthreads();
     for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
         const int n = uw_.n, b = uw_.g;
+        // ring offsets and lengths are even: (point 2n, point 2n+1) is one aligned pair
         if (L.rlz) {
-            const T *in = (const T *)L.in + ioff[b];
-            A[(size_t)b * sq + n] = {in[2 * n], in[2 * n + 1]};
+            A[(size_t)b * sq + n] = reinterpret_cast<const cpx<T> *>((const T *)L.in + ioff[b])[n];
         } else {
-            const P *in = (const P *)L.in + ioff[b];
-            A[(size_t)b * sq + n] = {to_compute<T>(in[2 * n]), to_compute<T>(in[2 * n + 1])};
+            const cpx<P> v = reinterpret_cast<const cpx<P> *>((const P *)L.in + ioff[b])[n];
+            A[(size_t)b * sq + n] = {to_compute<T>(v.x), to_compute<T>(v.y)};
         }
     }
     __syncthreads();
@@ -248,14 +248,11 @@ __device__ __forceinline__ void ring_inverse_body(const RingLaunch &L, const int
             for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
         const int n = uw_.n, b = uw_.g;
                 const cpx<T> w = zb0[(size_t)b * sq + n];
+                // even plane and ring offsets: points (2n, 2n+1) are one aligned pair
                 if (L.rlz) {
-                    T *dst = (T *)L.out + plane + ooff[b];
-                    dst[2 * n] = w.x;
-                    dst[2 * n + 1] = w.y;
+                    reinterpret_cast<cpx<T> *>((T *)L.out + plane + ooff[b])[n] = w;
                 } else {
-                    P *dst = (P *)L.out + plane + ooff[b];
-                    dst[2 * n] = to_storage<P>(w.x);
-                    dst[2 * n + 1] = to_storage<P>(w.y);
+                    reinterpret_cast<cpx<P> *>((P *)L.out + plane + ooff[b])[n] = {to_storage<P>(w.x), to_storage<P>(w.y)};
                 }
             }
             __syncthreads();

@@ -19,7 +19,7 @@
 namespace ss {
 
 template <typename T>
-struct cpx {
+struct alignas(2 * sizeof(T)) cpx {  // one 8- or 16-byte access per entry
     T x, y;
 };
 
