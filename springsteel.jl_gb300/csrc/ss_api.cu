@@ -208,6 +208,15 @@ static int32_t build_grid(ss_grid *g) {
         if (v >= 13 && v <= kMaxPrimeRadix) plans.max_prime = v;
     }
     if (const char *e = std::getenv("SS_FFT_RADER")) plans.rader = std::atoi(e) != 0;
+    // Rader inner lengths with a prime factor above 67 run as zero-padded smooth
+    // convolutions (measured: 200-cell FP64 ring stages 47.6 ms unpadded, 46.0 ms
+    // padded above 67, 46.6 above 31; 400-cell binary32 81.8 ms unpadded, 80.1
+    // padded above 67)
+    plans.pad_prime = 67;
+    if (const char *e = std::getenv("SS_FFT_RADER_PAD")) {
+        const int v = std::atoi(e);
+        if (v >= 13 && v <= kMaxPrimeRadix) plans.pad_prime = v;
+    }
     // CTA size of the ring kernels: FP64 butterflies leave fewer idle threads per
     // pass at 128 (measured on the 200-cell RLZ grid: 73.4 ms per round trip
     // against 77.2 at 256); binary32 is faster at 256 (156.9 against 172.2 ms on

@@ -431,9 +431,10 @@ __device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, i
 // Radix-p pass by Rader's algorithm (p prime, first pass: Ns = 1, no input
 // twiddles) over `nb` sequences of length N, `ss` apart.  Per butterfly j
 // (NR = N/p of them) of sequence b:
-//   u_a = x_{g^a} (a < p−1) into dst[(b·NR + j)(p−1) + a] (every inner
-//   sequence p−1 apart), x_0 into dst[tail + b·NR + j];
-//   c = u ⊛ h by two (p−1)-point DFTs (inner plan) and H = DFT(h)/(p−1);
+//   u_a = x_{g^a} (a < p−1) into dst[(b·NR + j)·rM + a] (every inner
+//   sequence rM apart, zero from p−1 to rM), x_0 into dst[tail + b·NR + j];
+//   c = u ⊛ h by two rM-point DFTs (inner plan) and H = DFT_rM(h')/rM, h' = h
+//   (rM = p − 1) or h wrapped into a zero-padded length-rM sequence;
 //   X_0 = x_0 + DFT(u)_0 (into src[tail + b·NR + j]), X_{g^{−b}} = x_0 + c_b.
 // The inverse transform runs as conj(forward(conj x)).  `tail` lies beyond
 // every sequence's N outputs, so the scatter never overwrites a tail entry it
@@ -441,7 +442,7 @@ __device__ cpx<T> *stockham_plain(cpx<T> *a, cpx<T> *b, int N, const int *rad, i
 template <int SIGN, typename T>
 __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl, const void *pool, int nb, int ss,
                               int tail) {
-    const int p = pl.rp, P1 = p - 1, NR = N / p;
+    const int p = pl.rp, P1 = p - 1, NR = N / p, M = pl.rM;  // inner sequences M ≥ p − 1 apart
     const float inv_p = 1.0f / (float)p;
     const void *H = tab_at<T>(pool, pl.rH);
     const void *perm = tab_at<T>(pool, pl.rperm);  // (g^a, g^{−a}) mod p
@@ -451,21 +452,23 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
         const int q = a < P1 ? ld_index_pair<T>(perm, a).x : 0;
         cpx<T> v = src[(size_t)b * ss + j + q * NR];
         if (SIGN > 0) v.y = -v.y;
-        dst[a < P1 ? (size_t)(b * NR + j) * P1 + a : (size_t)tail + b * NR + j] = v;
+        dst[a < P1 ? (size_t)(b * NR + j) * M + a : (size_t)tail + b * NR + j] = v;
     }
-    __syncthreads();
     const int ni = nb * NR;  // inner sequences
-    cpx<T> *r1 = stockham_plain<-1, T>(dst, src, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm, pl.rpt);
-    for (UnitWalk uw_(P1); uw_.g < (ni); uw_.next()) {
+    if (M > P1)  // zero padding of each inner sequence
+        for (UnitWalk uw_(M - P1); uw_.g < ni; uw_.next()) dst[(size_t)uw_.g * M + P1 + uw_.n] = c_zero<T>();
+    __syncthreads();
+    cpx<T> *r1 = stockham_plain<-1, T>(dst, src, M, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, M, pool, pl.rpm, pl.rpt);
+    for (UnitWalk uw_(M); uw_.g < (ni); uw_.next()) {
         const int k = uw_.n, sq = uw_.g;
-        cpx<T> *u = r1 + (size_t)sq * P1 + k;
+        cpx<T> *u = r1 + (size_t)sq * M + k;
         const cpx<T> U = *u;
         if (k == 0) src[tail + sq] = c_add(dst[tail + sq], U);  // X_0 into src's tail
         *u = c_mul(U, ld_cplx<T>(H, k));
     }
     __syncthreads();
     cpx<T> *other = (r1 == dst) ? src : dst;
-    cpx<T> *r2 = stockham_plain<1, T>(r1, other, P1, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, P1, pool, pl.rpm, pl.rpt);
+    cpx<T> *r2 = stockham_plain<1, T>(r1, other, M, pl.rrad, pl.rnrad, tab_at<T>(pool, pl.rtw), ni, M, pool, pl.rpm, pl.rpt);
     cpx<T> *out = (r2 == dst) ? src : dst;
     for (UnitWalk uw_(N); uw_.g < (nb); uw_.next()) {
         const int e = uw_.n, b = uw_.g;  // scatter: (j, b'), b' = p−1 → X_0
@@ -476,7 +479,7 @@ __device__ cpx<T> *rader_pass(cpx<T> *src, cpx<T> *dst, int N, const FftPlan &pl
             X = src[(size_t)tail + b * NR + j];
             s = 0;
         } else {
-            X = c_add(dst[(size_t)tail + b * NR + j], r2[(size_t)(b * NR + j) * P1 + bb]);
+            X = c_add(dst[(size_t)tail + b * NR + j], r2[(size_t)(b * NR + j) * M + bb]);
             s = ld_index_pair<T>(perm, bb).y;
         }
         if (SIGN > 0) X.y = -X.y;
@@ -501,7 +504,8 @@ __device__ cpx<T> *stockham(cpx<T> *a, cpx<T> *b, int N, const int *rad, int nra
 
 // Sequence stride of a plan inside a CTA's ping-pong buffers: N, or M for
 // Bluestein.  A buffer holds `cap` sequences (the CTA's item batch) and, for a
-// Rader plan, a tail of cap·N/p entries after them.
+// Rader plan, cap × rader_data_len entries (sequences or inner sequences)
+// followed by a tail of cap·N/p entries.
 __host__ __device__ inline int fft_seq_stride(const FftPlan &p) { return p.blu ? p.M : p.N; }
 
 // Length-N DFTs of the nb sequences in `a` (sign SIGN), sequence i at
@@ -511,7 +515,8 @@ __host__ __device__ inline int fft_seq_stride(const FftPlan &p) { return p.blu ?
 template <int SIGN, typename T>
 __device__ cpx<T> *dft(cpx<T> *a, cpx<T> *b, const FftPlan &p, const void *pool, int nb, int cap) {
     if (!p.blu)
-        return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw), nb, p.N, &p, pool, cap * p.N);
+        return stockham<SIGN, T>(a, b, p.N, p.rad, p.nrad, tab_at<T>(pool, p.tw), nb, p.N, &p, pool,
+                                 p.rp ? cap * rader_data_len(p) : 0);
     const int N = p.N, M = p.M;
     const void *chirp = tab_at<T>(pool, p.chirp);
     const void *filt = tab_at<T>(pool, p.filt);

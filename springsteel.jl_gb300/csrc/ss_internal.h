@@ -55,10 +55,15 @@ struct FftPlan {
     // rad[], stored as p): generator g, the (p−1)-point inner plan, and
     // H = FFT_{p−1}(h)/(p−1) with h_d = W_p^{g^{−d}}
     int rp, rg;
+    // length of the cyclic convolution's inner DFTs: p − 1, or a smooth M ≥ 2p − 3
+    // when p − 1 has a prime factor above the padding limit (the convolution is
+    // then taken with u zero-padded to M and h wrapped, Rader 1968 with a
+    // zero-padded convolution)
+    int rM;
     int rnrad;
     int rrad[kMaxRadices];
-    int64_t rtw;     // pool offset of W_{p−1}^t, t < p−1
-    int64_t rH;      // pool offset of H, p−1 entries
+    int64_t rtw;     // pool offset of W_rM^t, t < rM
+    int64_t rH;      // pool offset of H, rM entries
     int64_t rperm;   // pool offset of (g^a mod p, g^{−a} mod p), a < p−1, as exact reals
     // pool offsets of the DFT matrices of the direct prime passes (radix > 13) in
     // rad[] and rrad[]; −1 for every other radix (prime_matrix_width)
@@ -189,6 +194,7 @@ struct PlanSet {
     int max_smem_cplx = 0;          // largest complex buffer (N or M)
     int max_prime = kMaxPrimeRadix; // direct prime passes up to here, Rader or Bluestein above
     bool rader = true;              // Rader passes for larger primes (else Bluestein)
+    int pad_prime = kMaxPrimeRadix; // Rader inner lengths with a prime factor above this are zero-padded
     int plan_for(int N, TwiddlePool &pool);
     int64_t unpack_for(int L, TwiddlePool &pool);
     int64_t prime_matrix(int R, TwiddlePool &pool);
@@ -196,9 +202,12 @@ struct PlanSet {
     int64_t pass_table(int N, int Ns, int R, TwiddlePool &pool);
     void pass_tables(int n, const int *rad, int nrad, int s0, int Ns0, int64_t *pt, TwiddlePool &pool);
 };
-// complex entries of one ping-pong buffer of a plan
-// complex entries of one ping-pong buffer: M (Bluestein), N + N/p (Rader: a tail
-// of N/p entries beyond the N data entries holds the x_0 terms), else N
-SS_HD inline int fft_buffer_len(const FftPlan &p) { return p.blu ? p.M : (p.rp ? p.N + p.N / p.rp : p.N); }
+// entries of a Rader plan's data region: the N sequence entries, or the N/p
+// inner sequences of rM entries when those are longer
+SS_HD inline int rader_data_len(const FftPlan &p) { return p.N / p.rp * p.rM > p.N ? p.N / p.rp * p.rM : p.N; }
+// complex entries of one ping-pong buffer per sequence: M (Bluestein); for a
+// Rader plan its data region plus a tail of N/p entries that holds the x_0
+// terms; else N
+SS_HD inline int fft_buffer_len(const FftPlan &p) { return p.blu ? p.M : (p.rp ? rader_data_len(p) + p.N / p.rp : p.N); }
 
 }  // namespace ss

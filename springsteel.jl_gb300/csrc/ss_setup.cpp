@@ -553,37 +553,64 @@ static int primitive_root(int p) {
 // Rader plan: N = p·m with p the largest prime factor, above max_prime; m and
 // p − 1 covered by direct radices.  The p-point DFTs become cyclic convolutions of length p − 1
 // (Rader, 1968): X_{g^{−b}} = x_0 + Σ_a x_{g^a} W_p^{g^{a−b}}.
-static bool rader_plan(int N, int max_prime, FftPlan &p, TwiddlePool &pool) {
-    int n = N, P = 1;
+static int largest_prime_factor(int n) {
+    int P = 1;
     for (int d = 2; d * d <= n; d++)
         while (n % d == 0) { P = std::max(P, d); n /= d; }
-    if (n > 1) P = std::max(P, n);
+    return n > 1 ? std::max(P, n) : P;
+}
+
+static bool rader_plan(int N, int max_prime, int pad_prime, FftPlan &p, TwiddlePool &pool) {
+    const int P = largest_prime_factor(N);
     if (P <= max_prime || P > 4096) return false;
     int nr = 0;
-    // the cofactor and the inner length take direct passes up to the hard limit
+    // the cofactor and the inner length take direct passes up to the hard limit;
+    // an inner length with a prime factor above pad_prime becomes a smooth
+    // M ≥ 2(P − 1) − 1 (radices 2, 3, 5, 7) carrying the zero-padded convolution
     if (!factor_radices(N / P, p.rad + 1, nr, false, kMaxPrimeRadix)) return false;
-    if (!factor_radices(P - 1, p.rrad, p.rnrad, false, kMaxPrimeRadix)) return false;
+    const int P1 = P - 1;
+    int M = P1;
+    if (largest_prime_factor(P1) > pad_prime || !factor_radices(P1, p.rrad, p.rnrad, false, kMaxPrimeRadix)) {
+        M = 2 * P1 - 1;
+        while (!factor_radices(M, p.rrad, p.rnrad, true)) M++;
+    }
     p.rad[0] = P;
     p.nrad = 1 + nr;
     p.rp = P;
+    p.rM = M;
     p.rg = primitive_root(P);
-    const int P1 = P - 1;
-    p.rtw = pool.push_table(P1, -1, P1);
-    // h_d = W_P^{g^{−d}}, H = DFT_{P−1}(h) / (P − 1) (forward sign)
-    std::vector<std::complex<double>> h(P1), root(P1);
+    p.rtw = pool.push_table(M, -1, M);
+    // h_d = W_P^{g^{−d}} (d < P − 1); padded, h'_{M−q} = h_{P−1−q} (1 ≤ q < P − 1)
+    // and zero between, so that the length-M cyclic convolution of the
+    // zero-padded u with h' equals u ⊛ h on its first P − 1 entries.
+    // H = DFT_M(h')/M (forward sign)
+    std::vector<std::complex<double>> h(M, 0.0), root(M);
     const long ginv = mod_pow(p.rg, P - 2, P);
     long e = 1;
     for (int d = 0; d < P1; d++) {
         h[d] = unit_root(e, P, -1);
         e = e * ginv % P;
     }
-    for (int t = 0; t < P1; t++) root[t] = unit_root(t, P1, -1);
-    std::vector<double> H(2 * (size_t)P1);
-    for (int k = 0; k < P1; k++) {
-        std::complex<double> acc = 0.0;
-        for (int d = 0; d < P1; d++) acc += h[d] * root[(size_t)d * k % P1];
-        H[2 * k] = acc.real() / P1;
-        H[2 * k + 1] = acc.imag() / P1;
+    if (M > P1)
+        for (int q = 1; q < P1; q++) h[M - q] = h[P1 - q];
+    for (int t = 0; t < M; t++) root[t] = unit_root(t, M, -1);
+    bool small_radices = true;  // host_stockham takes radices up to 16
+    for (int i = 0; i < p.rnrad; i++) small_radices = small_radices && p.rrad[i] <= 16;
+    std::vector<std::complex<double>> Hc(M);
+    if (small_radices) {
+        Hc = h;
+        host_stockham(Hc, p.rrad, p.rnrad, root);
+    } else {
+        for (int k = 0; k < M; k++) {
+            std::complex<double> acc = 0.0;
+            for (int d = 0; d < M; d++) acc += h[d] * root[(size_t)d * k % M];
+            Hc[k] = acc;
+        }
+    }
+    std::vector<double> H(2 * (size_t)M);
+    for (int k = 0; k < M; k++) {
+        H[2 * k] = Hc[k].real() / M;
+        H[2 * k + 1] = Hc[k].imag() / M;
     }
     p.rH = pool.push(H);
     // index permutations of the gather (g^a) and the scatter (g^{−b})
@@ -608,7 +635,7 @@ int PlanSet::plan_for(int N, TwiddlePool &pool) {
     if (factor_radices(N, p.rad, p.nrad, false, max_prime)) {
         p.blu = 0;
         p.tw = pool.push_table(N, -1, N);
-    } else if (rader && rader_plan(N, max_prime, p, pool)) {
+    } else if (rader && rader_plan(N, max_prime, pad_prime, p, pool)) {
         p.blu = 0;
         p.tw = pool.push_table(N, -1, N);
     } else {
@@ -648,7 +675,7 @@ int PlanSet::plan_for(int N, TwiddlePool &pool) {
         pass_tables(0, nullptr, 0, 0, 1, p.rpt, pool);
     } else if (p.rp) {
         pass_tables(N, p.rad, p.nrad, 1, p.rp, p.pt, pool);
-        pass_tables(p.rp - 1, p.rrad, p.rnrad, 0, 1, p.rpt, pool);
+        pass_tables(p.rM, p.rrad, p.rnrad, 0, 1, p.rpt, pool);
         pass_tables(0, nullptr, 0, 0, 1, p.mpt, pool);
     } else {
         pass_tables(N, p.rad, p.nrad, 0, 1, p.pt, pool);
