@@ -519,10 +519,11 @@ __global__ void __launch_bounds__(128) cheb_forward_tiled_kernel(ChebLaunch C) {
     const int64_t c0 = C.col0 + blk * COLS;
     const int ncol = (int)((C.col1 - c0) < COLS ? (C.col1 - c0) : COLS);
     const P *in = (const P *)C.in + (size_t)v * C.np + c0 * N;
+    // (point z, column c) walked with carries: no division per element
     if constexpr (std::is_same<P, T>::value) {
-        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) cp_async<sizeof(T)>(xs + (e / N) * ldx + (e % N), in + e);
+        for (UnitWalk u(N); u.g < ncol; u.next()) cp_async<sizeof(T)>(xs + u.g * ldx + u.n, in + u.g * N + u.n);
     } else {
-        for (int e = threadIdx.x; e < ncol * N; e += blockDim.x) xs[(e / N) * ldx + (e % N)] = to_compute<T>(in[e]);
+        for (UnitWalk u(N); u.g < ncol; u.next()) xs[u.g * ldx + u.n] = to_compute<T>(in[u.g * N + u.n]);
     }
     for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
         if (c < ncol) {
@@ -580,8 +581,8 @@ __global__ void __launch_bounds__(128) cheb_forward_tiled_kernel(ChebLaunch C) {
     }
     __syncthreads();
     T *out = (T *)C.out + (size_t)v * C.bk * C.jDim;
-    for (int e = threadIdx.x; e < bk * ncol; e += blockDim.x) {
-        const int k = e / ncol, c = e % ncol;
+    for (UnitWalk u(ncol); u.g < bk; u.next()) {  // column u.n of mode u.g
+        const int k = u.g, c = u.n;
         out[col_base[c] + (int64_t)k * col_L[c]] = os[(size_t)k * COLS + c];
     }
     __syncthreads();  // os and col_base are rewritten by the next block
@@ -761,11 +762,18 @@ __device__ __forceinline__ void store_run(P *dst, const P (&u)[TJ], bool vec) {
 // mirror u[N−1−j] leave registers as 16-byte stores covering whole sectors.
 // Summation order per output is that of cheb_inverse_m_kernel (bit-identical).
 // ====================================================================
+// Columns per block of the persistent Chebyshev inverse.  (Measured on the
+// 400-cell binary32 grid: tiles whose parity halves sit on lane pairs joined by
+// shuffles ran slower — 23.5 ms with 8 × 8 tiles over 128 columns, 21.3 ms with
+// 8 × 4 over 64 — than 4 × 4 tiles of both halves, 20.7 ms.)
+template <typename T>
+__host__ __device__ constexpr int cheb_inv_cols() { return 64; }
+
 template <typename P, typename T>
 __global__ void __launch_bounds__(128) cheb_inverse_p_kernel(ChebLaunch C) {
     // binary64 columns are short (kz = 32: JT = 4): 2-column tiles keep all 128
     // threads busy; binary32 (kz = 64: JT = 8) takes 4-column tiles
-    constexpr int COLS = 64, TJ = 4, TC = std::is_same<T, float>::value ? 4 : 2, CT = COLS / TC;
+    constexpr int COLS = cheb_inv_cols<T>(), TJ = 4, TC = std::is_same<T, float>::value ? 4 : 2, CT = COLS / TC;
     constexpr int VEC = 16 / (int)sizeof(T);  // compute-type values per 16-byte copy
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int64_t col_base[COLS / VEC];
@@ -773,7 +781,7 @@ __global__ void __launch_bounds__(128) cheb_inverse_p_kernel(ChebLaunch C) {
     const int v = blockIdx.y;
     const ChebDev &cb = C.cheb[v];
     const int N = cb.N, bk = cb.bk, half = cb.half;
-    const int JT = (half + TJ - 1) / TJ, JP = JT * TJ;
+    const int JT = (half + TJ - 1) / TJ, JP = JT * TJ;  // JP = pad4(half), the host layout
     const int nr = cb.nrank, ke = (bk + 1) / 2, ko = bk / 2, Ke = ke + nr, Ko = ko + nr;
     const int kcap = cb.kcap;
     T *ms = reinterpret_cast<T *>(smem_raw);    // [d][pe][kcap][JP]
@@ -921,7 +929,7 @@ template <typename T>
 size_t cheb_inverse_p_smem(int N, int bk) {  // rank of the Γ fold ≤ 2
     const size_t kcap = (size_t)(bk + 1) / 2 + 2, jp = (size_t)cheb_pad4((N + 1) / 2);
     const size_t kk = (size_t)(bk + 1) / 2 + bk / 2 + 4;
-    return (6 * kcap * jp + 2 * kk * 64) * sizeof(T);
+    return (6 * kcap * jp + 2 * kk * cheb_inv_cols<T>()) * sizeof(T);
 }
 
 template <typename T>
@@ -1087,7 +1095,8 @@ cudaError_t launch_cheb_inverse(const ChebLaunch &C, size_t smem, cudaStream_t s
     const size_t sp = cheb_inverse_p_smem<T>(N, C.bk);
     if (sp <= (size_t)227 * 1024) {  // the three matrices stay resident: persistent CTAs
         set_smem(cheb_inverse_p_kernel<P, T>, sp);
-        const int64_t nblk = (C.col1 - C.col0 + 63) / 64;
+        constexpr int cols = cheb_inv_cols<T>();
+        const int64_t nblk = (C.col1 - C.col0 + cols - 1) / cols;
         const int64_t want = std::max<int64_t>(1, (int64_t)resident_ctas(sp, 128) / std::max(C.nvars, 1));
         cheb_inverse_p_kernel<P, T><<<dim3((unsigned)std::min(nblk, want), C.nvars), 128, sp, st>>>(C);
         return cudaGetLastError();
