@@ -195,7 +195,7 @@ static int32_t plan_sb(ss_batch *bt, const std::vector<ss_grid *> &gs, int tl, s
         L.push_back(sb_record(g));
         const SbLaunch &S = L.back();
         for (int bz = 0; bz < g->nitems; bz++)
-            for (int by = 0; by < (S.b + 63) / 64; by++)
+            for (int by = 0; by < (S.b + kSbOut - 1) / kSbOut; by++)
                 for (int bx = 0; bx < (S.nslots_z + 31) / 32; bx++) work.push_back({i, bx, by, bz});
     }
     const void *d_recs = nullptr, *w = nullptr;

@@ -267,41 +267,68 @@ __global__ void __launch_bounds__(256, kRingMinBlocks<T>) ring_inverse_kernel(Ri
 
 // ====================================================================
 // sb_project: spectral[(zb*(1+2K) + s)*b + mi] = Σ_taps w(mi,tap) F[row][s]
-// block (32 slots, 8 rows of outputs); 64 outputs per CTA in mi
+// CTA = 32 slots × kSbOut outputs mi (8 rows of threads).  The F rows that the
+// CTA's tap windows span (mubar·(kSbOut − 1) + 4·mubar of them) are staged once
+// in shared memory with coalesced loads, zero where a ring has no such slot
+// (k > ri: the reference zero-fills); each output then reads its 4·mubar taps
+// from there.  Grids with mubar > kSbMaxMubar read F from global memory.
 // ====================================================================
 template <typename P, typename T>
 __device__ __forceinline__ void sb_project_body(const SbLaunch &S, const int bx, const int by, const int bz) {
-    __shared__ T tile[32][65];
+    constexpr int MO = kSbOut, FROWS = MO * kSbMaxMubar + 4 * kSbMaxMubar;
+    __shared__ T fs[FROWS][32];
+    __shared__ T tile[32][MO + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int s0 = bx * 32, m0 = by * 64;
+    const int s0 = bx * 32, m0 = by * MO;
     const int item = bz;
     const int v = item / S.bk, zb = item % S.bk;
     const int s = s0 + tx;
     const SplineDev &sp = S.spl[v];
     const int taps = 4 * S.mubar;
     const T *F = (const T *)S.F + (size_t)item * S.frows;
-    for (int q = 0; q < 8; q++) {
-        const int mi = m0 + ty + 8 * q;
-        T acc = T(0.0f);
-        if (mi < S.b && s < S.nslots_z) {
-            const int row0 = S.mubar * (mi - 3);
-            for (int t = 0; t < taps; t++) {
-                const int row = row0 + t;  // radial mish index (0-based ring r-1)
-                if (row < 0 || row >= S.iDim) continue;
-                const int ri = row + 1 + S.pOL;
-                if (s >= 1 + 2 * ri) continue;  // wavenumber k > ri: the reference zero-fills
-                acc = acc + ld_real<T>(sp.sbw_t, (int64_t)mi * taps + t) * F[S.fofs[row] + s];
-            }
+    if (S.mubar <= kSbMaxMubar) {
+        const int rbase = S.mubar * (m0 - 3);  // tap 0 of output m0
+        const int nrows = S.mubar * (MO - 1) + taps;
+        for (int rr = ty; rr < nrows; rr += 8) {
+            const int row = rbase + rr;  // radial mish index (0-based ring r-1)
+            T val = T(0.0f);
+            if (row >= 0 && row < S.iDim && s < S.nslots_z && s < 1 + 2 * (row + 1 + S.pOL)) val = F[S.fofs[row] + s];
+            fs[rr][tx] = val;
         }
-        tile[tx][ty + 8 * q] = acc;
+        __syncthreads();
+        for (int q = 0; q < MO / 8; q++) {
+            const int ml = ty + 8 * q, mi = m0 + ml;
+            T acc = T(0.0f);
+            if (mi < S.b) {
+                const T *f = &fs[S.mubar * ml][tx];
+                for (int t = 0; t < taps; t++) acc = acc + ld_real<T>(sp.sbw_t, (int64_t)mi * taps + t) * f[t * 32];
+            }
+            tile[tx][ml] = acc;
+        }
+    } else {
+        for (int q = 0; q < MO / 8; q++) {
+            const int mi = m0 + ty + 8 * q;
+            T acc = T(0.0f);
+            if (mi < S.b && s < S.nslots_z) {
+                const int row0 = S.mubar * (mi - 3);
+                for (int t = 0; t < taps; t++) {
+                    const int row = row0 + t;
+                    if (row < 0 || row >= S.iDim) continue;
+                    const int ri = row + 1 + S.pOL;
+                    if (s >= 1 + 2 * ri) continue;
+                    acc = acc + ld_real<T>(sp.sbw_t, (int64_t)mi * taps + t) * F[S.fofs[row] + s];
+                }
+            }
+            tile[tx][ty + 8 * q] = acc;
+        }
     }
     __syncthreads();
     P *spec = (P *)S.spec + (size_t)v * S.nspec + (size_t)zb * S.nslots_z * S.b;
     const double *fw = S.fw ? S.fw + (size_t)v * (S.K + 1) : nullptr;
     const double *cw = S.cw ? S.cw + (size_t)v * S.bk : nullptr;
     const int tid = ty * 32 + tx;
-    for (int e = tid; e < 32 * 64; e += 256) {
-        const int sl = e / 64, ml = e % 64;
+    for (int e = tid; e < 32 * MO; e += 256) {
+        const int sl = e / MO, ml = e % MO;
         const int ss = s0 + sl, mi = m0 + ml;
         if (ss < S.nslots_z && mi < S.b) {
             T val = tile[sl][ml];
@@ -1062,7 +1089,7 @@ cudaError_t launch_sa_si_fused(const SaLaunch *recs, const BatchWork *work, int 
 }
 template <typename P, typename T>
 cudaError_t launch_sb_project(const SbLaunch &S, int nitems, cudaStream_t st) {
-    dim3 grid((S.nslots_z + 31) / 32, (S.b + 63) / 64, nitems);
+    dim3 grid((S.nslots_z + 31) / 32, (S.b + kSbOut - 1) / kSbOut, nitems);
     sb_project_kernel<P, T><<<grid, dim3(32, 8), 0, st>>>(S);
     return cudaGetLastError();
 }

@@ -44,6 +44,11 @@ inline int ring_batch(size_t per_item, int nitems, int nrings, int min_ctas, int
     return (int)ib;
 }
 
+// SB projection CTA: 32 slots × kSbOut outputs; its F rows are staged in shared
+// memory for mubar ≤ kSbMaxMubar
+constexpr int kSbOut = 32;
+constexpr int kSbMaxMubar = 4;
+
 struct SbLaunch {
     const void *F;
     void *spec;
