@@ -44,8 +44,9 @@ enum {
     SS_UNSUPPORTED_BC = 4,   /* mirrors DomainError, src/Chebyshev.jl:1174 */
     SS_CUDA_ERROR = 5,
     SS_DEVICE_TIMEOUT = 6,
-    SS_NAN_DETECTED = 7,
-    SS_NOT_CONVERGED = 8,
+    SS_NAN_DETECTED = 7,     /* reserved: not returned (NaN inputs propagate, as in the reference) */
+    SS_NOT_CONVERGED = 8,    /* reserved: ss_solve reports convergence in ss_solve_stats, as the
+                                reference's Krylov backend returns its stats instead of throwing */
     SS_OUT_OF_MEMORY = 9,
     SS_NO_DEVICE = 10
 };
