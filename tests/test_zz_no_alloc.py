@@ -86,3 +86,21 @@ def test_noalloc_rejects_grids_beyond_static_scratch():
     assert st == abi.SS_BAD_SHAPE
     assert b"static scratch" in lib.ss_last_error_string()
     grid.close()
+
+
+def test_noalloc_rejects_misaligned_input():
+    # the ring kernel reads (2n, 2n+1) point pairs as one 16-byte access: the call
+    # checks the caller's pointer before launching anything
+    import torch
+
+    lib = S.load_library()
+    gp = S.SpringsteelGridParameters(geometry="RL", iMin=0.0, iMax=20.0, num_cells=20, vars={"u": 1})
+    grid = S.createGrid(gp)
+    d = grid.dims
+    d_in = torch.zeros(d["n_physical"] * d["nvars"] + 2, dtype=torch.float64, device="cuda")
+    d_out = torch.zeros(d["n_spectral"] * d["nvars"], dtype=torch.float64, device="cuda")
+    st = lib.ss_spectral_transform_noalloc(grid.handle, C.c_void_p(d_in.data_ptr() + 8),
+                                           C.c_void_p(d_out.data_ptr()), None)
+    assert st == abi.SS_BAD_ARG
+    assert b"16-byte aligned" in lib.ss_last_error_string()
+    grid.close()
