@@ -210,32 +210,31 @@ __device__ __forceinline__ void ring_inverse_body(const RingLaunch &L, const int
         __syncthreads();
         const int nvar = (d == 0) ? 3 : 1;
         for (int dl = 0; dl < nvar; dl++) {
-            // packed spectrum Zp_k = E_k + i O_k, k < N (HC2R of length L via a length-N inverse DFT)
-            for (UnitWalk uw_(N); uw_.g < (G); uw_.next()) {
-        const int k = uw_.n, g = uw_.g;
+            // packed spectrum Zp_k = E_k + i O_k, k < N (HC2R of length L via a length-N
+            // inverse DFT).  With N = 2(ri + 1) > 2·kmax, entry k ≤ N/2 sees only X_k and
+            // entry N − k only conj(X_k): for x = (iκ)^dl X_k (FIxcoefficients, κ = k)
+            // and z = x·conj(W_L^k), Zp_k = x + i z and Zp_{N−k} = conj(x) + i conj(z) —
+            // one spectrum load and one twiddle per pair
+            const int NH = N / 2;
+            for (UnitWalk uw_(NH + 1); uw_.g < (G); uw_.next()) {
+                const int k = uw_.n, g = uw_.g;
                 const cpx<T> uw = c_conj(ld_cplx<T>(L.pool, rd.utw + k));
-                // FIxcoefficients: X_k → i κ X_k (twice for ∂λλ); κ = k for index k,
-                // κ = k - N for index k + N (its signed wavenumber k + N - L)
-                const float ka = (float)k, kb = (float)(k - N);
+                const float ka = (float)k;
 #pragma unroll
                 for (int t = 0; t < kSweepSeqs; t++) {
                     const int b = g * kSweepSeqs + t;
                     if (b >= nb) break;
-                    const int kmax = kmx[b];
-                    const cpx<T> *X = Xs + (size_t)b * nk;
-                    cpx<T> xa = c_zero<T>(), xb = c_zero<T>();
-                    if (k <= kmax) xa = X[k];
-                    if (N - k <= kmax && k > 0) xb = c_conj(X[N - k]);
+                    cpx<T> x = c_zero<T>();
+                    if (k <= kmx[b]) x = Xs[(size_t)b * nk + k];
                     if (dl == 1) {
-                        xa = {scale_f(xa.y, -ka), scale_f(xa.x, ka)};
-                        xb = {scale_f(xb.y, -kb), scale_f(xb.x, kb)};
+                        x = {scale_f(x.y, -ka), scale_f(x.x, ka)};
                     } else if (dl == 2) {
-                        xa = {scale_f(scale_f(xa.x, -ka), ka), scale_f(scale_f(xa.y, -ka), ka)};
-                        xb = {scale_f(scale_f(xb.x, -kb), kb), scale_f(scale_f(xb.y, -kb), kb)};
+                        x = {scale_f(scale_f(x.x, -ka), ka), scale_f(scale_f(x.y, -ka), ka)};
                     }
-                    const cpx<T> e = c_add(xa, xb);
-                    const cpx<T> o = c_mul(c_sub(xa, xb), uw);
-                    A[(size_t)b * sq + k] = {e.x - o.y, e.y + o.x};
+                    const cpx<T> z = c_mul(x, uw);
+                    cpx<T> *Ab = A + (size_t)b * sq;
+                    Ab[k] = {x.x - z.y, x.y + z.x};
+                    if (k > 0 && k < NH) Ab[N - k] = {x.x + z.y, z.x - x.y};
                 }
             }
             __syncthreads();
