@@ -500,17 +500,17 @@ def _oracle_roundtrip(gp, slot1, threads, var_index=None):
 # round trip's launches.  Bytes per round trip.
 MEASURED_TRAFFIC = {
     ("rlz200-f64", "cheb_forward"): 1.539e9,
-    ("rlz200-f64", "ring_forward"): 0.862e9,
-    ("rlz200-f64", "sb_project"): 0.494e9,
+    ("rlz200-f64", "ring_forward"): 0.863e9,
+    ("rlz200-f64", "sb_project"): 0.493e9,
     ("rlz200-f64", "sa_si"): 1.106e9,
-    ("rlz200-f64", "ring_inverse"): 3.913e9,
-    ("rlz200-f64", "cheb_inverse"): 9.644e9,
-    ("rlz400-f32", "cheb_forward"): 9.912e9,
-    ("rlz400-f32", "ring_forward"): 6.070e9,
+    ("rlz200-f64", "ring_inverse"): 3.903e9,
+    ("rlz200-f64", "cheb_inverse"): 9.642e9,
+    ("rlz400-f32", "cheb_forward"): 9.910e9,
+    ("rlz400-f32", "ring_forward"): 6.068e9,
     ("rlz400-f32", "sb_project"): 3.279e9,
-    ("rlz400-f32", "sa_si"): 24.046e9,
-    ("rlz400-f32", "ring_inverse"): 26.527e9,
-    ("rlz400-f32", "cheb_inverse"): 64.298e9,
+    ("rlz400-f32", "sa_si"): 24.037e9,
+    ("rlz400-f32", "ring_inverse"): 26.665e9,
+    ("rlz400-f32", "cheb_inverse"): 64.088e9,
 }
 
 
