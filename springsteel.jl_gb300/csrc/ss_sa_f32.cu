@@ -33,7 +33,9 @@
 
 namespace ss {
 
-constexpr int kSaSlots = 128;  // slots (threads) per CTA
+constexpr int kSaSlots = 128;  // slots (threads) per CTA; 6 resident CTAs leave 80 registers for
+                               // the FP64 residual window (measured 18.3 ms against 19.6 ms at 8
+                               // CTAs with a binary32 window, 400-cell binary32 grid)
 constexpr int kSaChunk = 32;   // rows per shared-memory staging chunk
 constexpr int kSaBlk = 8;      // rows per prefetch block in the substitution sweeps
 
@@ -153,11 +155,13 @@ __device__ __forceinline__ void sa_si_f32_body(const SaLaunch &A, float *X, floa
         // ---- sweep 3: r = Γb − A x in FP64, window w[q] = x_{i+q−3}; FP64 forward
         //      substitution of the correction L c' = r with the FP64 factor → X
         const double *Ld = sp.L4, *Dd = sp.dinv, *Ab = sp.Aband;
-        float w[7];
+        // the window is kept in FP64: each x_j is converted once, when it enters
+        // (conversions to FP64 share the FP64 pipe with the residual's FMAs)
+        double w[7];
 #pragma unroll
         for (int q = 0; q < 7; q++) {
             const int j = q - 3;
-            w[q] = (j >= 0 && j < n) ? Yc[(size_t)j * ns] : 0.f;
+            w[q] = (j >= 0 && j < n) ? (double)Yc[(size_t)j * ns] : 0.0;
         }
         double z1 = 0.0, z2 = 0.0, z3 = 0.0;
         for (int lo = 0; lo < n; lo += kSaBlk) {
@@ -177,7 +181,7 @@ __device__ __forceinline__ void sa_si_f32_body(const SaLaunch &A, float *X, floa
                 for (int q = 0; q < 7; q++) {
                     const int j = i + q - 3;
                     if (j < 0 || j >= n) continue;
-                    acc -= __ldg(Ab + min(i, j) * 4 + abs(q - 3)) * (double)w[q];
+                    acc -= __ldg(Ab + min(i, j) * 4 + abs(q - 3)) * w[q];
                 }
                 if (i >= 3) acc -= __ldg(Ld + (i - 3) * 4 + 3) * z3;
                 if (i >= 2) acc -= __ldg(Ld + (i - 2) * 4 + 2) * z2;
@@ -187,7 +191,7 @@ __device__ __forceinline__ void sa_si_f32_body(const SaLaunch &A, float *X, floa
                 z3 = z2; z2 = z1; z1 = zi;
 #pragma unroll
                 for (int q = 0; q < 6; q++) w[q] = w[q + 1];
-                w[6] = xn[k];
+                w[6] = (double)xn[k];
             }
         }
 
@@ -267,14 +271,14 @@ __device__ __forceinline__ void sa_si_f32_body(const SaLaunch &A, float *X, floa
 }
 
 template <typename P>
-__global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_kernel(SaLaunch A, float *X, float *Y) {
+__global__ void __launch_bounds__(kSaSlots, 6) sa_si_f32_kernel(SaLaunch A, float *X, float *Y) {
     sa_si_f32_body<P>(A, X, Y, blockIdx.x, blockIdx.y);
 }
 
 // fused multi-grid launch: CTA blockIdx.x runs work[blockIdx.x]; the record
 // (with its own scratch arrays) is staged in shared memory
 template <typename P>
-__global__ void __launch_bounds__(kSaSlots, 8) sa_si_f32_fused_kernel(const SaLaunch *recs, const BatchWork *work) {
+__global__ void __launch_bounds__(kSaSlots, 6) sa_si_f32_fused_kernel(const SaLaunch *recs, const BatchWork *work) {
     __shared__ __align__(16) SaLaunch A;
     const BatchWork w = work[blockIdx.x];
     for (int i = threadIdx.x; i < (int)(sizeof(SaLaunch) / 4); i += blockDim.x)
