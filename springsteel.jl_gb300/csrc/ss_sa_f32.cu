@@ -217,7 +217,7 @@ __device__ __forceinline__ void sa_si_f32_body(const SaLaunch &A, float *X, floa
                 if (i + 3 < n) acc -= __ldg(Ld + i * 4 + 3) * c3;
                 const double ci = acc * __ldg(Dd + i);
                 c3 = c2; c2 = c1; c1 = ci;
-                const float xf = (float)((double)xv[k] + ci);
+                const float xf = xv[k] + (float)ci;  // the binary32 result: one conversion
                 if (i == n - 1) xn1 = xf;
                 if (i == n - 2) xn2 = xf;
                 if (i == 1) xs1 = xf;
