@@ -105,8 +105,10 @@ static int32_t autotune_grid(ss_grid *g, cudaStream_t st) {
 
 // ---- fused plan
 // shared-memory classes of the fused ring and SA launches: a CTA's dynamic
-// shared memory is its class's largest, so records of similar size share a launch
-static const size_t kSmemClass[] = {12 << 10, 24 << 10, 48 << 10, 72 << 10, 100 << 10, 140 << 10, 227 << 10};
+// shared memory is its class's largest, so records of similar size share a launch.
+// The top class leaves 1 KB of the 227 KB per-block limit to the kernels' static
+// shared memory (the staged launch record, per-item offsets).
+static const size_t kSmemClass[] = {12 << 10, 24 << 10, 48 << 10, 72 << 10, 100 << 10, 140 << 10, 226 << 10};
 static int smem_class(size_t b) {
     for (int c = 0; c < (int)(sizeof kSmemClass / sizeof kSmemClass[0]); c++)
         if (b <= kSmemClass[c]) return c;
@@ -144,7 +146,7 @@ static int32_t plan_rings(ss_batch *bt, const std::vector<ss_grid *> &gs, int tl
             r.L.ring_list = g->d_ring_list + bkt.offset;
             r.threads = inverse ? g->ring_threads_inv : g->ring_threads_fwd;
             const size_t per = ring_item_smem(g, bkt, inverse);
-            int ib = ring_batch(per, g->nitems, bkt.count, 1, r.threads, bkt.max_buf) * bt->ib_scale;
+            int ib = ring_batch(per, g->nitems, bkt.count, 1, r.threads, bkt.max_buf, true) * bt->ib_scale;
             ib = std::max(1, std::min({ib, kRingBatchMax, g->nitems}));
             while (ib > 1 && per * ib > kSmemClass[6]) ib--;
             r.L.ib = ib;

@@ -2,6 +2,8 @@
 // passed by value to the kernels).
 #pragma once
 
+#include <cstdlib>
+
 #include <cuda_runtime.h>
 
 #include "ss_internal.h"
@@ -26,16 +28,34 @@ struct RingLaunch {
     int ib;                    // items per CTA (≤ kRingBatchMax): one batched DFT per pass
 };
 constexpr int kRingBatchMax = 16;
-constexpr size_t kRingBatchBytes = 64 * 1024;  // shared-memory budget of one ring batch
+constexpr size_t kRingBatchBytes = 128 * 1024;  // shared-memory budget of one ring batch
 // items per CTA for a launch of `nrings` rings of buffer length ≤ `buf` complex
-// entries, needing `per_item` shared-memory bytes each: enough sequences to
-// give each of the CTA's `threads` about one butterfly per pass (batching
-// only pays off for rings shorter than the CTA), within the shared-memory
-// budget, while the launch keeps at least `min_ctas` CTAs (each bucket of
-// rings is its own launch)
-inline int ring_batch(size_t per_item, int nitems, int nrings, int min_ctas, int threads, int buf) {
-    size_t ib = kRingBatchBytes / (per_item > 0 ? per_item : 1);
-    const size_t by_work = (size_t)(2 * threads) / (size_t)(buf > 0 ? buf : 1);
+// entries, needing `per_item` shared-memory bytes each: sequences until each of
+// the CTA's `threads` has about 16 complex entries per pass, within the
+// shared-memory budget, while the launch keeps at least `min_ctas` CTAs (each
+// bucket of rings is its own launch).  Measured on the 200-cell FP64 and
+// 400-cell binary32 grids (ring_inverse + ring_forward): 42.3 / 77.6 ms at 2
+// entries and 64 KB, 42.1 / 76.6 at 4, 41.8 / 74.2 at 8 and 96 KB, 41.2 / 71.7 at
+// 16 and 128 KB (the same at 200 KB), 50.5 / 97.5 at 32 and 160 KB.
+// (tuning overrides: SS_RING_WORK entries per thread, SS_RING_BATCH_KB budget)
+// `fused`: the multi-grid batch planner, which keeps 2 entries per thread and a 64 KB
+// budget (its autotuner scales the result by 1, 2 or 4 itself).
+inline int ring_batch(size_t per_item, int nitems, int nrings, int min_ctas, int threads, int buf,
+                      bool fused = false) {
+    static const int work_env = [] {
+        const char *e = std::getenv("SS_RING_WORK");
+        const int v = e ? std::atoi(e) : 0;
+        return (v >= 1 && v <= 64) ? v : 16;
+    }();
+    static const size_t budget_env = [] {
+        const char *e = std::getenv("SS_RING_BATCH_KB");
+        const int v = e ? std::atoi(e) : 0;
+        return (v >= 16 && v <= 220) ? (size_t)v * 1024 : kRingBatchBytes;
+    }();
+    const int work = fused ? 2 : work_env;
+    const size_t budget = fused ? (size_t)64 * 1024 : budget_env;
+    size_t ib = budget / (per_item > 0 ? per_item : 1);
+    const size_t by_work = (size_t)(work * threads) / (size_t)(buf > 0 ? buf : 1);
     if (ib > by_work) ib = by_work;
     if (ib < 1) ib = 1;
     if (ib > (size_t)kRingBatchMax) ib = kRingBatchMax;
