@@ -3,21 +3,21 @@
 // The ring transforms of the reference call FFTW's R2HC/HC2R on rings of
 // L = 4+4ri points (src/Fourier.jl:192-193, 388-395, 463-468).  Ring lengths
 // have arbitrary prime factors, so a length-N complex DFT (N = L/2 after real
-// packing) is evaluated by mixed-radix Stockham autosort passes (radices
-// 4,2,3,5,7,11,13 in registers, odd primes up to the plan set's limit as
-// output-pair passes); a larger prime factor p gets one Rader pass (a
-// (p−1)-point cyclic convolution by two inner Stockham DFTs), and lengths with
-// no such plan fall back to Bluestein's chirp-z convolution of smooth length
-// M >= 2N-1.  Twiddles and index tables come from FP64-accurate tables built
-// on the host (ss_setup.cpp), stored in the compute type's layout.
+// packing) is evaluated by mixed-radix Stockham autosort passes: radices
+// 4,2,3,5,7,11,13 in registers with per-pass twiddle rows; odd primes up to the
+// plan set's limit as output-pair passes that read a per-prime DFT matrix; a
+// larger prime factor p gets one Rader pass (a (p−1)-point cyclic convolution
+// by two inner Stockham DFTs, zero-padded to a smooth length when p − 1 has a
+// large prime factor), and lengths with no such plan fall back to Bluestein's
+// chirp-z convolution of smooth length M >= 2N-1.  Twiddle rows, DFT matrices
+// and index tables come from FP64-accurate tables built on the host
+// (ss_setup.cpp), stored in the compute type's layout.
 //
 // Every routine transforms `ns` sequences of the same plan, `ss` complex
 // entries apart in shared memory, with one barrier per pass for all of them.
-// A work unit is one butterfly position of a group of IT sequences: the
-// butterfly's index arithmetic and twiddles are computed once and applied to
-// the IT sequences, and the CTA's threads walk the units (position fastest, so
-// a warp touches consecutive shared-memory entries) without a division per
-// unit.
+// The CTA's threads walk the work units (butterfly position fastest, so a warp
+// touches consecutive shared-memory entries) with carries, without a division
+// per unit.
 #pragma once
 
 #include <cuda_runtime.h>
