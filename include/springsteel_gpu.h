@@ -385,6 +385,23 @@ int32_t ss_spectral_transform_noalloc(const ss_grid *grid, const double *d_physi
 int32_t ss_grid_profile(ss_grid *grid, int32_t enable);
 int32_t ss_grid_profile_read(ss_grid *grid, double *ms, int64_t *launches);
 
+/* ---- FFT plan inspection (host only: no GPU needed) ----------------------
+ * The plan grid creation builds for the complex DFT of length n (n = L/2 of a
+ * ring of L = 4 + 4 ri points) in `precision`, with the same limits and tuning
+ * overrides (SS_FFT_MAX_PRIME, SS_FFT_RADER, SS_FFT_RADER_PAD).  kind 0: Stockham
+ * passes with radices rad[0..nrad) (odd primes above 13 as direct prime passes);
+ * 1: one Rader pass for the prime rad[0] = rader_p, then rad[1..nrad), its
+ * (p − 1)-point cyclic convolution taken by inner DFTs of length rader_inner —
+ * p − 1, or a smooth length ≥ 2p − 3 holding the zero-padded convolution — with
+ * radices inner_rad[0..inner_nrad); 2: Bluestein with a smooth length bluestein_m
+ * (radices in rad[]). */
+typedef struct {
+    int32_t n, kind, nrad, rad[24];
+    int32_t rader_p, rader_inner, inner_nrad, inner_rad[24];
+    int32_t bluestein_m, max_prime, pad_prime, _pad;
+} ss_fft_plan_info;
+int32_t ss_fft_plan(int32_t n, int32_t precision, ss_fft_plan_info *out);
+
 /* ---- elliptic solve on RL grids ------------------------------------------
  * Replaces SpringsteelProblem(grid, L*u => f; backend, preconditioner) and
  * solve / solve! (src/solver_problem.jl:311-339, :474-529; Krylov backend

@@ -118,6 +118,31 @@ static void free_grid(ss_grid *g) {
     delete g;
 }
 
+
+// FFT plan-set limits of a compute layout: direct prime passes up to 67 (FP64,
+// double-float) or 127 (binary32) and one Rader pass above.  Measured with the
+// DFT-matrix prime passes: 200-cell FP64 RLZ ring_inverse 40.6 ms at 31, 40.0 at
+// 67, 40.9 at 127, 43.8 at 199; 400-cell binary32 ring_inverse + ring_forward
+// 88.1 ms at 31, 83.9 at 67, 82.4 at 127, 83.6 at 199.  Rader inner lengths with
+// a prime factor above 67 run as zero-padded smooth convolutions (200-cell FP64
+// ring stages 47.6 ms unpadded, 46.0 ms padded above 67, 46.6 above 31; 400-cell
+// binary32 81.8 ms unpadded, 80.1 padded above 67).  Tuning overrides:
+// SS_FFT_MAX_PRIME (13-199), SS_FFT_RADER (0: Bluestein), SS_FFT_RADER_PAD.
+static void configure_plans(PlanSet &plans, int tl) {
+    plans.max_prime = (tl == TL_F32) ? 127 : 67;
+    plans.rader = true;
+    if (const char *e = std::getenv("SS_FFT_MAX_PRIME")) {
+        const int v = std::atoi(e);
+        if (v >= 13 && v <= kMaxPrimeRadix) plans.max_prime = v;
+    }
+    if (const char *e = std::getenv("SS_FFT_RADER")) plans.rader = std::atoi(e) != 0;
+    plans.pad_prime = 67;
+    if (const char *e = std::getenv("SS_FFT_RADER_PAD")) {
+        const int v = std::atoi(e);
+        if (v >= 13 && v <= kMaxPrimeRadix) plans.pad_prime = v;
+    }
+}
+
 static int32_t build_grid(ss_grid *g) {
     const ss_grid_params &p = g->p;
     const int nv = p.nvars;
@@ -195,28 +220,7 @@ static int32_t build_grid(ss_grid *g) {
     // ---- rings (src/factory.jl:608-624) and FFT plans
     TwiddlePool pool;
     PlanSet plans;
-    // direct prime passes up to 67 (FP64, double-float) or 127 (binary32) and one
-    // Rader pass above.  Measured with the DFT-matrix prime passes: 200-cell FP64
-    // RLZ ring_inverse 40.6 ms at 31, 40.0 at 67, 40.9 at 127, 43.8 at 199;
-    // 400-cell binary32 ring_inverse + ring_forward 88.1 ms at 31, 83.9 at 67,
-    // 82.4 at 127, 83.6 at 199.
-    plans.max_prime = (g->tl == TL_F32) ? 127 : 67;
-    plans.rader = true;
-    // tuning override of the direct-pass limit (odd, 13 ≤ limit ≤ 199)
-    if (const char *e = std::getenv("SS_FFT_MAX_PRIME")) {
-        const int v = std::atoi(e);
-        if (v >= 13 && v <= kMaxPrimeRadix) plans.max_prime = v;
-    }
-    if (const char *e = std::getenv("SS_FFT_RADER")) plans.rader = std::atoi(e) != 0;
-    // Rader inner lengths with a prime factor above 67 run as zero-padded smooth
-    // convolutions (measured: 200-cell FP64 ring stages 47.6 ms unpadded, 46.0 ms
-    // padded above 67, 46.6 above 31; 400-cell binary32 81.8 ms unpadded, 80.1
-    // padded above 67)
-    plans.pad_prime = 67;
-    if (const char *e = std::getenv("SS_FFT_RADER_PAD")) {
-        const int v = std::atoi(e);
-        if (v >= 13 && v <= kMaxPrimeRadix) plans.pad_prime = v;
-    }
+    configure_plans(plans, g->tl);
     // CTA size of the ring kernels: FP64 butterflies leave fewer idle threads per
     // pass at 128 (measured on the 200-cell RLZ grid: 73.4 ms per round trip
     // against 77.2 at 256); binary32 is faster at 256 (156.9 against 172.2 ms on
@@ -1128,5 +1132,39 @@ extern "C" int32_t ss_spectral_transform_noalloc(const ss_grid *g, const double 
     S.nslots_z = g->nslots_z; S.bk = 1; S.filtered = g->filtered;
     if (g->tl == TL_DF64) CUDA_TRY((launch_sb_project<double, df64>(S, g->nitems, st)));
     else CUDA_TRY((launch_sb_project<double, double>(S, g->nitems, st)));
+    return SS_OK;
+}
+
+// The FFT plan grid creation builds for a length-n ring DFT (host only).
+extern "C" int32_t ss_fft_plan(int32_t n, int32_t precision, ss_fft_plan_info *out) {
+    if (!out || n < 1 || n > (1 << 22)) { set_error("ss_fft_plan: null output or n out of range"); return SS_BAD_ARG; }
+    if (precision != SS_PREC_F64 && precision != SS_PREC_F64_FAST && precision != SS_PREC_F32_REFINED) {
+        set_error("ss_fft_plan: unknown precision %d", precision);
+        return SS_BAD_ARG;
+    }
+    const int tl = precision == SS_PREC_F32_REFINED ? TL_F32 : (precision == SS_PREC_F64_FAST ? TL_DF64 : TL_F64);
+    PlanSet plans;
+    configure_plans(plans, tl);
+    TwiddlePool pool;
+    const FftPlan &p = plans.plans[plans.plan_for(n, pool)];
+    std::memset(out, 0, sizeof *out);
+    out->n = n;
+    out->kind = p.blu ? 2 : (p.rp ? 1 : 0);
+    out->max_prime = plans.max_prime;
+    out->pad_prime = plans.pad_prime;
+    if (p.blu) {
+        out->bluestein_m = p.M;
+        out->nrad = p.mnrad;
+        for (int i = 0; i < p.mnrad; i++) out->rad[i] = p.mrad[i];
+        return SS_OK;
+    }
+    out->nrad = p.nrad;
+    for (int i = 0; i < p.nrad; i++) out->rad[i] = p.rad[i];
+    if (p.rp) {
+        out->rader_p = p.rp;
+        out->rader_inner = p.rM;
+        out->inner_nrad = p.rnrad;
+        for (int i = 0; i < p.rnrad; i++) out->inner_rad[i] = p.rrad[i];
+    }
     return SS_OK;
 }

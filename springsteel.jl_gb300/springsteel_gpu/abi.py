@@ -159,7 +159,7 @@ EXPORTED = [
     "ss_upload_physical", "ss_download_physical", "ss_upload_spectral", "ss_download_spectral",
     "ss_spectral_transform", "ss_grid_transform", "ss_spectral_transform_from_host",
     "ss_grid_transform_to_host", "ss_grid_set_filter", "ss_grid_set_ahat",
-    "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read",
+    "ss_grid_clear_ahat", "ss_grid_synchronize", "ss_grid_profile", "ss_grid_profile_read", "ss_fft_plan",
     "ss_spectral_transform_noalloc", "ss_regular_grid_transform", "ss_evaluate_unstructured", "ss_relocate_grid", "ss_spline_transform", "ss_tile_transform",
     "ss_grid_save", "ss_grid_load", "ss_grid_load_arrays", "ss_grid_archive_user",
     "ss_batch_create", "ss_batch_destroy", "ss_batch_run", "ss_batch_synchronize", "ss_batch_ring_threads", "ss_batch_fused_launches",
@@ -189,6 +189,15 @@ class ss_train_stats(C.Structure):
     _fields_ = [("epochs", C.c_int32), ("_pad", C.c_int32), ("steps", C.c_int64), ("rows", C.c_int64),
                 ("first_epoch_loss", C.c_double), ("last_epoch_loss", C.c_double), ("ms", C.c_double)]
 
+
+class ss_fft_plan_info(C.Structure):
+    _fields_ = [("n", C.c_int32), ("kind", C.c_int32), ("nrad", C.c_int32), ("rad", C.c_int32 * 24),
+                ("rader_p", C.c_int32), ("rader_inner", C.c_int32), ("inner_nrad", C.c_int32),
+                ("inner_rad", C.c_int32 * 24), ("bluestein_m", C.c_int32), ("max_prime", C.c_int32),
+                ("pad_prime", C.c_int32), ("_pad", C.c_int32)]
+
+
+FFT_DIRECT, FFT_RADER, FFT_BLUESTEIN = 0, 1, 2
 
 STAGES = ["cheb_forward", "ring_forward", "sb_project", "sa_si", "ring_inverse", "cheb_inverse"]
 
@@ -220,6 +229,7 @@ def bind(lib):
         "ss_grid_synchronize": ([vp], i32),
         "ss_grid_profile": ([vp, i32], i32),
         "ss_grid_profile_read": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)], i32),
+        "ss_fft_plan": ([i32, i32, C.POINTER(ss_fft_plan_info)], i32),
         "ss_spectral_transform_noalloc": ([vp, vp, vp, vp], i32),
         "ss_regular_grid_transform": ([vp, vp, i32, vp, i32, vp, i32, vp, vp], i32),
         "ss_spline_transform": ([vp, vp, vp], i32),
