@@ -104,3 +104,24 @@ def test_stage_models_of_the_default_workload():
     assert sb["ring_inverse"] == 8 * 5 * (3 * 22 * 360600 + 5 * 22 * 723600)
     assert sb["cheb_inverse"] == 8 * 5 * (5 * 22 * 723600 + 7 * 723600 * 32)
     assert bench._bytes_per_roundtrip(dims, 8) == 8 * 5 * (723600 * 32 * 8 + 2 * 5363666)
+
+
+def test_output_check_tolerances_and_detection():
+    import numpy as np
+
+    from springsteel_gpu.io import _params_from_json
+
+    assert set(bench.CHECK_TOLERANCE) == {"f64", "f64_fast", "f32"}
+    assert len(bench.CHECK_TOLERANCE["f32"]) == 7
+    # the check's per-slot errors on a golden fixture: zero against itself, and a
+    # perturbation of one slot (planted in a host copy) is caught by the FP64 bound
+    z = np.load(os.path.join(ROOT, "tests", "golden", "rlz4_k10_dirichlet.npz"))
+    gp = _params_from_json(json.loads(str(z["params"])))
+    phys = z["physical"]
+    errs = bench._slot_errors(lambda v, s: phys[:, v, s], phys, gp)
+    assert errs.shape == (1, 7) and np.all(errs == 0.0)
+    bad = phys.copy()
+    bad[17, 0, 5] += 1e-9 * np.max(np.abs(phys[:, 0, 5]))
+    errs = bench._slot_errors(lambda v, s: bad[:, v, s], phys, gp)
+    tol = np.broadcast_to(np.asarray(bench.CHECK_TOLERANCE["f64"], np.float64), (7,))
+    assert errs[0, 5] > tol[5] and np.all(np.delete(errs[0], 5) <= tol[:6])
